@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark of the IGA-ADS explicit heat step on GB300.
+
+Metric: DOF-updates/s of the explicit step (RHS assembly + ADS mass solve,
+FP64).  Workload (default): the 3D heat problem with quadratic B-splines on
+128^3 elements (130^3 = 2,197,000 dofs), 3-point Gauss, dt = 1e-6.  A "step"
+is one explicit time step of the whole grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload heat3d_p2_128|heat2d_p2_32|heat3d_p4_256]
+
+Our arm: inputs resident in HBM, every timed step preceded by an L2 flush
+(a 512 MiB memset, outside the step's CUDA-event interval), the steps issued
+through the C-ABI's device entry points (adsg_heat_rhs + adsg_ads_solve) on
+one stream; `e2e` times the reference-facing host entry point
+(adsg_heat_steps_host: pinned host tensor in, one step, host tensor out).
+The reference arm (--impl reference) times the CPU oracle (a C restatement
+of the reference's heat step: Galois-style element loop on all host threads,
+single-threaded ADS solve) on the same workload.
+Multi-GPU: replicas only (the single-grid step does not shard); each rank
+runs its own copy and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "iga-ads_gb300"))
+
+WORKLOADS = {
+    # name: (ndim, p, elements, dt)
+    "heat3d_p2_128": (3, 2, 128, 1e-6),
+    "heat2d_p2_32": (2, 2, 32, 1e-5),
+    "heat3d_p4_256": (3, 4, 256, 1e-6),
+}
+METRIC = "DOF-updates/s per explicit step (RHS+ADS solve, FP64, <=1e-12 rel L2)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="heat3d_p2_128", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_config(name):
+    nd, p, E, dt = WORKLOADS[name]
+    n = E + p
+    return {"workload": f"{nd}D heat, p={p}, {E}^{nd} elements ({n}^{nd} = {n ** nd} dofs), "
+                        f"{p + 1}-point Gauss, dt={dt:g}",
+            "ndim": nd, "p": p, "elements": E, "dofs": n ** nd, "dt": dt}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle: a C restatement of the reference's step)
+# ---------------------------------------------------------------------------
+def cpu_baseline(cfg, seconds_budget=20.0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+
+    nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
+    threads = os.cpu_count() or 1
+    pr = oracle.Problem([p] * nd, [E] * nd)
+    rng = np.random.default_rng(0)
+    u = rng.uniform(-1, 1, pr.size)
+    # one step first to size the sample, then as many whole steps as the budget allows
+    t0 = time.perf_counter()
+    u = pr.heat_steps(u, dt, 1, nthreads=threads)
+    t1 = time.perf_counter()
+    steps = 1
+    per = t1 - t0
+    extra = int(max(0, min(50, (seconds_budget - per) // max(per, 1e-9))))
+    if extra:
+        t0 = time.perf_counter()
+        u = pr.heat_steps(u, dt, extra, nthreads=threads)
+        t1 = time.perf_counter()
+        steps, per = extra, (t1 - t0) / extra
+    return {"value": cfg["dofs"] / per, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full step(s) of the benchmark grid; RHS on {threads} threads (element loop + "
+                      f"locked scatter), ADS solve single-threaded", "s_per_step": per}
+
+
+def run_reference(args, cfg):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    budget = 60.0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+
+    nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
+    threads = os.cpu_count() or 1
+    pr = oracle.Problem([p] * nd, [E] * nd)
+    u = np.random.default_rng(0).uniform(-1, 1, pr.size)
+    # warm-up steps (bounded), then timed steps (bounded so the run stays within minutes)
+    t_start = time.perf_counter()
+    for _ in range(min(args.warmup, 3)):
+        u = pr.heat_steps(u, dt, 1, nthreads=threads)
+    per_warm = (time.perf_counter() - t_start) / max(1, min(args.warmup, 3))
+    k = max(1, min(args.steps, int(budget // max(per_warm, 1e-9))))
+    t0 = time.perf_counter()
+    u = pr.heat_steps(u, dt, k, nthreads=threads)
+    el = time.perf_counter() - t0
+    v = cfg["dofs"] * k / el
+    line = {"metric": METRIC, "value": v, "unit": "DOF-updates/s", "n_gpus": args.gpus, "steps": k,
+            "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * el / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform field)",
+            "config": {k2: v2 for k2, v2 in cfg.items()}, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} full steps of the benchmark grid (requested {args.steps}); the CPU "
+                                       f"oracle restating the reference step, RHS on {threads} threads"},
+            "e2e": {"value": v, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def fp64_peak_tflops(torch, dev):
+    """cuBLAS DGEMM throughput (best of 5), the FP64 roof used for the roofline."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def profiled_traffic(stage):
+    """DRAM bytes per launch of a stage from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.md")
+    try:
+        for ln in open(path):
+            if ln.startswith(f"| {stage} |"):
+                return float(ln.split("|")[3].strip())
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+def run_ours(args, cfg):
+    import numpy as np
+    import torch
+
+    import ads_gb300 as ads
+    from ads_gb300 import inputs
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
+
+    dims = [ads.Dimension(p, E) for _ in range(nd)]
+    ctx = ads.Context(dims)
+    u0 = inputs.initial_field(dims, seed=rank)
+    A = torch.from_numpy(u0).to(dev)
+    B = torch.empty_like(A)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    size = ctx.size
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream(dev)
+    ctx.set_stream(stream)  # the flush, the events and our kernels share one stream
+
+    def step(prev, nxt):
+        ctx.heat_rhs(prev, nxt, dt)
+        ctx.ads_solve(nxt)
+
+    # warm-up
+    bufs = [A, B]
+    for i in range(max(args.warmup, 3)):
+        step(bufs[i % 2], bufs[(i + 1) % 2])
+    torch.cuda.synchronize()
+
+    peak_fp64 = fp64_peak_tflops(torch, dev)
+    ctx.stage_times()  # reset
+    ctx.enable_stage_timers(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(int(os.environ.get("ADSG_NVSMI_INDEX", local)))
+    sampler.start()
+    time.sleep(0.3)
+    w0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step(bufs[i % 2], bufs[(i + 1) % 2])
+            ends[i].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    stage = ctx.stage_times()
+    ctx.enable_stage_timers(False)
+    step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if world > 1:
+        t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = world * size * args.steps / (step_ms * 1e-3)
+
+    # --- e2e: the reference-facing host entry point with pinned host buffers ---
+    ctx.set_stream(None)
+    ke = min(args.steps, 200)
+    host = torch.from_numpy(u0.copy()).pin_memory()
+    hnp = host.numpy()
+    ctx.heat_steps_host(hnp, dt, 1)  # warm the host path
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        ctx.heat_steps_host(hnp, dt, 1)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * size * ke / e2e_s
+
+    # --- roofline of the dominant kernel ---
+    work = ctx.stage_work()
+    per_stage = {}
+    for name, (ms, n) in stage.items():
+        if n:
+            fl, by = work[name]
+            avg = ms / n
+            per_stage[name] = {"launches": n, "avg_us": 1e3 * avg, "share": 0.0,
+                               "gflop_per_launch": fl / 1e9, "tflops": fl / (avg * 1e-3) / 1e12,
+                               "gbs": by / (avg * 1e-3) / 1e9}
+    tot = sum(v["avg_us"] * v["launches"] for v in per_stage.values())
+    for v in per_stage.values():
+        v["share"] = v["avg_us"] * v["launches"] / tot
+    dom = max(per_stage, key=lambda k: per_stage[k]["share"])
+    d = per_stage[dom]
+    peaks = measured_peaks()
+    roof = {"bound": "fp64", "kernel": dom, "achieved": d["tflops"], "peak": peak_fp64, "unit": "TFLOP/s",
+            "frac": d["tflops"] / peak_fp64,
+            "traffic": profiled_traffic(dom),
+            "peak_source": "cuBLAS DGEMM 4096^3 measured live in bench.py (GB300 FP64 is not in "
+                           "MEASURED_PEAKS.json)",
+            "algorithmic_bytes_per_launch": work[dom][1], "hbm_gbs": d["gbs"],
+            "hbm_frac_of_measured": d["gbs"] / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None}
+    step_flops = sum(work[k][0] * per_stage[k]["launches"] for k in per_stage) / args.steps
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": step_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: L2 projection of prod sin(pi x_d) + seeded SplitMix64 noise in [-1e-2, 1e-2]",
+        "config": {**cfg, "l2": "flushed before every timed step (512 MiB memset outside the step interval)",
+                   "parallelism": f"replicas x{world}", "rhs": "factored quadrature (1D Gauss-assembled bands)"},
+        "e2e": {"value": e2e, "unit": "DOF-updates/s", "h2d_bytes_per_step": 8 * size, "d2h_bytes_per_step": 8 * size,
+                "steps": ke, "entry": "adsg_heat_steps_host"},
+        "gpu_launches": sum(v["launches"] for v in per_stage.values()),
+        "roofline": roof,
+        "stages": per_stage,
+        "step_tflops": step_flops / (step_ms / args.steps * 1e-3) / 1e12,
+        "clocks": clocks,
+        "wall_s": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cfg)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    cfg = workload_config(args.workload)
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,332 @@
+"""Python mirror of the IGA-ADS explicit-step API over the GB300 C-ABI.
+
+The names follow the reference (marcinlos/iga-ads): a :class:`Dimension`
+holds what ``ads::dimension`` holds (include/ads/simulation/dimension.hpp:20-59),
+:func:`ads_solve` is ``ads::ads_solve`` (include/ads/solver.hpp:222-226),
+:class:`Heat` runs ``heat_3d``'s step (examples/heat/heat_3d.hpp:39-67) and
+:func:`dgbtrs` is the LAPACK call the reference makes for every direction
+(include/ads/lin/band_solve.hpp:20-31).  Every call goes through
+``libads_gb300.so`` (include/ads_gb300.h); there is no CPU fallback: if the
+library or a GPU is missing, the calls raise.
+
+Device buffers may be given as ``torch`` CUDA tensors (float64, contiguous)
+or as raw integer device addresses; host buffers are ``numpy`` float64 arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libads_gb300.so")
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+class AdsError(RuntimeError):
+    """A non-zero status from the C-ABI (message from adsg_last_error)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"ads_gb300 error {code}: {message}")
+        self.code = code
+
+
+class DimDesc(ctypes.Structure):
+    """adsg_dim_desc (include/ads_gb300.h)."""
+
+    _fields_ = [
+        ("p", ctypes.c_int),
+        ("elements", ctypes.c_int),
+        ("quad_order", ctypes.c_int),
+        ("n", ctypes.c_int),
+        ("btab", _c_double_p),
+        ("w", _c_double_p),
+        ("J", _c_double_p),
+        ("first_dofs", _c_int_p),
+        ("kl", ctypes.c_int),
+        ("ku", ctypes.c_int),
+        ("ldab", ctypes.c_int),
+        ("lu", _c_double_p),
+        ("ipiv", _c_int_p),
+    ]
+
+
+_lib = None
+
+
+def library() -> ctypes.CDLL:
+    """Load libads_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python iga-ads_gb300/build.py` "
+            "(or __graft_entry__.build()); there is no CPU fallback")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    sig = {
+        "adsg_dim_create": (i, [i, i, d, d, i, ctypes.POINTER(vp)]),
+        "adsg_dim_destroy": (None, [vp]),
+        "adsg_dim_describe": (i, [vp, ctypes.POINTER(DimDesc)]),
+        "adsg_dim_fix_dof": (i, [vp, i]),
+        "adsg_dim_form_band": (i, [vp, i, _c_double_p]),
+        "adsg_ctx_create": (i, [i, ctypes.POINTER(DimDesc), ctypes.POINTER(vp)]),
+        "adsg_ctx_destroy": (i, [vp]),
+        "adsg_ctx_size": (ll, [vp]),
+        "adsg_ctx_set_stream": (i, [vp, vp]),
+        "adsg_ctx_synchronize": (i, [vp]),
+        "adsg_last_error": (ctypes.c_char_p, []),
+        "adsg_heat_rhs": (i, [vp, vp, vp, d]),
+        "adsg_heat_rhs_elem": (i, [vp, vp, vp, vp, d]),
+        "adsg_ads_solve": (i, [vp, vp, vp]),
+        "adsg_ads_solve_t": (i, [vp, vp]),
+        "adsg_heat_steps": (i, [vp, vp, d, i]),
+        "adsg_heat_steps_host": (i, [vp, _c_double_p, d, i]),
+        "adsg_ads_solve_host": (i, [vp, _c_double_p]),
+        "adsg_heat_rhs_host": (i, [vp, _c_double_p, _c_double_p, d]),
+        "adsg_ctx_enable_stage_timers": (i, [vp, i]),
+        "adsg_ctx_stage_times": (i, [vp, _c_double_p, ctypes.POINTER(ctypes.c_longlong)]),
+        "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
+        "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
+                             _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        msg = library().adsg_last_error()
+        raise AdsError(code, msg.decode() if msg else "")
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_c_double_p)
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(_c_int_p)
+
+
+def _devptr(x) -> int:
+    """Device address of a torch CUDA float64 tensor (or an int address)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if getattr(x, "is_cuda", False):
+        if str(x.dtype) != "torch.float64":
+            raise TypeError("device tensors must be float64")
+        if not x.is_contiguous():
+            raise ValueError("device tensors must be contiguous")
+        return x.data_ptr()
+    raise TypeError(f"expected a CUDA tensor or a device address, got {type(x)!r}")
+
+
+def _host(a: np.ndarray) -> np.ndarray:
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+        raise TypeError("host buffers must be C-contiguous float64 numpy arrays")
+    return a
+
+
+NSTAGES = 7
+STAGES = ("rhs_outer", "rhs_middle", "rhs_x", "solve_x", "solve_y", "solve_z", "rhs_elem")
+
+
+class Dimension:
+    """One dimension: open uniform B-spline basis on [a, b], its Gauss tables,
+    its mass matrix and that matrix's pivoted band LU (ads::dimension with
+    derivatives = 1 after factorize_matrix())."""
+
+    def __init__(self, p: int, elements: int, a: float = 0.0, b: float = 1.0, quad_order: int = 0):
+        lib = library()
+        h = ctypes.c_void_p()
+        _check(lib.adsg_dim_create(p, elements, a, b, quad_order, ctypes.byref(h)))
+        self._h = h
+        self._desc = DimDesc()
+        _check(lib.adsg_dim_describe(h, ctypes.byref(self._desc)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.adsg_dim_destroy(h)
+            self._h = None
+
+    @property
+    def p(self) -> int:
+        return self._desc.p
+
+    @property
+    def elements(self) -> int:
+        return self._desc.elements
+
+    def dofs(self) -> int:
+        return self._desc.n
+
+    @property
+    def quad_order(self) -> int:
+        return self._desc.quad_order
+
+    def descriptor(self) -> DimDesc:
+        return self._desc
+
+    def fix_dof(self, k: int) -> None:
+        """dimension::fix_dof: identity row k of M (affects the solve only)."""
+        _check(library().adsg_dim_fix_dof(self._h, k))
+        _check(library().adsg_dim_describe(self._h, ctypes.byref(self._desc)))
+
+    def fix_left(self) -> None:
+        self.fix_dof(0)
+
+    def fix_right(self) -> None:
+        self.fix_dof(self.dofs() - 1)
+
+    def form_band(self, which: int) -> np.ndarray:
+        """Mass (0) or stiffness (1) band, LAPACK layout kl = ku = p, shape (n, 3p+1)."""
+        ldab = 3 * self.p + 1
+        out = np.zeros(ldab * self.dofs())
+        _check(library().adsg_dim_form_band(self._h, which, _dptr(out)))
+        return out.reshape(self.dofs(), ldab)
+
+    def tables(self) -> dict:
+        """Copies of the basis_data-like tables and the factorised band."""
+        d = self._desc
+        nb = d.elements * d.quad_order * 2 * (d.p + 1)
+        return {
+            "btab": np.ctypeslib.as_array(d.btab, (nb,)).copy(),
+            "w": np.ctypeslib.as_array(d.w, (d.quad_order,)).copy(),
+            "J": np.ctypeslib.as_array(d.J, (d.elements,)).copy(),
+            "first_dofs": np.ctypeslib.as_array(d.first_dofs, (d.elements,)).copy(),
+            "lu": np.ctypeslib.as_array(d.lu, (d.ldab * d.n,)).copy(),
+            "ipiv": np.ctypeslib.as_array(d.ipiv, (d.n,)).copy(),
+            "kl": d.kl,
+            "ku": d.ku,
+            "ldab": d.ldab,
+        }
+
+
+class Context:
+    """Device-side state for a 1-3D tensor-product space (adsg_ctx)."""
+
+    def __init__(self, dims: Sequence[Dimension]):
+        lib = library()
+        arr = (DimDesc * len(dims))(*[d.descriptor() for d in dims])
+        h = ctypes.c_void_p()
+        _check(lib.adsg_ctx_create(len(dims), arr, ctypes.byref(h)))
+        self._h = h
+        self.dims = list(dims)
+        self.shape = tuple(d.dofs() for d in dims)  # (nx, ny, nz): x fastest in memory
+        self.size = int(lib.adsg_ctx_size(h))
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.adsg_ctx_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream) -> None:
+        """Enqueue on a cudaStream_t (int handle, torch.cuda.Stream or None)."""
+        if stream is not None and not isinstance(stream, int):
+            stream = stream.cuda_stream
+        _check(library().adsg_ctx_set_stream(self._h, stream))
+
+    def synchronize(self) -> None:
+        _check(library().adsg_ctx_synchronize(self._h))
+
+    # --- stage timers -----------------------------------------------------
+    def enable_stage_timers(self, on: bool = True) -> None:
+        _check(library().adsg_ctx_enable_stage_timers(self._h, 1 if on else 0))
+
+    def stage_times(self) -> dict:
+        """{stage: (total_ms, launches)} accumulated since the last call (synchronises)."""
+        ms = np.zeros(NSTAGES)
+        n = (ctypes.c_longlong * NSTAGES)()
+        _check(library().adsg_ctx_stage_times(self._h, _dptr(ms), n))
+        return {STAGES[i]: (float(ms[i]), int(n[i])) for i in range(NSTAGES)}
+
+    def stage_work(self) -> dict:
+        """{stage: (fp64_flops, hbm_bytes)} of one launch of each stage."""
+        f = np.zeros(NSTAGES)
+        b = np.zeros(NSTAGES)
+        _check(library().adsg_ctx_stage_work(self._h, _dptr(f), _dptr(b)))
+        return {STAGES[i]: (float(f[i]), float(b[i])) for i in range(NSTAGES)}
+
+    # --- device-buffer entry points -------------------------------------
+    def heat_rhs(self, u_prev, rhs, dt: float) -> None:
+        _check(library().adsg_heat_rhs(self._h, _devptr(u_prev), _devptr(rhs), float(dt)))
+
+    def heat_rhs_elem(self, u_prev, rhs, dt: float, kappa=None) -> None:
+        _check(library().adsg_heat_rhs_elem(self._h, _devptr(u_prev), _devptr(kappa), _devptr(rhs), float(dt)))
+
+    def ads_solve(self, rhs, buf=None) -> None:
+        _check(library().adsg_ads_solve(self._h, _devptr(rhs), _devptr(buf)))
+
+    def ads_solve_t(self, rhs) -> None:
+        _check(library().adsg_ads_solve_t(self._h, _devptr(rhs)))
+
+    def heat_steps(self, u, dt: float, nsteps: int) -> None:
+        _check(library().adsg_heat_steps(self._h, _devptr(u), float(dt), int(nsteps)))
+
+    # --- host-buffer entry points ---------------------------------------
+    def heat_steps_host(self, u: np.ndarray, dt: float, nsteps: int) -> None:
+        _check(library().adsg_heat_steps_host(self._h, _dptr(_host(u)), float(dt), int(nsteps)))
+
+    def ads_solve_host(self, rhs: np.ndarray) -> None:
+        _check(library().adsg_ads_solve_host(self._h, _dptr(_host(rhs))))
+
+    def heat_rhs_host(self, u_prev: np.ndarray, rhs: np.ndarray, dt: float) -> None:
+        _check(library().adsg_heat_rhs_host(self._h, _dptr(_host(u_prev)), _dptr(_host(rhs)), float(dt)))
+
+
+class Heat:
+    """heat_3d / heat_2d of the reference on the GPU: a state u and step(), with
+    p, elements and dt as in the examples' dim_config / timesteps_config."""
+
+    def __init__(self, ndim: int, p: int, elements: int, dt: float):
+        self.dims = [Dimension(p, elements) for _ in range(ndim)]
+        self.ctx = Context(self.dims)
+        self.dt = dt
+
+    def run_host(self, u: np.ndarray, steps: int) -> None:
+        self.ctx.heat_steps_host(u, self.dt, steps)
+
+
+def ads_solve(ctx: Context, rhs, buf=None) -> None:
+    """ads::ads_solve(rhs, buf, dims...) on a device tensor; the solution is left in rhs."""
+    ctx.ads_solve(rhs, buf)
+
+
+def dgbtrs(trans: str, n: int, kl: int, ku: int, nrhs: int, ab: np.ndarray, ldab: int,
+           ipiv: np.ndarray, b: np.ndarray, ldb: int) -> int:
+    """LAPACK dgbtrs_ with the same arguments (host arrays, column-major b), solved
+    on the GPU through adsg_dgbtrs_.  Returns info (0 or -k for argument k)."""
+    ab = np.ascontiguousarray(ab, dtype=np.float64)
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    _host(b)
+    info = ctypes.c_int(0)
+    ints = [ctypes.c_int(v) for v in (n, kl, ku, nrhs, ldab, ldb)]
+    code = library().adsg_dgbtrs_(trans.encode(), ctypes.byref(ints[0]), ctypes.byref(ints[1]),
+                                  ctypes.byref(ints[2]), ctypes.byref(ints[3]), _dptr(ab), ctypes.byref(ints[4]),
+                                  _iptr(ipiv), _dptr(b), ctypes.byref(ints[5]), ctypes.byref(info))
+    if code > 0:
+        _check(code)
+    return info.value
+
+
+__all__ = ["AdsError", "Context", "DimDesc", "Dimension", "Heat", "ads_solve", "dgbtrs", "library", "LIB_PATH"]

@@ -1,0 +1,701 @@
+// C-ABI of the engine: contexts, device tables, the heat RHS, the ADS solve,
+// the graph-replayed step loop and the LAPACK-compatible dgbtrs_.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "adsg_internal.hpp"
+#include "adsg_kernels.cuh"
+
+namespace adsg {
+
+static thread_local std::string g_last_error = "no error";
+
+int fail(int code, const char* msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int fail_cuda(int err, const char* where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(static_cast<cudaError_t>(err));
+    return ADSG_ERR_CUDA;
+}
+
+}  // namespace adsg
+
+using namespace adsg;
+
+#define ADSG_CUDA_TRY(expr, where)                          \
+    do {                                                    \
+        cudaError_t e_ = (expr);                            \
+        if (e_ != cudaSuccess) return fail_cuda(e_, where); \
+    } while (0)
+
+namespace {
+
+// Device allocations of one context, freed together.
+struct dev_arena {
+    std::vector<void*> blocks;
+    ~dev_arena() {
+        for (void* p : blocks) cudaFree(p);
+    }
+    template <typename T>
+    cudaError_t alloc(T** out, size_t count) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        blocks.push_back(p);
+        *out = static_cast<T*>(p);
+        return cudaSuccess;
+    }
+    template <typename T>
+    cudaError_t upload(T** out, const T* src, size_t count, cudaStream_t s) {
+        cudaError_t e = alloc(out, count);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpyAsync(*out, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+};
+
+// Row-format band (n rows x (2p+1)) of sum_e sum_q B_a B_b w_q J_e with the
+// basis values (which = 0) or derivatives (which = 1) of a descriptor.
+std::vector<double> row_band(const adsg_dim_desc& d, int which) {
+    const int p = d.p, bw = 2 * p + 1;
+    std::vector<double> rows(static_cast<size_t>(d.n) * bw, 0.0);
+    for (int e = 0; e < d.elements; ++e) {
+        const int f = d.first_dofs[e];
+        for (int k = 0; k < d.quad_order; ++k) {
+            const double* v = d.btab + ((static_cast<size_t>(e) * d.quad_order + k) * 2 + which) * (p + 1);
+            for (int a = 0; a <= p; ++a)
+                for (int b = 0; b <= p; ++b) rows[static_cast<size_t>(f + a) * bw + (b - a + p)] += v[a] * v[b] * d.w[k] * d.J[e];
+        }
+    }
+    return rows;
+}
+
+bool valid_desc(const adsg_dim_desc& d) {
+    if (d.p < 1 || d.p > ADSG_MAX_DEGREE || d.elements < 1 || d.quad_order < 1 || d.n < 1) return false;
+    if (!d.btab || !d.w || !d.J || !d.first_dofs || !d.lu || !d.ipiv) return false;
+    if (d.kl < 0 || d.ku < 0 || d.ldab < 2 * d.kl + d.ku + 1) return false;
+    if (d.kl > 16 || d.kl + d.ku > 32) return false;
+    for (int e = 0; e < d.elements; ++e)
+        if (d.first_dofs[e] < 0 || d.first_dofs[e] + d.p >= d.n) return false;
+    for (int j = 0; j < d.n; ++j)
+        if (d.ipiv[j] < j + 1 || d.ipiv[j] > std::min(d.n, j + 1 + d.kl)) return false;
+    return true;
+}
+
+// Solve tables extracted from a dgbtrf band.
+struct solve_tables {
+    std::vector<double> lmul, ucol, rdiag;
+    std::vector<int> piv, uext;
+    int kl = 0, w = 0;
+};
+
+int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t) {
+    const int kv = kl + ku;
+    t.kl = std::max(kl, 1);
+    t.w = std::max(kv, 1);
+    t.lmul.assign(static_cast<size_t>(n) * t.kl, 0.0);
+    t.ucol.assign(static_cast<size_t>(n) * t.w, 0.0);
+    t.rdiag.assign(n, 0.0);
+    t.piv.assign(n, 0);
+    t.uext.assign(n, 0);
+    for (int j = 0; j < n; ++j) {
+        const double* col = ab + static_cast<size_t>(j) * ldab;
+        const double diag = col[kv];
+        if (diag == 0.0) return j + 1;
+        t.rdiag[j] = 1.0 / diag;
+        t.piv[j] = ipiv[j] - 1;
+        for (int i = 1; i <= kl && j + i < n; ++i) t.lmul[static_cast<size_t>(j) * t.kl + i - 1] = col[kv + i];
+        int ext = 0;
+        for (int d = 1; d <= kv && d <= j; ++d) {
+            const double u = col[kv - d];
+            t.ucol[static_cast<size_t>(j) * t.w + d - 1] = u;
+            if (u != 0.0) ext = d;
+        }
+        t.uext[j] = ext;
+    }
+    return 0;
+}
+
+}  // namespace
+
+struct adsg_ctx {
+    int ndim = 0;
+    int n[3] = {1, 1, 1};
+    long long size = 0;
+    dim_dev dims[3];
+    double* nrow[3] = {nullptr, nullptr, nullptr};
+    double* kdt[3] = {nullptr, nullptr, nullptr};
+    double band_dt = std::nan("");
+    double* scratch[4] = {nullptr, nullptr, nullptr, nullptr};
+    double* ping = nullptr;  // second state buffer of the step loop
+    double uext_sum[3] = {0, 0, 0};  // sum over columns of the applied U extents
+    double* host_io = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    dev_arena arena;
+    // graph of two steps u -> ping -> u, specialised on (u, dt)
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = std::nan("");
+    double* graph_u = nullptr;
+    // stage timers
+    bool timing = false;
+    bool capturing = false;
+    struct timed { int stage; cudaEvent_t a, b; };
+    std::vector<timed> pending;
+    std::vector<cudaEvent_t> spare;
+    double stage_ms[ADSG_NSTAGES] = {};
+    long long stage_launches[ADSG_NSTAGES] = {};
+
+    cudaEvent_t take_event() {
+        if (!spare.empty()) {
+            cudaEvent_t e = spare.back();
+            spare.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void drain() {
+        for (auto& t : pending) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
+                stage_ms[t.stage] += ms;
+                stage_launches[t.stage] += 1;
+            }
+            spare.push_back(t.a);
+            spare.push_back(t.b);
+        }
+        pending.clear();
+    }
+
+    ~adsg_ctx() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto& t : pending) {
+            cudaEventDestroy(t.a);
+            cudaEventDestroy(t.b);
+        }
+        for (auto e : spare) cudaEventDestroy(e);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+// Brackets one kernel launch with timer events when timers are on.
+struct stage_scope {
+    adsg_ctx* c;
+    int stage;
+    cudaEvent_t a = nullptr;
+    stage_scope(adsg_ctx* ctx, int st) : c(ctx), stage(st) {
+        if (c->timing && !c->capturing) {
+            a = c->take_event();
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~stage_scope() {
+        if (a) {
+            cudaEvent_t b = c->take_event();
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({stage, a, b});
+        }
+    }
+};
+
+namespace {
+
+int ensure_dt_bands(adsg_ctx* c, double dt) {
+    if (c->band_dt == dt) return 0;
+    for (int d = 0; d < c->ndim; ++d) {
+        ADSG_CUDA_TRY(launch_dt_bands(c->dims[d], dt, c->nrow[d], c->kdt[d], c->stream), "dt bands");
+        c->dims[d].nrow = c->nrow[d];
+        c->dims[d].kdt = c->kdt[d];
+    }
+    c->band_dt = dt;
+    return 0;
+}
+
+// rhs = (M(x)M(x)M - dt (K(x)M(x)M + M(x)K(x)M + M(x)M(x)K)) u_prev as a sequence of
+// band passes along z, y, x (3D), y, x (2D) or x (1D).
+int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) {
+    int st = ensure_dt_bands(c, dt);
+    if (st) return st;
+    const long long total = c->size;
+    const dim_dev* D = c->dims;
+    cudaStream_t s = c->stream;
+    double** T = c->scratch;
+    if (c->ndim == 1) {
+        stage_scope sc(c, ADSG_STAGE_RHS_X);
+        ADSG_CUDA_TRY(launch_band_pass(D[0].p, u, nullptr, rhs, nullptr, D[0].nrow, nullptr, nullptr, D[0].n, 1,
+                                       total, s),
+                      "rhs pass x");
+    } else if (c->ndim == 2) {
+        const long long sy = c->n[0];
+        // A = My u, C = Ny u
+        stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
+        ADSG_CUDA_TRY(launch_band_pass(D[1].p, u, nullptr, T[0], T[1], D[1].mrow, nullptr, D[1].nrow, D[1].n, sy,
+                                       total, s),
+                      "rhs pass y");
+        // rhs = (-dt Kx) A + Mx C
+        stage_scope s2(c, ADSG_STAGE_RHS_X);
+        ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[0], T[1], rhs, nullptr, D[0].kdt, D[0].mrow, nullptr, D[0].n, 1,
+                                       total, s),
+                      "rhs pass x");
+    } else {
+        const long long sy = c->n[0], sz = static_cast<long long>(c->n[0]) * c->n[1];
+        // A = Mz u, C = Nz u
+        { stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
+        ADSG_CUDA_TRY(launch_band_pass(D[2].p, u, nullptr, T[0], T[1], D[2].mrow, nullptr, D[2].nrow, D[2].n, sz,
+                                       total, s),
+                      "rhs pass z"); }
+        // F = (-dt Ky) A + My C,  G = My A
+        { stage_scope s2(c, ADSG_STAGE_RHS_MIDDLE);
+        ADSG_CUDA_TRY(launch_band_pass(D[1].p, T[0], T[1], T[2], T[3], D[1].kdt, D[1].mrow, D[1].mrow, D[1].n, sy,
+                                       total, s),
+                      "rhs pass y"); }
+        // rhs = (-dt Kx) G + Mx F
+        stage_scope s3(c, ADSG_STAGE_RHS_X);
+        ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[3], T[2], rhs, nullptr, D[0].kdt, D[0].mrow, nullptr, D[0].n, 1,
+                                       total, s),
+                      "rhs pass x");
+    }
+    return 0;
+}
+
+int enqueue_solve(adsg_ctx* c, double* x, int trans) {
+    for (int d = 0; d < c->ndim; ++d) {
+        line_layout L = make_line_layout(c->n, c->ndim, d);
+        stage_scope sc(c, ADSG_STAGE_SOLVE_X + d);
+        ADSG_CUDA_TRY(launch_line_solve(x, c->dims[d], L, trans, c->stream), "line solve");
+    }
+    return 0;
+}
+
+int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
+    int st = enqueue_rhs(c, prev, next, dt);
+    if (st) return st;
+    return enqueue_solve(c, next, 0);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* adsg_last_error(void) { return g_last_error.c_str(); }
+
+int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
+    if (ndim < 1 || ndim > 3) return fail(-1, "ndim must be 1, 2 or 3");
+    if (!dims) return fail(-2, "dims is NULL");
+    if (!out) return fail(-3, "out is NULL");
+    *out = nullptr;
+    for (int d = 0; d < ndim; ++d)
+        if (!valid_desc(dims[d])) return fail(-2, "invalid dimension descriptor");
+    auto* c = new (std::nothrow) adsg_ctx;
+    if (!c) return fail(ADSG_ERR_NOMEM, "host allocation failed");
+    c->ndim = ndim;
+    c->size = 1;
+    for (int d = 0; d < ndim; ++d) {
+        c->n[d] = dims[d].n;
+        c->size *= dims[d].n;
+    }
+    if (c->size >= (1LL << 31)) {
+        delete c;
+        return fail(-2, "tensor larger than 2^31 dofs");
+    }
+    for (int d = 0; d < ndim; ++d) {
+        if (line_solve_smem_per_warp(dims[d].n) > 220 * 1024) {
+            delete c;
+            return fail(ADSG_ERR_UNSUPPORTED, "more than 850 dofs along one dimension");
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail_cuda(e, "cudaStreamCreate");
+    }
+    c->own_stream = true;
+
+    auto bail = [&](cudaError_t err, const char* where) {
+        int r = fail_cuda(err, where);
+        delete c;
+        return r;
+    };
+    for (int d = 0; d < ndim; ++d) {
+        const adsg_dim_desc& h = dims[d];
+        dim_dev& D = c->dims[d];
+        D.n = h.n;
+        D.p = h.p;
+        D.elements = h.elements;
+        D.q = h.quad_order;
+        solve_tables t;
+        if (make_solve_tables(h.n, h.kl, h.ku, h.ldab, h.lu, h.ipiv, t)) {
+            delete c;
+            return fail(ADSG_ERR_SINGULAR, "zero diagonal in the factorised band");
+        }
+        D.kl = t.kl;
+        D.w = t.w;
+        for (int v : t.uext) c->uext_sum[d] += v;
+        const std::vector<double> m = row_band(h, 0);
+        const std::vector<double> k = row_band(h, 1);
+        const size_t nb = static_cast<size_t>(h.elements) * h.quad_order * 2 * (h.p + 1);
+        double *mrow = nullptr, *krow = nullptr, *lmul = nullptr, *ucol = nullptr, *rdiag = nullptr;
+        double *btab = nullptr, *wq = nullptr, *jac = nullptr;
+        int *piv = nullptr, *uext = nullptr, *first = nullptr;
+        dev_arena& A = c->arena;
+        cudaStream_t s = c->stream;
+        e = A.upload(&mrow, m.data(), m.size(), s);
+        if (e == cudaSuccess) e = A.upload(&krow, k.data(), k.size(), s);
+        if (e == cudaSuccess) e = A.alloc(&c->nrow[d], m.size());
+        if (e == cudaSuccess) e = A.alloc(&c->kdt[d], m.size());
+        if (e == cudaSuccess) e = A.upload(&lmul, t.lmul.data(), t.lmul.size(), s);
+        if (e == cudaSuccess) e = A.upload(&ucol, t.ucol.data(), t.ucol.size(), s);
+        if (e == cudaSuccess) e = A.upload(&rdiag, t.rdiag.data(), t.rdiag.size(), s);
+        if (e == cudaSuccess) e = A.upload(&piv, t.piv.data(), t.piv.size(), s);
+        if (e == cudaSuccess) e = A.upload(&uext, t.uext.data(), t.uext.size(), s);
+        if (e == cudaSuccess) e = A.upload(&btab, h.btab, nb, s);
+        if (e == cudaSuccess) e = A.upload(&wq, h.w, h.quad_order, s);
+        if (e == cudaSuccess) e = A.upload(&jac, h.J, h.elements, s);
+        if (e == cudaSuccess) e = A.upload(&first, h.first_dofs, h.elements, s);
+        // the host staging vectors above die at the end of this iteration
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return bail(e, "set-up upload");
+        D.mrow = mrow;
+        D.krow = krow;
+        D.lmul = lmul;
+        D.ucol = ucol;
+        D.rdiag = rdiag;
+        D.piv = piv;
+        D.uext = uext;
+        D.btab = btab;
+        D.wq = wq;
+        D.jac = jac;
+        D.first = first;
+    }
+    const int nscratch = ndim == 3 ? 4 : (ndim == 2 ? 2 : 0);
+    for (int i = 0; i < nscratch; ++i)
+        if ((e = c->arena.alloc(&c->scratch[i], c->size)) != cudaSuccess) return bail(e, "scratch alloc");
+    if ((e = c->arena.alloc(&c->ping, c->size)) != cudaSuccess) return bail(e, "state alloc");
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return bail(e, "set-up copies");
+    *out = c;
+    return 0;
+}
+
+int adsg_ctx_destroy(adsg_ctx* ctx) {
+    if (!ctx) return 0;
+    cudaStreamSynchronize(ctx->stream);
+    delete ctx;
+    return 0;
+}
+
+long long adsg_ctx_size(const adsg_ctx* ctx) { return ctx ? ctx->size : 0; }
+
+int adsg_ctx_set_stream(adsg_ctx* ctx, void* cuda_stream) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    if (ctx->own_stream) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+        ctx->own_stream = false;
+        ctx->stream = nullptr;
+    }
+    if (cuda_stream) {
+        ctx->stream = static_cast<cudaStream_t>(cuda_stream);
+    } else {
+        ADSG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamDefault), "cudaStreamCreate");
+        ctx->own_stream = true;
+    }
+    return 0;
+}
+
+int adsg_ctx_synchronize(adsg_ctx* ctx) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    return 0;
+}
+
+int adsg_heat_rhs(adsg_ctx* ctx, const double* u_prev_dev, double* rhs_dev, double dt) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_prev_dev) return fail(-2, "u_prev is NULL");
+    if (!rhs_dev) return fail(-3, "rhs is NULL");
+    if (u_prev_dev == rhs_dev) return fail(-3, "rhs must not alias u_prev");
+    if (!std::isfinite(dt)) return fail(-4, "dt must be finite");
+    return enqueue_rhs(ctx, u_prev_dev, rhs_dev, dt);
+}
+
+int adsg_heat_rhs_elem(adsg_ctx* ctx, const double* u_prev_dev, const double* kappa_dev, double* rhs_dev,
+                       double dt) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_prev_dev) return fail(-2, "u_prev is NULL");
+    if (!rhs_dev) return fail(-4, "rhs is NULL");
+    if (u_prev_dev == rhs_dev || kappa_dev == rhs_dev) return fail(-4, "rhs must not alias an input");
+    if (!std::isfinite(dt)) return fail(-5, "dt must be finite");
+    ADSG_CUDA_TRY(cudaMemsetAsync(rhs_dev, 0, sizeof(double) * ctx->size, ctx->stream), "memset rhs");
+    stage_scope sc(ctx, ADSG_STAGE_RHS_ELEM);
+    ADSG_CUDA_TRY(launch_rhs_elem(ctx->ndim, ctx->dims, u_prev_dev, kappa_dev, rhs_dev, dt, ctx->stream),
+                  "element rhs");
+    return 0;
+}
+
+int adsg_ads_solve(adsg_ctx* ctx, double* rhs_dev, double* buf_dev) {
+    (void)buf_dev;
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!rhs_dev) return fail(-2, "rhs is NULL");
+    return enqueue_solve(ctx, rhs_dev, 0);
+}
+
+int adsg_ads_solve_t(adsg_ctx* ctx, double* rhs_dev) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!rhs_dev) return fail(-2, "rhs is NULL");
+    return enqueue_solve(ctx, rhs_dev, 1);
+}
+
+int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_dev) return fail(-2, "u is NULL");
+    if (!std::isfinite(dt)) return fail(-3, "dt must be finite");
+    if (nsteps < 0) return fail(-4, "nsteps must be >= 0");
+    if (nsteps == 0) return 0;
+    int st = ensure_dt_bands(ctx, dt);
+    if (st) return st;
+    if (nsteps >= 2 && !(ctx->graph && ctx->graph_dt == dt && ctx->graph_u == u_dev)) {
+        if (ctx->graph) {
+            cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        ADSG_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        ctx->capturing = true;
+        int s1 = enqueue_step(ctx, u_dev, ctx->ping, dt);
+        int s2 = s1 ? s1 : enqueue_step(ctx, ctx->ping, u_dev, dt);
+        ctx->capturing = false;
+        cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        if (s2) {
+            if (g) cudaGraphDestroy(g);
+            return s2;
+        }
+        if (ec != cudaSuccess) return fail_cuda(ec, "end capture");
+        cudaError_t ei = cudaGraphInstantiate(&ctx->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            ctx->graph = nullptr;
+            return fail_cuda(ei, "graph instantiate");
+        }
+        ctx->graph_dt = dt;
+        ctx->graph_u = u_dev;
+    }
+    for (int i = 0; i + 1 < nsteps; i += 2) ADSG_CUDA_TRY(cudaGraphLaunch(ctx->graph, ctx->stream), "graph launch");
+    if (nsteps % 2) {
+        st = enqueue_step(ctx, u_dev, ctx->ping, dt);
+        if (st) return st;
+        ADSG_CUDA_TRY(cudaMemcpyAsync(u_dev, ctx->ping, sizeof(double) * ctx->size, cudaMemcpyDeviceToDevice,
+                                      ctx->stream),
+                      "copy state");
+    }
+    return 0;
+}
+
+int adsg_ctx_enable_stage_timers(adsg_ctx* ctx, int enable) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    ctx->timing = enable != 0;
+    return 0;
+}
+
+int adsg_ctx_stage_times(adsg_ctx* ctx, double* ms, long long* launches) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    ctx->drain();
+    for (int i = 0; i < ADSG_NSTAGES; ++i) {
+        if (ms) ms[i] = ctx->stage_ms[i];
+        if (launches) launches[i] = ctx->stage_launches[i];
+        ctx->stage_ms[i] = 0.0;
+        ctx->stage_launches[i] = 0;
+    }
+    return 0;
+}
+
+int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!flops) return fail(-2, "flops is NULL");
+    if (!bytes) return fail(-3, "bytes is NULL");
+    for (int i = 0; i < ADSG_NSTAGES; ++i) flops[i] = bytes[i] = 0.0;
+    const double total = static_cast<double>(ctx->size);
+    // in-band terms of one matvec along dimension d, per output, on average
+    auto terms = [&](int d) {
+        const double n = ctx->dims[d].n, p = ctx->dims[d].p;
+        const double inband = n * (2 * p + 1) - p * (p + 1);
+        return inband / n;
+    };
+    if (ctx->ndim == 3) {
+        flops[ADSG_STAGE_RHS_OUTER] = 2.0 * total * 2 * terms(2);  // Mz, Nz
+        bytes[ADSG_STAGE_RHS_OUTER] = 8.0 * total * 3;
+        flops[ADSG_STAGE_RHS_MIDDLE] = 2.0 * total * 3 * terms(1);  // -dtKy, My (F); My (G)
+        bytes[ADSG_STAGE_RHS_MIDDLE] = 8.0 * total * 4;
+        flops[ADSG_STAGE_RHS_X] = 2.0 * total * 2 * terms(0);
+        bytes[ADSG_STAGE_RHS_X] = 8.0 * total * 3;
+    } else if (ctx->ndim == 2) {
+        flops[ADSG_STAGE_RHS_OUTER] = 2.0 * total * 2 * terms(1);
+        bytes[ADSG_STAGE_RHS_OUTER] = 8.0 * total * 3;
+        flops[ADSG_STAGE_RHS_X] = 2.0 * total * 2 * terms(0);
+        bytes[ADSG_STAGE_RHS_X] = 8.0 * total * 3;
+    } else {
+        flops[ADSG_STAGE_RHS_X] = 2.0 * total * terms(0);
+        bytes[ADSG_STAGE_RHS_X] = 8.0 * total * 2;
+    }
+    for (int d = 0; d < ctx->ndim; ++d) {
+        // per line: forward sum_j min(kl, n-1-j) FMAs, backward sum_j (uext_j FMAs + 1 multiply)
+        const int n = ctx->dims[d].n;
+        const double lines = total / n;
+        double fma = 0.0;
+        for (int j = 0; j + 1 < n; ++j) fma += std::min(ctx->dims[d].kl, n - 1 - j);
+        fma += ctx->uext_sum[d];
+        flops[ADSG_STAGE_SOLVE_X + d] = lines * (2.0 * fma + n);
+        bytes[ADSG_STAGE_SOLVE_X + d] = 16.0 * total;
+    }
+    {
+        // element quadrature: sum-factorised contractions per element (3D/2D, p = q - 1)
+        const int nd = ctx->ndim;
+        if (nd >= 2) {
+            const double n = ctx->dims[0].p + 1, q = ctx->dims[0].q;
+            double elems = 1;
+            for (int d = 0; d < nd; ++d) elems *= ctx->dims[d].elements;
+            double f;
+            if (nd == 3)
+                f = 2 * (2 * n * n * q * n + 3 * n * q * q * n + 4 * q * q * q * n + 4 * n * q * q * q +
+                         3 * n * n * q * q + 2 * n * n * n * q) +
+                    6 * q * q * q;
+            else
+                f = 2 * (2 * n * q * n + 3 * q * q * n + 3 * n * q * q + 2 * n * n * q) + 5 * q * q;
+            flops[ADSG_STAGE_RHS_ELEM] = elems * f;
+            bytes[ADSG_STAGE_RHS_ELEM] = 16.0 * total;
+        }
+    }
+    return 0;
+}
+
+int adsg_heat_steps_host(adsg_ctx* ctx, double* u_host, double dt, int nsteps) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_host) return fail(-2, "u is NULL");
+    if (!ctx->host_io) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->host_io, ctx->size), "io alloc");
+    const size_t bytes = sizeof(double) * ctx->size;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(ctx->host_io, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    int st = adsg_heat_steps(ctx, ctx->host_io, dt, nsteps);
+    if (st) return st;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(u_host, ctx->host_io, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    return 0;
+}
+
+int adsg_ads_solve_host(adsg_ctx* ctx, double* rhs_host) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!rhs_host) return fail(-2, "rhs is NULL");
+    if (!ctx->host_io) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->host_io, ctx->size), "io alloc");
+    const size_t bytes = sizeof(double) * ctx->size;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(ctx->host_io, rhs_host, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    int st = enqueue_solve(ctx, ctx->host_io, 0);
+    if (st) return st;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(rhs_host, ctx->host_io, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    return 0;
+}
+
+int adsg_heat_rhs_host(adsg_ctx* ctx, const double* u_prev_host, double* rhs_host, double dt) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_prev_host) return fail(-2, "u_prev is NULL");
+    if (!rhs_host) return fail(-3, "rhs is NULL");
+    if (!ctx->host_io) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->host_io, ctx->size), "io alloc");
+    const size_t bytes = sizeof(double) * ctx->size;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(ctx->host_io, u_prev_host, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
+    int st = enqueue_rhs(ctx, ctx->host_io, ctx->ping, dt);
+    if (st) return st;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(rhs_host, ctx->ping, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    return 0;
+}
+
+int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs, const double* ab,
+                 const int* ldab, const int* ipiv, double* b, const int* ldb, int* info) {
+    auto ret = [&](int code, const char* msg) {
+        if (info) *info = code < 0 ? code : 0;
+        return fail(code, msg);
+    };
+    if (!trans) return ret(-1, "trans is NULL");
+    const char t = *trans;
+    const bool tr = (t == 'T' || t == 't' || t == 'C' || t == 'c');
+    if (!tr && t != 'N' && t != 'n') return ret(-1, "trans must be N or T");
+    if (!n || *n < 0) return ret(-2, "n < 0");
+    if (!kl || *kl < 0) return ret(-3, "kl < 0");
+    if (!ku || *ku < 0) return ret(-4, "ku < 0");
+    if (!nrhs || *nrhs < 0) return ret(-5, "nrhs < 0");
+    if (!ldab || *ldab < 2 * *kl + *ku + 1) return ret(-7, "ldab < 2*kl+ku+1");
+    if (!ldb || *ldb < std::max(1, *n)) return ret(-10, "ldb < max(1, n)");
+    if (!ab) return ret(-6, "ab is NULL");
+    if (!ipiv) return ret(-8, "ipiv is NULL");
+    if (!b) return ret(-9, "b is NULL");
+    if (*kl > 16 || *kl + *ku > 32) return ret(ADSG_ERR_UNSUPPORTED, "band wider than kl=16, kl+ku=32");
+    if (line_solve_smem_per_warp(*n) > 220 * 1024) return ret(ADSG_ERR_UNSUPPORTED, "n > 850");
+    if (info) *info = 0;
+    if (*n == 0 || *nrhs == 0) return 0;
+    for (int j = 0; j < *n; ++j)
+        if (ipiv[j] < 1 || ipiv[j] > *n) return ret(-8, "pivot out of range");
+    solve_tables tb;
+    if (make_solve_tables(*n, *kl, *ku, *ldab, ab, ipiv, tb)) return ret(ADSG_ERR_SINGULAR, "zero diagonal in U");
+
+    cudaStream_t s = nullptr;
+    ADSG_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+    dev_arena ar;
+    dim_dev D;
+    D.n = *n;
+    D.kl = tb.kl;
+    D.w = tb.w;
+    double *lmul, *ucol, *rdiag, *x;
+    int *piv, *uext;
+    cudaError_t e = cudaSuccess;
+    const size_t cols = static_cast<size_t>(*nrhs);
+    const size_t n_ = static_cast<size_t>(*n);
+    if (e == cudaSuccess) e = ar.upload(&lmul, tb.lmul.data(), tb.lmul.size(), s);
+    if (e == cudaSuccess) e = ar.upload(&ucol, tb.ucol.data(), tb.ucol.size(), s);
+    if (e == cudaSuccess) e = ar.upload(&rdiag, tb.rdiag.data(), tb.rdiag.size(), s);
+    if (e == cudaSuccess) e = ar.upload(&piv, tb.piv.data(), tb.piv.size(), s);
+    if (e == cudaSuccess) e = ar.upload(&uext, tb.uext.data(), tb.uext.size(), s);
+    if (e == cudaSuccess) e = ar.alloc(&x, n_ * cols);
+    // gather the columns densely (ldb may exceed n)
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(x, n_ * sizeof(double), b, static_cast<size_t>(*ldb) * sizeof(double), n_ * sizeof(double),
+                              cols, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        D.lmul = lmul;
+        D.ucol = ucol;
+        D.rdiag = rdiag;
+        D.piv = piv;
+        D.uext = uext;
+        int nn = *n;
+        line_layout L;
+        L.nlines = static_cast<long long>(cols);
+        L.a = L.nlines;
+        L.sa = nn;
+        L.contiguous = 1;
+        e = launch_line_solve(x, D, L, tr ? 1 : 0, s);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(b, static_cast<size_t>(*ldb) * sizeof(double), x, n_ * sizeof(double), n_ * sizeof(double),
+                              cols, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) {
+        if (info) *info = 0;
+        return fail_cuda(e, "dgbtrs");
+    }
+    return 0;
+}
+
+}  // extern "C"

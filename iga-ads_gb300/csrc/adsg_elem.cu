@@ -1,0 +1,325 @@
+// Element-wise sum-factorised quadrature of the heat form
+//     rhs_a += sum_q w_q J_e ( u v_a - dt kappa(x_q) grad u . grad v_a )
+// (reference examples/heat/heat_3d.hpp:49-67 with an optional coefficient
+// field).  One warp per element: the element's coefficient tile and its 1D
+// basis/derivative rows (basis_data::b) are staged in shared memory, u and
+// grad u are interpolated to the q^d points one direction at a time, the
+// pointwise form is applied and the result is projected back with the
+// transposed 1D factors.  Elements are processed in (p+1)^d colours so that no
+// two concurrently processed elements share a dof: the scatter into the
+// global RHS is a plain read-modify-write, with no atomics, in a fixed order.
+#include <cuda_runtime.h>
+
+#include "adsg_kernels.cuh"
+
+namespace adsg {
+
+namespace {
+
+
+template <int N, int Q>
+struct elem3_smem {
+    double c[N * N * N];
+    double kc[N * N * N];
+    double B[3][Q * N];   // B[d][q*N + a]
+    double dB[3][Q * N];
+    double T0[N * N * Q], T1[N * N * Q];          // x-contracted, [bz][by][qx]
+    double V00[N * Q * Q], V01[N * Q * Q], V10[N * Q * Q];  // [bz][qy][qx]
+    double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
+    double K0[N * N * Q], K1[N * Q * Q];
+};
+
+// warps per block so that the static shared memory stays within 48 KB
+template <typename S>
+constexpr int warps_for() {
+    return sizeof(S) * 4 <= 48 * 1024 ? 4 : (sizeof(S) * 3 <= 48 * 1024 ? 3 : (sizeof(S) * 2 <= 48 * 1024 ? 2 : 1));
+}
+
+template <int P, int Q, int kWarpsPerBlock = warps_for<elem3_smem<P + 1, Q>>()>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    elem3_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
+                 dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt) {
+    constexpr int N = P + 1;
+    __shared__ elem3_smem<N, Q> sm_all[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
+    if (wid >= static_cast<long long>(mx) * my * mz) return;
+    elem3_smem<N, Q>& S = sm_all[warp];
+    const int iz = static_cast<int>(wid % mz);
+    const int iy = static_cast<int>((wid / mz) % my);
+    const int ix = static_cast<int>(wid / (static_cast<long long>(mz) * my));
+    const int e[3] = {cx + ix * N, cy + iy * N, cz + iz * N};
+    const dim_dev* D[3] = {&X, &Y, &Z};
+    const int f0 = X.first[e[0]], f1 = Y.first[e[1]], f2 = Z.first[e[2]];
+    const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
+
+    // stage coefficients and tables
+    for (int t = lane; t < N * N * N; t += 32) {
+        const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
+        const long long g = (f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az);
+        S.c[t] = u[g];
+        S.kc[t] = kappa ? kappa[g] : 0.0;
+    }
+    for (int t = lane; t < 3 * Q * N; t += 32) {
+        const int d = t / (Q * N), r = t % (Q * N), q = r / N, a = r % N;
+        const double* bt = D[d]->btab + ((static_cast<long long>(e[d]) * Q + q) * 2) * N;
+        S.B[d][r] = bt[a];
+        S.dB[d][r] = bt[N + a];
+    }
+    __syncwarp();
+    // x: T0/T1[bz][by][qx]
+    for (int t = lane; t < N * N * Q; t += 32) {
+        const int qx = t % Q, byz = t / Q;
+        double a0 = 0.0, a1 = 0.0, k0 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const double cv = S.c[byz * N + b];
+            a0 = fma(S.B[0][qx * N + b], cv, a0);
+            a1 = fma(S.dB[0][qx * N + b], cv, a1);
+            if (kappa) k0 = fma(S.B[0][qx * N + b], S.kc[byz * N + b], k0);
+        }
+        S.T0[t] = a0;
+        S.T1[t] = a1;
+        if (kappa) S.K0[t] = k0;
+    }
+    __syncwarp();
+    // y: V..[bz][qy][qx]
+    for (int t = lane; t < N * Q * Q; t += 32) {
+        const int qx = t % Q, qy = (t / Q) % Q, bz = t / (Q * Q);
+        double v00 = 0.0, v01 = 0.0, v10 = 0.0, k1 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const int src = (bz * N + b) * Q + qx;
+            const double by = S.B[1][qy * N + b], dby = S.dB[1][qy * N + b];
+            v00 = fma(by, S.T0[src], v00);
+            v01 = fma(dby, S.T0[src], v01);
+            v10 = fma(by, S.T1[src], v10);
+            if (kappa) k1 = fma(by, S.K0[src], k1);
+        }
+        S.V00[t] = v00;
+        S.V01[t] = v01;
+        S.V10[t] = v10;
+        if (kappa) S.K1[t] = k1;
+    }
+    __syncwarp();
+    // z + pointwise form: f = W u, g* = -dt kappa W d*u
+    const double J = X.jac[e[0]] * Y.jac[e[1]] * Z.jac[e[2]];
+    for (int t = lane; t < Q * Q * Q; t += 32) {
+        const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
+        double uv = 0.0, ux = 0.0, uy = 0.0, uz = 0.0, kv = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const int src = (b * Q + qy) * Q + qx;
+            const double bz = S.B[2][qz * N + b], dbz = S.dB[2][qz * N + b];
+            uv = fma(bz, S.V00[src], uv);
+            uz = fma(dbz, S.V00[src], uz);
+            uy = fma(bz, S.V01[src], uy);
+            ux = fma(bz, S.V10[src], ux);
+            if (kappa) kv = fma(bz, S.K1[src], kv);
+        }
+        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * J;
+        const double g = (kappa ? -dt * kv : -dt) * W;
+        S.f[t] = uv * W;
+        S.gx[t] = ux * g;
+        S.gy[t] = uy * g;
+        S.gz[t] = uz * g;
+    }
+    __syncwarp();
+    // z back: V00 <- S0[az][qy][qx], V01 <- Sx, V10 <- Sy
+    for (int t = lane; t < N * Q * Q; t += 32) {
+        const int qx = t % Q, qy = (t / Q) % Q, az = t / (Q * Q);
+        double s0 = 0.0, sx = 0.0, sy = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int src = (q * Q + qy) * Q + qx;
+            const double bz = S.B[2][q * N + az], dbz = S.dB[2][q * N + az];
+            s0 = fma(bz, S.f[src], s0);
+            s0 = fma(dbz, S.gz[src], s0);
+            sx = fma(bz, S.gx[src], sx);
+            sy = fma(bz, S.gy[src], sy);
+        }
+        S.V00[t] = s0;
+        S.V01[t] = sx;
+        S.V10[t] = sy;
+    }
+    __syncwarp();
+    // y back: T0 <- R0[az][ay][qx], T1 <- Rx
+    for (int t = lane; t < N * N * Q; t += 32) {
+        const int qx = t % Q, ay = (t / Q) % N, az = t / (Q * N);
+        double r0 = 0.0, rx = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int src = (az * Q + q) * Q + qx;
+            const double by = S.B[1][q * N + ay], dby = S.dB[1][q * N + ay];
+            r0 = fma(by, S.V00[src], r0);
+            r0 = fma(dby, S.V10[src], r0);
+            rx = fma(by, S.V01[src], rx);
+        }
+        S.T0[t] = r0;
+        S.T1[t] = rx;
+    }
+    __syncwarp();
+    // x back and scatter (this colour owns every dof of the element)
+    for (int t = lane; t < N * N * N; t += 32) {
+        const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
+        double o = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int src = (az * N + ay) * Q + q;
+            o = fma(S.B[0][q * N + ax], S.T0[src], o);
+            o = fma(S.dB[0][q * N + ax], S.T1[src], o);
+        }
+        const long long g = (f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az);
+        rhs[g] += o;
+    }
+}
+
+template <int N, int Q>
+struct elem2_smem {
+    double c[N * N], kc[N * N];
+    double B[2][Q * N], dB[2][Q * N];
+    double T0[N * Q], T1[N * Q], K0[N * Q];  // [by][qx]
+    double f[Q * Q], gx[Q * Q], gy[Q * Q];
+};
+
+template <int P, int Q, int kWarpsPerBlock = warps_for<elem2_smem<P + 1, Q>>()>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    elem2_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
+                 dim_dev X, dim_dev Y, int cx, int cy, int mx, int my, double dt) {
+    constexpr int N = P + 1;
+    __shared__ elem2_smem<N, Q> sm_all[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
+    if (wid >= static_cast<long long>(mx) * my) return;
+    elem2_smem<N, Q>& S = sm_all[warp];
+    const int iy = static_cast<int>(wid % my);
+    const int ix = static_cast<int>(wid / my);
+    const int e[2] = {cx + ix * N, cy + iy * N};
+    const dim_dev* D[2] = {&X, &Y};
+    const int f0 = X.first[e[0]], f1 = Y.first[e[1]];
+    const long long nx = X.n;
+    for (int t = lane; t < N * N; t += 32) {
+        const long long g = (f0 + t % N) + nx * (f1 + t / N);
+        S.c[t] = u[g];
+        S.kc[t] = kappa ? kappa[g] : 0.0;
+    }
+    for (int t = lane; t < 2 * Q * N; t += 32) {
+        const int d = t / (Q * N), r = t % (Q * N), q = r / N, a = r % N;
+        const double* bt = D[d]->btab + ((static_cast<long long>(e[d]) * Q + q) * 2) * N;
+        S.B[d][r] = bt[a];
+        S.dB[d][r] = bt[N + a];
+    }
+    __syncwarp();
+    for (int t = lane; t < N * Q; t += 32) {
+        const int qx = t % Q, by = t / Q;
+        double a0 = 0.0, a1 = 0.0, k0 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            a0 = fma(S.B[0][qx * N + b], S.c[by * N + b], a0);
+            a1 = fma(S.dB[0][qx * N + b], S.c[by * N + b], a1);
+            if (kappa) k0 = fma(S.B[0][qx * N + b], S.kc[by * N + b], k0);
+        }
+        S.T0[t] = a0;
+        S.T1[t] = a1;
+        if (kappa) S.K0[t] = k0;
+    }
+    __syncwarp();
+    const double J = X.jac[e[0]] * Y.jac[e[1]];
+    for (int t = lane; t < Q * Q; t += 32) {
+        const int qx = t % Q, qy = t / Q;
+        double uv = 0.0, ux = 0.0, uy = 0.0, kv = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const double by = S.B[1][qy * N + b], dby = S.dB[1][qy * N + b];
+            uv = fma(by, S.T0[b * Q + qx], uv);
+            uy = fma(dby, S.T0[b * Q + qx], uy);
+            ux = fma(by, S.T1[b * Q + qx], ux);
+            if (kappa) kv = fma(by, S.K0[b * Q + qx], kv);
+        }
+        const double W = X.wq[qx] * Y.wq[qy] * J;
+        const double g = (kappa ? -dt * kv : -dt) * W;
+        S.f[t] = uv * W;
+        S.gx[t] = ux * g;
+        S.gy[t] = uy * g;
+    }
+    __syncwarp();
+    // y back: T0 <- S0[ay][qx], T1 <- Sx
+    for (int t = lane; t < N * Q; t += 32) {
+        const int qx = t % Q, ay = t / Q;
+        double s0 = 0.0, sx = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const double by = S.B[1][q * N + ay], dby = S.dB[1][q * N + ay];
+            s0 = fma(by, S.f[q * Q + qx], s0);
+            s0 = fma(dby, S.gy[q * Q + qx], s0);
+            sx = fma(by, S.gx[q * Q + qx], sx);
+        }
+        S.T0[t] = s0;
+        S.T1[t] = sx;
+    }
+    __syncwarp();
+    for (int t = lane; t < N * N; t += 32) {
+        const int ax = t % N, ay = t / N;
+        double o = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            o = fma(S.B[0][q * N + ax], S.T0[ay * Q + q], o);
+            o = fma(S.dB[0][q * N + ax], S.T1[ay * Q + q], o);
+        }
+        rhs[(f0 + ax) + nx * (f1 + ay)] += o;
+    }
+}
+
+int colour_count(int E, int c, int N) { return E > c ? (E - c + N - 1) / N : 0; }
+
+template <int P>
+cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* kappa, double* rhs, double dt,
+                   cudaStream_t s) {
+    constexpr int N = P + 1, Q = P + 1;
+    constexpr int W3 = warps_for<elem3_smem<N, Q>>();
+    constexpr int W2 = warps_for<elem2_smem<N, Q>>();
+    if (ndim == 3) {
+        for (int cx = 0; cx < N; ++cx)
+            for (int cy = 0; cy < N; ++cy)
+                for (int cz = 0; cz < N; ++cz) {
+                    const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N),
+                              mz = colour_count(d[2].elements, cz, N);
+                    const long long work = static_cast<long long>(mx) * my * mz;
+                    if (!work) continue;
+                    const long long blocks = (work + W3 - 1) / W3;
+                    elem3_kernel<P, Q><<<blocks, 32 * W3, 0, s>>>(u, kappa, rhs, d[0], d[1], d[2], cx, cy,
+                                                                             cz, mx, my, mz, dt);
+                }
+    } else {
+        for (int cx = 0; cx < N; ++cx)
+            for (int cy = 0; cy < N; ++cy) {
+                const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N);
+                const long long work = static_cast<long long>(mx) * my;
+                if (!work) continue;
+                const long long blocks = (work + W2 - 1) / W2;
+                elem2_kernel<P, Q><<<blocks, 32 * W2, 0, s>>>(u, kappa, rhs, d[0], d[1], cx, cy, mx, my, dt);
+            }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev, const double* kappa, double* rhs,
+                            double dt, cudaStream_t s) {
+    if (ndim < 2) return cudaErrorNotSupported;
+    const int p = dims[0].p;
+    for (int d = 0; d < ndim; ++d)
+        if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    switch (p) {
+        case 1: return elem_p<1>(ndim, dims, u_prev, kappa, rhs, dt, s);
+        case 2: return elem_p<2>(ndim, dims, u_prev, kappa, rhs, dt, s);
+        case 3: return elem_p<3>(ndim, dims, u_prev, kappa, rhs, dt, s);
+        case 4: return elem_p<4>(ndim, dims, u_prev, kappa, rhs, dt, s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+}  // namespace adsg

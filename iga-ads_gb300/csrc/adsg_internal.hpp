@@ -1,0 +1,39 @@
+// Internal declarations shared by the host set-up, the kernels and the C-ABI.
+#ifndef ADSG_INTERNAL_HPP
+#define ADSG_INTERNAL_HPP
+
+#include <cstddef>
+#include <vector>
+
+#include "../../include/ads_gb300.h"
+
+namespace adsg {
+
+// One dimension on the host: what the reference's ads::dimension holds.
+struct dim_host {
+    int p = 0, elements = 0, q = 0, n = 0;
+    int kl = 0, ku = 0, ldab = 0;
+    std::vector<double> knots;
+    std::vector<double> btab;  // [E][q][2][p+1]
+    std::vector<double> xq;    // [E][q]
+    std::vector<double> w;     // [q]
+    std::vector<double> J;     // [E]
+    std::vector<int> first_dofs;
+    std::vector<double> mass;   // unfactorised, LAPACK band layout kl = ku = p
+    std::vector<double> stiff;  // same layout
+    std::vector<double> lu;     // factorised copy of mass
+    std::vector<int> ipiv;      // 1-based
+};
+
+bool gauss_legendre(int q, double* x, double* w);
+bool build_dimension(dim_host& d, int p, int elements, double a, double b, int q);
+void form_band(const dim_host& d, int which, std::vector<double>& ab);
+int factorize(dim_host& d);
+
+// Records msg as the calling thread's last error and returns code.
+int fail(int code, const char* msg);
+int fail_cuda(int err, const char* where);
+
+}  // namespace adsg
+
+#endif

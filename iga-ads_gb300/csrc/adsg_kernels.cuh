@@ -1,0 +1,62 @@
+// Device-side data of a context and the kernel launchers.
+#ifndef ADSG_KERNELS_CUH
+#define ADSG_KERNELS_CUH
+
+#include <cuda_runtime.h>
+
+namespace adsg {
+
+// Per-dimension device tables.  Band rows hold the 2p+1 coefficients of row r
+// for columns r-p .. r+p (zero outside the matrix).
+struct dim_dev {
+    int n = 0, p = 0, kl = 0, w = 0;  // w = kl + ku: widest upper extent of U
+    int elements = 0, q = 0;
+    const double* mrow = nullptr;   // [n][2p+1] 1D mass matrix
+    const double* krow = nullptr;   // [n][2p+1] 1D stiffness matrix
+    const double* nrow = nullptr;   // [n][2p+1] M - dt K     (per dt)
+    const double* kdt = nullptr;    // [n][2p+1] -dt K        (per dt)
+    const double* lmul = nullptr;   // [n][kl] L multipliers of column j (dgbtrf)
+    const int* piv = nullptr;       // [n] 0-based row exchanged with row j
+    const double* ucol = nullptr;   // [n][w] U(j-d, j), d = 1..w
+    const int* uext = nullptr;      // [n] number of non-zero U(j-d, j) to apply
+    const double* rdiag = nullptr;  // [n] 1 / U(j, j)
+    const double* btab = nullptr;   // [E][q][2][p+1] basis values / derivatives
+    const double* wq = nullptr;     // [q]
+    const double* jac = nullptr;    // [E]
+    const int* first = nullptr;     // [E]
+};
+
+// Where the grid lines of one direction sit in a tensor of extents n[0..2]
+// (x fastest): element j of line g is at base(g) + j*elem_stride with
+// base(g) = (g % a) * sa + (g / a) * sb.
+struct line_layout {
+    long long nlines = 0;
+    long long a = 1, sa = 0, sb = 0, elem_stride = 1;
+    int contiguous = 0;  // lines are consecutive blocks of n doubles
+};
+
+line_layout make_line_layout(const int* n, int ndim, int d);
+
+// rhs passes -------------------------------------------------------------
+// out0 = A0 (.) in0 [+ A1 (.) in1],  out1 = B0 (.) in0  along one axis, where
+// (.) applies a band with rows of 2p+1 coefficients.
+cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double* out0, double* out1,
+                             const double* A0, const double* A1, const double* B0, int n_axis,
+                             long long stride, long long total, cudaStream_t s);
+
+// nrow = mrow - dt*krow, kdt = -dt*krow for one dimension
+cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* kdt, cudaStream_t s);
+
+// line solves ------------------------------------------------------------
+// trans = 0: dgbtrs 'N', trans = 1: dgbtrs 'T', along every line of layout L.
+cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans,
+                              cudaStream_t s);
+size_t line_solve_smem_per_warp(int n);
+
+// element-wise sum-factorised quadrature (optional kappa field) -----------
+cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev, const double* kappa,
+                            double* rhs, double dt, cudaStream_t s);
+
+}  // namespace adsg
+
+#endif

@@ -1,0 +1,176 @@
+/*
+ * ads_gb300.h -- C-ABI of the GB300 (sm_103a) explicit-step engine for
+ * IGA-ADS: Gauss-quadrature heat RHS assembly over tensor-product B-spline
+ * elements and the alternating-directions (Kronecker) banded mass solve.
+ *
+ * Conventions shared by every entry point:
+ *  - plain C types only; every function returns an int status:
+ *      0                   success
+ *      -k  (k >= 1)        the k-th argument is invalid (LAPACK's convention)
+ *      ADSG_ERR_* (> 0)    runtime or numerical failure; adsg_last_error()
+ *                          returns a message for the calling thread
+ *  - tensors are x-fastest: u[i + nx*(j + ny*k)], the layout of ads::lin::tensor
+ *    (reference include/ads/util/multi_array/ordering/reverse.hpp:27-31);
+ *  - band matrices use LAPACK band storage (dgbtrf/dgbtrs layout): entry (i,j)
+ *    of a kl/ku band is ab[(kl+ku+i-j) + j*ldab], ldab >= 2*kl+ku+1
+ *    (reference include/ads/lin/band_matrix.hpp:66-73 with row_offset = kl);
+ *    pivots are 1-based as dgbtrf writes them;
+ *  - "_dev" pointers are device (HBM) addresses; everything else is host memory.
+ *    Device work runs on the context's stream and is asynchronous unless the
+ *    function's comment says it synchronises.
+ *
+ * A context is not thread-safe: use one context per host thread, or serialise.
+ */
+#ifndef ADS_GB300_H
+#define ADS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADSG_ERR_CUDA 1001      /* a CUDA runtime call failed */
+#define ADSG_ERR_NOMEM 1002     /* host or device allocation failed */
+#define ADSG_ERR_SINGULAR 1003  /* zero pivot in a band factorisation */
+#define ADSG_ERR_DEVICE 1004    /* a kernel reported an error word (bounds, timeout) */
+#define ADSG_ERR_UNSUPPORTED 1005
+
+/* Maximum degree handled by the device kernels. */
+#define ADSG_MAX_DEGREE 8
+
+typedef struct adsg_ctx adsg_ctx;
+typedef struct adsg_dim adsg_dim;
+
+/* ---- one dimension: the data of ads::dimension -------------------------
+ * Replaces what reference include/ads/simulation/dimension.hpp:20-59 holds:
+ * basis_data tables (basis_data.hpp:21-86, derivatives = 1) and the
+ * factorised mass matrix with its pivots (dim_data{M, ctx}, solver.hpp:17-20).
+ */
+typedef struct adsg_dim_desc {
+    int p;                  /* B-spline degree */
+    int elements;           /* number of elements */
+    int quad_order;         /* Gauss points per element */
+    int n;                  /* number of dofs */
+    const double* btab;     /* [elements][quad_order][2][p+1]: b[e][q][d][a] */
+    const double* w;        /* [quad_order] Gauss weights on [-1,1] */
+    const double* J;        /* [elements] element Jacobians (x2-x1)/2 */
+    const int* first_dofs;  /* [elements] basis_data::first_dofs */
+    int kl, ku, ldab;       /* band parameters of the factorised matrix */
+    const double* lu;       /* dgbtrf output, ldab*n doubles */
+    const int* ipiv;        /* [n] 1-based pivots */
+} adsg_dim_desc;
+
+/* Build a dimension on the host exactly as the reference's dimension ctor
+ * does (dimension.cpp:8-21 -> bspline::create_basis, basis_data,
+ * gram_matrix_1d) and factorise its mass matrix (dimension::factorize_matrix,
+ * dimension.hpp:52 -> dgbtrf).  Open uniform knots on [a, b],
+ * repeated_nodes = 0.  quad_order <= 0 means p + 1.  No GPU needed. */
+int adsg_dim_create(int p, int elements, double a, double b, int quad_order, adsg_dim** out);
+void adsg_dim_destroy(adsg_dim* d);
+/* Descriptor pointing into d's arrays (valid while d lives). */
+int adsg_dim_describe(const adsg_dim* d, adsg_dim_desc* out);
+/* dimension::fix_dof (dimension.cpp:23-29): identity row k in M, then the
+ * matrix is refactorised.  Affects only the solve, as in the reference. */
+int adsg_dim_fix_dof(adsg_dim* d, int k);
+/* Unfactorised 1D mass (which = 0, gram_matrix_1d, form_matrix.cpp:8-24) or
+ * stiffness (which = 1, stiffness_matrix_1d, form_matrix.cpp:26-42) band with
+ * kl = ku = p in the layout above (ldab = 3p+1). ab has (3p+1)*n doubles. */
+int adsg_dim_form_band(const adsg_dim* d, int which, double* ab);
+
+/* ---- contexts ------------------------------------------------------------
+ * A context owns the device copies of ndim (1..3) dimension descriptors, the
+ * 1D mass/stiffness bands derived from their quadrature tables, scratch
+ * tensors and a CUDA stream.  The host descriptors may be freed afterwards.
+ * The context's own stream is a blocking stream: it is ordered with work on
+ * the legacy default stream (e.g. torch's default stream). */
+int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out);
+int adsg_ctx_destroy(adsg_ctx* ctx);
+/* Number of dofs of the whole tensor (product of the dimension sizes). */
+long long adsg_ctx_size(const adsg_ctx* ctx);
+/* Make the context enqueue on an existing cudaStream_t (NULL: its own). */
+int adsg_ctx_set_stream(adsg_ctx* ctx, void* cuda_stream);
+/* Wait for all work of the context and report any device error word. */
+int adsg_ctx_synchronize(adsg_ctx* ctx);
+/* Thread-local message describing the last failure (never NULL). */
+const char* adsg_last_error(void);
+
+/* ---- the hot path (device buffers) ---------------------------------------- */
+
+/* heat_3d::compute_rhs (reference examples/heat/heat_3d.hpp:49-67; 2D:
+ * heat_2d.hpp:166-192): rhs_a = sum_e sum_q w_q J_e (u v_a - dt grad u . grad v_a)
+ * with u from u_prev.  Computed by the factored quadrature: the tensor-product
+ * Gauss rule and the separable Jacobian make the element sum equal to
+ * (Mx(x)My(x)Mz - dt (Kx(x)My(x)Mz + Mx(x)Ky(x)Mz + Mx(x)My(x)Kz)) u_prev with the
+ * 1D quadrature-assembled mass/stiffness bands.  u_prev and rhs must not alias. */
+int adsg_heat_rhs(adsg_ctx* ctx, const double* u_prev_dev, double* rhs_dev, double dt);
+
+/* The same RHS by element-wise sum-factorised quadrature over the basis
+ * tables, optionally with a diffusion field kappa given as spline
+ * coefficients on the same space (kappa_dev may be NULL for kappa = 1):
+ * rhs_a = sum_e sum_q w J (u v_a - dt kappa(x_q) grad u . grad v_a). */
+int adsg_heat_rhs_elem(adsg_ctx* ctx, const double* u_prev_dev, const double* kappa_dev,
+                       double* rhs_dev, double dt);
+
+/* ads_solve(rhs, buf, dims...) (reference include/ads/solver.hpp:222-226,
+ * standard ADS, 1D case :199-203): solves (M_x (x) M_y (x) M_z) x = rhs with the
+ * factorised bands, one pivoted band substitution (dgbtrs) per grid line and
+ * direction, with no transpose passes.  The solution is left in rhs_dev;
+ * buf_dev is accepted for signature parity and may be NULL. */
+int adsg_ads_solve(adsg_ctx* ctx, double* rhs_dev, double* buf_dev);
+
+/* The transposed solve (dgbtrs 'T' along every direction): the adjoint of
+ * adsg_ads_solve. */
+int adsg_ads_solve_t(adsg_ctx* ctx, double* rhs_dev);
+
+/* nsteps of simulation_base::run's loop with heat_3d's step
+ * (simulation_base.cpp:11-20, heat_3d.hpp:39-47): swap, compute_rhs, solve.
+ * u_dev holds the state in and out.  Steps are replayed from a CUDA graph. */
+int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps);
+
+/* ---- stage timers (observability) -----------------------------------------
+ * Stages of a step, in launch order.  With timers enabled every kernel launch
+ * of the context is bracketed by CUDA events on the context's stream (not
+ * while a CUDA graph replays).  adsg_ctx_stage_times synchronises, adds the
+ * elapsed times to ms[stage] and launch counts to launches[stage] (arrays of
+ * ADSG_NSTAGES entries, accumulated since the last call) and resets them.
+ * adsg_ctx_stage_work gives each stage's algorithmic work per launch: FP64
+ * flops (FMA = 2, multiply = 1) and compulsory HBM bytes (each input read and
+ * each output written once). */
+#define ADSG_STAGE_RHS_OUTER 0  /* band pass along z (3D) or y (2D) */
+#define ADSG_STAGE_RHS_MIDDLE 1 /* band pass along y (3D) */
+#define ADSG_STAGE_RHS_X 2      /* band pass along x, writes the RHS */
+#define ADSG_STAGE_SOLVE_X 3
+#define ADSG_STAGE_SOLVE_Y 4
+#define ADSG_STAGE_SOLVE_Z 5
+#define ADSG_STAGE_RHS_ELEM 6   /* element-wise sum-factorised quadrature */
+#define ADSG_NSTAGES 7
+int adsg_ctx_enable_stage_timers(adsg_ctx* ctx, int enable);
+int adsg_ctx_stage_times(adsg_ctx* ctx, double* ms, long long* launches);
+int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
+
+/* ---- host-buffer entry points (the reference-facing boundary) ------------- */
+
+/* adsg_heat_steps on a host tensor: copies u_host to the device, runs nsteps,
+ * copies the result back; synchronises. */
+int adsg_heat_steps_host(adsg_ctx* ctx, double* u_host, double dt, int nsteps);
+
+/* adsg_ads_solve on a host tensor (copy in, solve, copy out; synchronises). */
+int adsg_ads_solve_host(adsg_ctx* ctx, double* rhs_host);
+
+/* adsg_heat_rhs on host tensors (synchronises). */
+int adsg_heat_rhs_host(adsg_ctx* ctx, const double* u_prev_host, double* rhs_host, double dt);
+
+/* Drop-in for LAPACK dgbtrs_ as the reference declares it
+ * (include/ads/lin/lapack.hpp:27-39, called from lin/band_solve.hpp:26-31):
+ * same arguments, by pointer, host memory, column-major B with ldb >= n.
+ * Solves on the GPU (all nrhs columns in parallel) and synchronises.
+ * *info = 0 on success or -k for an invalid k-th argument; the return value
+ * is the same status. */
+int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs,
+                 const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
+                 int* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADS_GB300_H */

@@ -1,0 +1,280 @@
+// Driver around the reference's OWN compiled code (built by oracle/Makefile
+// from the reference sources where they lie; output only into oracle/_ref/).
+// TEST INFRASTRUCTURE ONLY: it exists to pin the C restatement in
+// ads_oracle.c and to generate the golden fixtures under tests/golden/.
+//
+// Exposes a small extern "C" surface so Python can load it with ctypes.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <iostream>
+#include <memory>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "ads/executor/sequential.hpp"
+#include "ads/lin/band_solve.hpp"
+#include "ads/simulation.hpp"
+
+// The reference's examples/heat/heat_3d.hpp keeps compute_rhs private; open
+// it up so the literal reference loop (eval_fun inside the dof loop) runs.
+#define private public
+#include "heat/heat_3d.hpp"
+#undef private
+
+namespace {
+
+// 3D heat step in the executor form of heat_2d.hpp:166-192 /
+// scalability/test3d.hpp:223-251 (eval_fun hoisted, local element tile,
+// synchronized scatter), driven by the reference's sequential_executor.
+class heat3_driver : public ads::simulation_3d {
+public:
+    vector_type u, u_prev;
+    ads::sequential_executor executor;
+
+    explicit heat3_driver(const ads::config_3d& c)
+    : simulation_3d{c}
+    , u{shape()}
+    , u_prev{shape()} { }
+
+    void compute_rhs() {
+        auto& rhs = u;
+        zero(rhs);
+        executor.for_each(elements(), [&](index_type e) {
+            auto U = element_rhs();
+            double J = jacobian(e);
+            for (auto q : quad_points()) {
+                double w = weight(q);
+                value_type uu = eval_fun(u_prev, e, q);
+                for (auto a : dofs_on_element(e)) {
+                    auto aa = dof_global_to_local(e, a);
+                    value_type v = eval_basis(e, q, a);
+                    double gradient_prod = grad_dot(uu, v);
+                    double val = uu.val * v.val - steps.dt * gradient_prod;
+                    U(aa[0], aa[1], aa[2]) += val * w * J;
+                }
+            }
+            executor.synchronized([&]() { update_global_rhs(rhs, U, e); });
+        });
+    }
+
+    void prepare() { prepare_matrices(); }
+    void do_solve(vector_type& v) { solve(v); }
+    void step() {
+        std::swap(u, u_prev);
+        compute_rhs();
+        solve(u);
+    }
+};
+
+class heat2_driver : public ads::simulation_2d {
+public:
+    vector_type u, u_prev;
+    ads::sequential_executor executor;
+
+    explicit heat2_driver(const ads::config_2d& c)
+    : simulation_2d{c}
+    , u{shape()}
+    , u_prev{shape()} { }
+
+    void compute_rhs() {
+        auto& rhs = u;
+        zero(rhs);
+        executor.for_each(elements(), [&](index_type e) {
+            auto U = element_rhs();
+            double J = jacobian(e);
+            for (auto q : quad_points()) {
+                double w = weight(q);
+                for (auto a : dofs_on_element(e)) {
+                    auto aa = dof_global_to_local(e, a);
+                    value_type v = eval_basis(e, q, a);
+                    value_type uu = eval_fun(u_prev, e, q);
+                    double gradient_prod = grad_dot(uu, v);
+                    double val = uu.val * v.val - steps.dt * gradient_prod;
+                    U(aa[0], aa[1]) += val * w * J;
+                }
+            }
+            executor.synchronized([&]() { update_global_rhs(rhs, U, e); });
+        });
+    }
+
+    void prepare() { prepare_matrices(); }
+    void do_solve(vector_type& v) { solve(v); }
+    template <typename F>
+    void do_projection(vector_type& v, F f) {
+        projection(v, f);
+    }
+    void step() {
+        std::swap(u, u_prev);
+        compute_rhs();
+        solve(u);
+    }
+};
+
+template <typename T>
+void load(T& t, const double* src) {
+    std::copy(src, src + t.size(), t.data());
+}
+
+template <typename T>
+void store(const T& t, double* dst) {
+    std::copy(t.data(), t.data() + t.size(), dst);
+}
+
+}  // namespace
+
+extern "C" {
+
+// Per-dimension tables exactly as the reference builds them (dimension ctor,
+// dimension.cpp:8-17) and the factorised matrix (dimension::factorize_matrix).
+int ref_dim_tables(int p, int elements, double* btab, double* xq, double* w, double* J,
+                   int* first_dofs, double* mass_ab, double* lu_ab, int* ipiv) {
+    ads::dim_config cfg{p, elements};
+    ads::dimension d{cfg, 1};
+    const auto& bd = d.basis;
+    int q = bd.quad_order;
+    for (int e = 0; e < bd.elements; ++e) {
+        for (int k = 0; k < q; ++k) {
+            xq[e * q + k] = bd.x[e][k];
+            for (int dd = 0; dd < 2; ++dd)
+                for (int a = 0; a <= p; ++a) btab[((e * q + k) * 2 + dd) * (p + 1) + a] = bd.b[e][k][dd][a];
+        }
+        J[e] = bd.J[e];
+        first_dofs[e] = bd.first_dof(e);
+    }
+    for (int k = 0; k < q; ++k) w[k] = bd.w[k];
+    int ldab = d.M.column_size();
+    int n = d.dofs();
+    std::copy(d.M.full_buffer(), d.M.full_buffer() + ldab * n, mass_ab);
+    d.factorize_matrix();
+    std::copy(d.M.full_buffer(), d.M.full_buffer() + ldab * n, lu_ab);
+    std::copy(d.ctx.pivot_vector.begin(), d.ctx.pivot_vector.end(), ipiv);
+    return d.ctx.info;
+}
+
+// Stiffness matrix of the same basis (form_matrix.cpp:26-42).
+int ref_stiffness(int p, int elements, double* ab) {
+    ads::dim_config cfg{p, elements};
+    ads::dimension d{cfg, 1};
+    ads::lin::band_matrix K{p, p, d.dofs()};
+    ads::stiffness_matrix_1d(K, d.basis);
+    std::copy(K.full_buffer(), K.full_buffer() + K.column_size() * d.dofs(), ab);
+    return 0;
+}
+
+// LAPACK band factorisation + solve through the reference's lin:: wrappers
+// (band_solve.hpp:16-31). ab is a kl/ku band in the layout of band_matrix.
+int ref_band_solve(int kl, int ku, int n, const double* ab_in, int nrhs, double* b, double* lu_out,
+                   int* ipiv_out) {
+    ads::lin::band_matrix M{kl, ku, n};
+    std::copy(ab_in, ab_in + M.column_size() * n, M.full_buffer());
+    ads::lin::solver_ctx ctx{M};
+    ads::lin::factorize(M, ctx);
+    if (ctx.info != 0) return ctx.info;
+    ads::lin::solve_with_factorized(M, b, ctx, nrhs);
+    if (lu_out) std::copy(M.full_buffer(), M.full_buffer() + M.column_size() * n, lu_out);
+    if (ipiv_out) std::copy(ctx.pivot_vector.begin(), ctx.pivot_vector.end(), ipiv_out);
+    return ctx.info;
+}
+
+// ads_solve (solver.hpp:222-226) on the factorised mass matrices of a
+// uniform p / elements grid in ndim dimensions.
+int ref_ads_solve(int ndim, int p, int elements, double* rhs) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{1, 0.0};
+    if (ndim == 3) {
+        heat3_driver s{ads::config_3d{dim, dim, dim, steps, 1}};
+        s.prepare();
+        load(s.u, rhs);
+        s.do_solve(s.u);
+        store(s.u, rhs);
+    } else if (ndim == 2) {
+        heat2_driver s{ads::config_2d{dim, dim, steps, 1}};
+        s.prepare();
+        load(s.u, rhs);
+        s.do_solve(s.u);
+        store(s.u, rhs);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+// nsteps explicit heat steps from u (in/out). mode 0: executor form with the
+// hoisted eval_fun; mode 1 (3D only): the literal heat_3d::compute_rhs.
+int ref_heat_steps(int ndim, int p, int elements, double dt, int nsteps, double* u, int mode) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{nsteps, dt};
+    if (ndim == 3) {
+        ads::config_3d c{dim, dim, dim, steps, 1};
+        if (mode == 1) {
+            ads::problems::heat_3d s{c};
+            s.prepare_matrices();
+            load(s.u, u);
+            for (int i = 0; i < nsteps; ++i) {
+                s.before_step(i, i * dt);
+                s.step(i, i * dt);
+            }
+            store(s.u, u);
+        } else {
+            heat3_driver s{c};
+            s.prepare();
+            load(s.u, u);
+            for (int i = 0; i < nsteps; ++i) s.step();
+            store(s.u, u);
+        }
+    } else if (ndim == 2) {
+        heat2_driver s{ads::config_2d{dim, dim, steps, 1}};
+        s.prepare();
+        load(s.u, u);
+        for (int i = 0; i < nsteps; ++i) s.step();
+        store(s.u, u);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+// One RHS evaluation (no solve) from u_prev into rhs, executor form.
+int ref_heat_rhs(int ndim, int p, int elements, double dt, const double* u_prev, double* rhs) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{1, dt};
+    if (ndim == 3) {
+        heat3_driver s{ads::config_3d{dim, dim, dim, steps, 1}};
+        load(s.u_prev, u_prev);
+        s.compute_rhs();
+        store(s.u, rhs);
+    } else if (ndim == 2) {
+        heat2_driver s{ads::config_2d{dim, dim, steps, 1}};
+        load(s.u_prev, u_prev);
+        s.compute_rhs();
+        store(s.u, rhs);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+// compute_projection of prod_d sin(pi x_d) (projection.hpp:148-153), unsolved.
+int ref_projection_sin(int ndim, int p, int elements, double* out) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{1, 0.0};
+    if (ndim == 3) {
+        heat3_driver s{ads::config_3d{dim, dim, dim, steps, 1}};
+        s.projection(s.u, [](double x, double y, double z) {
+            return std::sin(M_PI * x) * std::sin(M_PI * y) * std::sin(M_PI * z);
+        });
+        store(s.u, out);
+    } else if (ndim == 2) {
+        heat2_driver s{ads::config_2d{dim, dim, steps, 1}};
+        s.do_projection(s.u, [](double x, double y) { return std::sin(M_PI * x) * std::sin(M_PI * y); });
+        store(s.u, out);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+}  // extern "C"

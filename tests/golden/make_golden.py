@@ -1,0 +1,186 @@
+"""Generates the golden fixtures in this folder from the reference's OWN code.
+
+Run in a container where the reference sources are present:
+    make -C oracle ref           # builds oracle/_ref/libadsref.so from them
+    python tests/golden/make_golden.py
+
+Every output array below is produced by the reference implementation
+(oracle/_ref: the reference's src/ads/*.cpp and headers compiled as they lie,
+driven through their own classes -- ads::dimension, simulation_2d/3d,
+ads_solve, lin::factorize/solve_with_factorized).  Initial fields are the
+reference's projection of prod sin(pi x_d) solved by its ads_solve, plus
+SplitMix64 noise (the same generator as ads_gb300.inputs.splitmix_uniform).
+
+The small systems in solver_known_answers are those of the reference tests
+tests/ads/solver_test.cpp:63-255 and tests/ads/lin/band_solve_test.cpp:15-46,
+with the answers those tests expect.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libadsref.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def dp(a):
+    return a.ctypes.data_as(_dp)
+
+
+def ip(a):
+    return a.ctypes.data_as(_ip)
+
+
+def splitmix_uniform(seed, count):
+    m1, m2, m3 = np.uint64(0x9E3779B97F4A7C15), np.uint64(0xBF58476D1CE4E5B9), np.uint64(0x94D049BB133111EB)
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + idx * m1
+        z = (z ^ (z >> np.uint64(30))) * m2
+        z = (z ^ (z >> np.uint64(27))) * m3
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def load_ref():
+    if not os.path.exists(REF_LIB):
+        sys.exit(f"{REF_LIB} missing: run `make -C oracle ref` where the reference sources are present")
+    L = ctypes.CDLL(REF_LIB)
+    i, d = ctypes.c_int, ctypes.c_double
+    L.ref_dim_tables.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip]
+    L.ref_stiffness.argtypes = [i, i, _dp]
+    L.ref_band_solve.argtypes = [i, i, i, _dp, i, _dp, _dp, _ip]
+    L.ref_ads_solve.argtypes = [i, i, i, _dp]
+    L.ref_heat_steps.argtypes = [i, i, i, d, i, _dp, i]
+    L.ref_heat_rhs.argtypes = [i, i, i, d, _dp, _dp]
+    L.ref_projection_sin.argtypes = [i, i, i, _dp]
+    return L
+
+
+def tables(L, p, E):
+    q, n, ldab = p + 1, E + p, 3 * p + 1
+    out = dict(btab=np.zeros(E * q * 2 * (p + 1)), xq=np.zeros(E * q), w=np.zeros(q), J=np.zeros(E),
+               first_dofs=np.zeros(E, np.int32), mass=np.zeros(ldab * n), lu=np.zeros(ldab * n),
+               ipiv=np.zeros(n, np.int32), stiffness=np.zeros(ldab * n))
+    info = L.ref_dim_tables(p, E, dp(out["btab"]), dp(out["xq"]), dp(out["w"]), dp(out["J"]), ip(out["first_dofs"]),
+                            dp(out["mass"]), dp(out["lu"]), ip(out["ipiv"]))
+    assert info == 0
+    L.ref_stiffness(p, E, dp(out["stiffness"]))
+    out["p"] = np.int32(p)
+    out["elements"] = np.int32(E)
+    return out
+
+
+def band_from_rows(kl, ku, n, rows):
+    """band_matrix{kl, ku, n} filled as make_matrix (solver_test.cpp:31-41)."""
+    ldab = 2 * kl + ku + 1
+    ab = np.zeros(ldab * n)
+    for i, r in enumerate(rows):
+        j = max(i - kl, 0)
+        for v in r:
+            ab[j * ldab + kl + ku + i - j] = v
+            j += 1
+    return ab
+
+
+def known_answers(L):
+    out = {}
+    # tests/ads/solver_test.cpp:63-99 ("ADS one dimension") and the x matrix of :101-255
+    mx = band_from_rows(1, 1, 4, [[1, 2], [2, 3, 1], [-1, 4], [1, 3]])
+    my = band_from_rows(1, 1, 3, [[2, 3], [1, 2, -3], [2, 2]])
+    mz = band_from_rows(1, 1, 2, [[1, 2], [3, 4]])
+    out["mx"], out["my"], out["mz"] = mx, my, mz
+    rhs1 = np.array([5.0, 11, 10, 15])
+    rhs2 = np.array([61.0, 127, 86, 123, -48, -96, -48, -64, 92, 188, 112, 156])
+    rhs3 = np.array([543.0, 1101, 618, 849, -144, -288, -144, -192, 564, 1140, 624, 852,
+                     1147, 2329, 1322, 1821, -336, -672, -336, -448, 1220, 2468, 1360, 1860])
+    out["rhs1"], out["rhs2"], out["rhs3"] = rhs1, rhs2, rhs3
+    out["expected1"] = np.arange(1.0, 5.0)
+    out["expected2"] = np.arange(1.0, 13.0)
+    out["expected3"] = np.arange(1.0, 25.0)
+    # factorise with the reference and solve direction by direction as ads_solve does
+    for name, (a, n) in dict(x=(mx, 4), y=(my, 3), z=(mz, 2)).items():
+        lu = np.zeros_like(a)
+        piv = np.zeros(n, np.int32)
+        b = np.zeros(n)
+        assert L.ref_band_solve(1, 1, n, dp(a), 1, dp(b), dp(lu), ip(piv)) == 0
+        out["lu_" + name], out["ipiv_" + name] = lu, piv
+    x = rhs1.copy()
+    assert L.ref_band_solve(1, 1, 4, dp(mx), 1, dp(x), None, None) == 0
+    out["ref_solution1"] = x
+    # tests/ads/lin/band_solve_test.cpp:15-46: kl=1, ku=2, n=6, 4 right-hand sides
+    kl, ku, n, d = 1, 2, 6, 4
+    ldab = 2 * kl + ku + 1
+    ab = np.zeros(ldab * n)
+    for i in range(n):
+        for j in range(max(0, i - kl), min(n, i + ku + 1)):
+            ab[j * ldab + kl + ku + i - j] = (i + 1) * 10 + j + 1
+    b = np.zeros(n * d)  # column-major n x d
+    for i in range(n):
+        for j in range(d):
+            b[j * n + i] = (j + 1) * (i + 1)
+    sol = np.array([0.230377, -0.126052, -0.0016554, -0.00111222, 0.203603, -0.109609])
+    out["band6_ab"] = ab.copy()
+    out["band6_b"] = b.copy()
+    out["band6_expected"] = np.concatenate([(j + 1) * sol for j in range(d)])
+    lu = np.zeros_like(ab)
+    piv = np.zeros(n, np.int32)
+    x = b.copy()
+    assert L.ref_band_solve(kl, ku, n, dp(ab), d, dp(x), dp(lu), ip(piv)) == 0
+    out["band6_lu"], out["band6_ipiv"], out["band6_ref_x"] = lu, piv, x
+    return out
+
+
+def heat_case(L, nd, p, E, dt, nsteps, seed, mode=0):
+    n = E + p
+    size = n ** nd
+    u0 = np.zeros(size)
+    L.ref_projection_sin(nd, p, E, dp(u0))
+    proj = u0.copy()
+    L.ref_ads_solve(nd, p, E, dp(u0))
+    u0 += (2.0 * splitmix_uniform(seed, size) - 1.0) * 1e-2
+    rhs = np.zeros(size)
+    L.ref_heat_rhs(nd, p, E, dt, dp(u0), dp(rhs))
+    sol = u0.copy()
+    L.ref_ads_solve(nd, p, E, dp(sol))
+    u1 = u0.copy()
+    L.ref_heat_steps(nd, p, E, dt, 1, dp(u1), mode)
+    uN = u0.copy()
+    L.ref_heat_steps(nd, p, E, dt, nsteps, dp(uN), mode)
+    return dict(ndim=np.int32(nd), p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps),
+                seed=np.int64(seed), mode=np.int32(mode), projection=proj, u0=u0, rhs=rhs, solve=sol, u1=u1, uN=uN)
+
+
+CASES = [
+    # (ndim, p, elements, dt, nsteps, seed, mode)
+    (2, 2, 32, 1e-5, 100, 1, 0),   # the 2D heat configuration: 34x34 dofs, 100 steps
+    (2, 4, 10, 1e-5, 10, 2, 0),
+    (3, 2, 4, 1e-6, 3, 3, 1),      # literal heat_3d::compute_rhs
+    (3, 2, 8, 1e-6, 10, 4, 0),
+    (3, 3, 6, 1e-6, 5, 5, 0),
+    (3, 4, 8, 1e-6, 5, 6, 0),      # p = 4: pivoted band LU
+    (3, 2, 16, 1e-6, 3, 7, 0),
+]
+
+
+def main():
+    L = load_ref()
+    for p, E in [(2, 8), (3, 7), (4, 12), (2, 32), (4, 36)]:
+        np.savez_compressed(os.path.join(HERE, f"tables_p{p}_e{E}.npz"), **tables(L, p, E))
+    np.savez_compressed(os.path.join(HERE, "solver_known_answers.npz"), **known_answers(L))
+    for nd, p, E, dt, ns, seed, mode in CASES:
+        name = f"heat_{nd}d_p{p}_e{E}" + ("_literal" if mode else "")
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **heat_case(L, nd, p, E, dt, ns, seed, mode))
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

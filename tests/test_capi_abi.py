@@ -1,0 +1,97 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares;
+argument checks answer with LAPACK-style negative codes before touching the
+GPU.  CPU only: no device call is made."""
+from __future__ import annotations
+
+import ctypes
+import glob
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import ads_gb300 as ads
+from conftest import ROOT
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(adsg_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("adsg_ctx_create", "adsg_heat_rhs", "adsg_ads_solve", "adsg_heat_steps", "adsg_dgbtrs_"):
+        assert must in names
+
+
+@pytest.mark.parametrize("name", declared_functions())
+def test_library_exports(name):
+    lib = ads.library()
+    assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_exported_symbols_are_c_linkage():
+    out = subprocess.run(["nm", "-D", "--defined-only", ads.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (adsg_\w+)", out))
+    assert set(declared_functions()) <= exported
+
+
+def _dgbtrs(trans=b"N", n=4, kl=1, ku=1, nrhs=1, ldab=4, ldb=4, ab=None, ipiv=None, b=None):
+    lib = ads.library()
+    ab = np.zeros(max(ldab, 1) * max(n, 1)) if ab is None else ab
+    ipiv = np.arange(1, max(n, 1) + 1, dtype=np.int32) if ipiv is None else ipiv
+    b = np.zeros(max(ldb, 1) * max(nrhs, 1)) if b is None else b
+    ints = [ctypes.c_int(v) for v in (n, kl, ku, nrhs, ldab, ldb)]
+    info = ctypes.c_int(99)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    code = lib.adsg_dgbtrs_(trans, ctypes.byref(ints[0]), ctypes.byref(ints[1]), ctypes.byref(ints[2]),
+                            ctypes.byref(ints[3]), ab.ctypes.data_as(dp), ctypes.byref(ints[4]),
+                            ipiv.ctypes.data_as(ip), b.ctypes.data_as(dp), ctypes.byref(ints[5]), ctypes.byref(info))
+    return code, info.value
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(trans=b"X"), -1),
+    (dict(n=-1), -2),
+    (dict(kl=-1), -3),
+    (dict(ku=-1), -4),
+    (dict(nrhs=-1), -5),
+    (dict(ldab=2), -7),
+    (dict(ldb=2), -10),
+])
+def test_dgbtrs_argument_errors_match_lapack(kw, code):
+    c, info = _dgbtrs(**kw)
+    assert c == code and info == code
+
+
+def test_dgbtrs_empty_problem_is_a_no_op():
+    assert _dgbtrs(n=0, ldb=1) == (0, 0)
+    assert _dgbtrs(nrhs=0) == (0, 0)
+
+
+def test_ctx_create_rejects_bad_arguments_without_gpu():
+    lib = ads.library()
+    h = ctypes.c_void_p()
+    assert lib.adsg_ctx_create(0, None, ctypes.byref(h)) == -1
+    assert lib.adsg_ctx_create(4, None, ctypes.byref(h)) == -1
+    assert lib.adsg_ctx_create(2, None, ctypes.byref(h)) == -2
+    bad = (ads.DimDesc * 1)()
+    assert lib.adsg_ctx_create(1, bad, ctypes.byref(h)) == -2
+    assert b"invalid" in lib.adsg_last_error()
+
+
+def test_device_entry_points_reject_null_context():
+    lib = ads.library()
+    assert lib.adsg_heat_rhs(None, None, None, 1.0) == -1
+    assert lib.adsg_ads_solve(None, None, None) == -1
+    assert lib.adsg_heat_steps(None, None, 1.0, 1) == -1
+    assert lib.adsg_ctx_destroy(None) == 0

@@ -1,0 +1,279 @@
+"""GPU parity: the CUDA path through the C-ABI against the reference's own
+outputs (golden fixtures) and the CPU oracle, plus size-independent
+properties at the benchmark sizes.  All tests here need a GB300."""
+from __future__ import annotations
+
+import ctypes
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import ads_gb300 as ads
+import oracle
+from _tol import mass_condition, run_tol, step_tol
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+HEAT = sorted(glob.glob(os.path.join(GOLDEN, "heat_*.npz")))
+
+
+def _ctx(nd, p, E):
+    dims = [ads.Dimension(p, E) for _ in range(nd)]
+    return dims, ads.Context(dims)
+
+
+def _conds(dims):
+    return [mass_condition(d.form_band(0).ravel(), d.p) for d in dims]
+
+
+@pytest.mark.parametrize("path", HEAT, ids=os.path.basename)
+def test_heat_against_reference_golden(path, cuda):
+    g = np.load(path)
+    nd, p, E = int(g["ndim"]), int(g["p"]), int(g["elements"])
+    dt, N = float(g["dt"]), int(g["nsteps"])
+    dims, ctx = _ctx(nd, p, E)
+    conds = _conds(dims)
+    u0 = np.ascontiguousarray(g["u0"])
+    rhs = np.zeros_like(u0)
+    ctx.heat_rhs_host(u0, rhs, dt)
+    assert oracle.rel_l2(rhs, g["rhs"]) <= 1e-13
+    x = u0.copy()
+    ctx.ads_solve_host(x)
+    assert oracle.rel_l2(x, g["solve"]) <= step_tol(conds) / 10
+    u1 = u0.copy()
+    ctx.heat_steps_host(u1, dt, 1)
+    assert oracle.rel_l2(u1, g["u1"]) <= step_tol(conds)
+    uN = u0.copy()
+    ctx.heat_steps_host(uN, dt, N)
+    assert oracle.rel_l2(uN, g["uN"]) <= run_tol(conds)
+
+
+@pytest.mark.parametrize("path", HEAT, ids=os.path.basename)
+def test_element_quadrature_against_reference_golden(path, cuda):
+    import torch
+
+    g = np.load(path)
+    nd, p, E = int(g["ndim"]), int(g["p"]), int(g["elements"])
+    dims, ctx = _ctx(nd, p, E)
+    u = torch.from_numpy(g["u0"]).to(cuda)
+    r = torch.empty_like(u)
+    ctx.heat_rhs_elem(u, r, float(g["dt"]))
+    ctx.synchronize()
+    assert oracle.rel_l2(r.cpu().numpy(), g["rhs"]) <= 1e-13
+
+
+def test_element_quadrature_with_kappa_against_oracle(cuda):
+    import torch
+
+    p, E = 2, 7
+    dims, ctx = _ctx(3, p, E)
+    pr = oracle.Problem([p] * 3, [E] * 3)
+    rng = np.random.default_rng(11)
+    u = rng.uniform(-1, 1, pr.size)
+    kappa = 1.0 + 0.5 * rng.uniform(-1, 1, pr.size)
+    ref = pr.heat_rhs_kappa(u, kappa, 1e-3)
+    ud, kd = torch.from_numpy(u).to(cuda), torch.from_numpy(kappa).to(cuda)
+    r = torch.empty_like(ud)
+    ctx.heat_rhs_elem(ud, r, 1e-3, kappa=kd)
+    ctx.synchronize()
+    assert oracle.rel_l2(r.cpu().numpy(), ref) <= 1e-13
+
+
+def _raw_dim(n, lu, ipiv, kl=1, ku=1):
+    """A descriptor for a bare factorised band (basis tables of a p = 1 space
+    with n-1 elements; only the solve uses the band)."""
+    E = n - 1
+    keep = dict(btab=np.full(E * 2 * 2 * 2, 0.5), w=np.ones(2), J=np.full(E, 0.5),
+                first=np.arange(E, dtype=np.int32), lu=np.ascontiguousarray(lu, np.float64),
+                ipiv=np.ascontiguousarray(ipiv, np.int32))
+    d = ads.DimDesc()
+    d.p, d.elements, d.quad_order, d.n = 1, E, 2, n
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    d.btab = keep["btab"].ctypes.data_as(dp)
+    d.w = keep["w"].ctypes.data_as(dp)
+    d.J = keep["J"].ctypes.data_as(dp)
+    d.first_dofs = keep["first"].ctypes.data_as(ip)
+    d.kl, d.ku, d.ldab = kl, ku, 2 * kl + ku + 1
+    d.lu = keep["lu"].ctypes.data_as(dp)
+    d.ipiv = keep["ipiv"].ctypes.data_as(ip)
+    return d, keep
+
+
+def _raw_ctx(descs):
+    arr = (ads.DimDesc * len(descs))(*descs)
+    h = ctypes.c_void_p()
+    ads._check(ads.library().adsg_ctx_create(len(descs), arr, ctypes.byref(h)))
+    return h
+
+
+def test_known_answers_ads_solve_1d_2d_3d(cuda):
+    """solver_test.cpp:63-255 through adsg_ads_solve_host."""
+    g = np.load(os.path.join(GOLDEN, "solver_known_answers.npz"))
+    lib = ads.library()
+    dx, kx = _raw_dim(4, g["lu_x"], g["ipiv_x"])
+    dy, ky = _raw_dim(3, g["lu_y"], g["ipiv_y"])
+    dz, kz = _raw_dim(2, g["lu_z"], g["ipiv_z"])
+    for descs, rhs, exp in (([dx], "rhs1", "expected1"), ([dx, dy], "rhs2", "expected2"),
+                            ([dx, dy, dz], "rhs3", "expected3")):
+        h = _raw_ctx(descs)
+        b = np.ascontiguousarray(g[rhs], np.float64).copy()
+        ads._check(lib.adsg_ads_solve_host(h, b.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        lib.adsg_ctx_destroy(h)
+        np.testing.assert_allclose(b, g[exp], rtol=1e-13)
+
+
+def test_known_answers_dgbtrs_drop_in(cuda):
+    """band_solve_test.cpp:15-46 through the LAPACK-signature entry point."""
+    g = np.load(os.path.join(GOLDEN, "solver_known_answers.npz"))
+    b = g["band6_b"].copy()
+    info = ads.dgbtrs("N", 6, 1, 2, 4, g["band6_lu"], 5, g["band6_ipiv"], b, 6)
+    assert info == 0
+    np.testing.assert_allclose(b, g["band6_expected"], atol=1e-5)
+    assert oracle.rel_l2(b, g["band6_ref_x"]) <= 1e-14
+    x = g["rhs1"].copy()
+    assert ads.dgbtrs("N", 4, 1, 1, 1, g["lu_x"], 4, g["ipiv_x"], x, 4) == 0
+    np.testing.assert_allclose(x, g["expected1"], rtol=1e-13)
+
+
+def test_dgbtrs_pivoted_p4_many_columns_and_ldb(cuda):
+    pr = oracle.Problem([4], [36])
+    d = pr.dim(0)
+    n, ldab, ldb, nrhs = 40, 13, 43, 77
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal(ldb * nrhs)
+    for trans in ("N", "T"):
+        ref = oracle.dgbtrs(trans, n, 4, 4, nrhs, d["lu"], ldab, d["ipiv"], b, ldb)
+        x = b.copy()
+        assert ads.dgbtrs(trans, n, 4, 4, nrhs, d["lu"], ldab, d["ipiv"], x, ldb) == 0
+        assert oracle.rel_l2(x, ref) <= 1e-13
+        pad = np.ones(ldb, bool)
+        pad[:n] = False
+        np.testing.assert_array_equal(x.reshape(nrhs, ldb)[:, pad], b.reshape(nrhs, ldb)[:, pad])
+
+
+@pytest.mark.parametrize("p,elements", [
+    ((2, 2, 2), (5, 7, 9)),
+    ((2, 3, 4), (6, 5, 4)),
+    ((4, 4), (33, 1)),
+    ((3,), (40,)),
+    ((1, 1, 1), (3, 4, 5)),
+])
+def test_uneven_grids_against_oracle(p, elements, cuda):
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    pr = oracle.Problem(list(p), list(elements))
+    conds = _conds(dims)
+    rng = np.random.default_rng(sum(elements))
+    u = rng.uniform(-1, 1, pr.size)
+    dt = 1e-5
+    r = np.zeros_like(u)
+    ctx.heat_rhs_host(u, r, dt)
+    assert oracle.rel_l2(r, pr.heat_rhs(u, dt)) <= 1e-13
+    x = u.copy()
+    ctx.ads_solve_host(x)
+    assert oracle.rel_l2(x, pr.ads_solve(u)) <= step_tol(conds) / 10
+    s = u.copy()
+    ctx.heat_steps_host(s, dt, 3)
+    assert oracle.rel_l2(s, pr.heat_steps(u, dt, 3)) <= step_tol(conds) * 3
+
+
+def test_transposed_solve_is_adjoint(cuda):
+    import torch
+
+    dims, ctx = _ctx(3, 4, 9)
+    rng = np.random.default_rng(2)
+    a = torch.from_numpy(rng.standard_normal(ctx.size)).to(cuda)
+    b = torch.from_numpy(rng.standard_normal(ctx.size)).to(cuda)
+    xa, xb = a.clone(), b.clone()
+    ctx.ads_solve(xa)
+    ctx.ads_solve_t(xb)
+    ctx.synchronize()
+    lhs, rhs = float((xa * b).sum()), float((a * xb).sum())
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+# --- full-size properties (the 3D p=2 128^3 benchmark grid) ------------------
+
+@pytest.fixture(scope="module")
+def big(cuda):
+    import torch
+
+    dims, ctx = _ctx(3, 2, 128)
+    from ads_gb300 import inputs
+
+    u = torch.from_numpy(inputs.initial_field(dims, seed=1)).to(cuda)
+    return dims, ctx, u
+
+
+def test_full_size_mass_solve_round_trip(big):
+    import torch
+
+    dims, ctx, u = big
+    Mu = torch.empty_like(u)
+    ctx.heat_rhs(u, Mu, 0.0)  # dt = 0: rhs = (Mx (x) My (x) Mz) u
+    ctx.ads_solve(Mu)
+    ctx.synchronize()
+    err = float(torch.linalg.norm(Mu - u) / torch.linalg.norm(u))
+    assert err <= step_tol(_conds(dims))
+
+
+def test_full_size_linearity_and_determinism(big):
+    import torch
+
+    dims, ctx, u = big
+    v = torch.roll(u, 7) * 0.5
+    r1, r2, r3 = torch.empty_like(u), torch.empty_like(u), torch.empty_like(u)
+    ctx.heat_rhs(u, r1, 1e-6)
+    ctx.heat_rhs(v, r2, 1e-6)
+    w = 2.0 * u - 3.0 * v
+    ctx.heat_rhs(w, r3, 1e-6)
+    ctx.synchronize()
+    lin = float(torch.linalg.norm(r3 - (2.0 * r1 - 3.0 * r2)) / torch.linalg.norm(r3))
+    assert lin <= 1e-13
+    s1, s2 = u.clone(), u.clone()
+    ctx.heat_steps(s1, 1e-6, 4)
+    ctx.heat_steps(s2, 1e-6, 4)
+    ctx.synchronize()
+    assert torch.equal(s1, s2)
+
+
+def test_full_size_graph_steps_equal_explicit_loop(big):
+    import torch
+
+    dims, ctx, u = big
+    a = u.clone()
+    ctx.heat_steps(a, 1e-6, 3)
+    b = u.clone()
+    tmp = torch.empty_like(u)
+    for _ in range(3):
+        ctx.heat_rhs(b, tmp, 1e-6)
+        ctx.ads_solve(tmp)
+        b, tmp = tmp, b
+    ctx.synchronize()
+    assert torch.equal(a, b)
+
+
+def test_full_size_element_and_factored_rhs_agree(big):
+    import torch
+
+    dims, ctx, u = big
+    r1, r2 = torch.empty_like(u), torch.empty_like(u)
+    ctx.heat_rhs(u, r1, 1e-6)
+    ctx.heat_rhs_elem(u, r2, 1e-6)
+    ctx.synchronize()
+    assert float(torch.linalg.norm(r1 - r2) / torch.linalg.norm(r1)) <= 1e-13
+
+
+def test_full_size_against_oracle_one_step_sampled(big):
+    """One full 130^3 step against the multi-threaded oracle."""
+    dims, ctx, u = big
+    pr = oracle.Problem([2] * 3, [128] * 3)
+    u0 = u.cpu().numpy()
+    ref = pr.heat_steps(u0, 1e-6, 1, nthreads=max(1, min(16, os.cpu_count() or 1)))
+    got = u0.copy()
+    ctx.heat_steps_host(got, 1e-6, 1)
+    assert oracle.rel_l2(got, ref) <= step_tol(_conds(dims))
