@@ -95,13 +95,14 @@ struct solve_tables {
     std::vector<double> lmul, ucol, rdiag;
     std::vector<int> piv, uext;
     int kl = 0, w = 0;
+    int fwd_fast = 0, bwd_fast = 0;
 };
 
 int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t) {
     const int kv = kl + ku;
     t.kl = std::max(kl, 1);
     t.w = std::max(kv, 1);
-    t.lmul.assign(static_cast<size_t>(n) * t.kl, 0.0);
+    t.lmul.assign(static_cast<size_t>(n + 16) * t.kl, 0.0);  // padded for block-wise prefetch
     t.ucol.assign(static_cast<size_t>(n) * t.w, 0.0);
     t.rdiag.assign(n, 0.0);
     t.piv.assign(n, 0);
@@ -121,6 +122,13 @@ int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const i
         }
         t.uext[j] = ext;
     }
+    // columns from which the sweeps need no exchange / no extra U terms
+    t.fwd_fast = 0;
+    for (int j = 0; j < n; ++j)
+        if (t.piv[j] != j) t.fwd_fast = j + 1;
+    t.bwd_fast = 0;
+    for (int j = 0; j < n; ++j)
+        if (t.uext[j] > ku) t.bwd_fast = j + 1;
     return 0;
 }
 
@@ -341,6 +349,9 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         }
         D.kl = t.kl;
         D.w = t.w;
+        D.ku_regular = h.ku;
+        D.fwd_fast = t.fwd_fast;
+        D.bwd_fast = t.bwd_fast;
         for (int v : t.uext) c->uext_sum[d] += v;
         const std::vector<double> m = row_band(h, 0);
         const std::vector<double> k = row_band(h, 1);
@@ -646,7 +657,7 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
     if (info) *info = 0;
     if (*n == 0 || *nrhs == 0) return 0;
     for (int j = 0; j < *n; ++j)
-        if (ipiv[j] < 1 || ipiv[j] > *n) return ret(-8, "pivot out of range");
+        if (ipiv[j] < j + 1 || ipiv[j] > std::min(*n, j + 1 + *kl)) return ret(-8, "pivot outside the band of a dgbtrf factorisation");
     solve_tables tb;
     if (make_solve_tables(*n, *kl, *ku, *ldab, ab, ipiv, tb)) return ret(ADSG_ERR_SINGULAR, "zero diagonal in U");
 
@@ -657,6 +668,9 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
     D.n = *n;
     D.kl = tb.kl;
     D.w = tb.w;
+    D.ku_regular = *ku;
+    D.fwd_fast = tb.fwd_fast;
+    D.bwd_fast = tb.bwd_fast;
     double *lmul, *ucol, *rdiag, *x;
     int *piv, *uext;
     cudaError_t e = cudaSuccess;

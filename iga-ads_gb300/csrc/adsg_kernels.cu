@@ -112,7 +112,6 @@ cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* k
 // ---------------------------------------------------------------------------
 constexpr int kPitch = 33;
 
-size_t line_solve_smem_per_warp(int n) { return static_cast<size_t>(n) * kPitch * sizeof(double); }
 
 line_layout make_line_layout(const int* n, int ndim, int d) {
     long long nx = n[0], ny = ndim > 1 ? n[1] : 1, nz = ndim > 2 ? n[2] : 1;
@@ -140,23 +139,37 @@ line_layout make_line_layout(const int* n, int ndim, int d) {
     return L;
 }
 
+// Asynchronous 8-byte global->shared copies (cp.async): every lane issues the
+// copies of its whole tile before waiting once, so the staging of a tile
+// keeps hundreds of loads in flight instead of one per loop iteration.
+__device__ __forceinline__ void async_copy8(double* dst_smem, const double* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 __device__ __forceinline__ void stage_in(const double* __restrict__ data, double* s, const line_layout& L,
                                          int n, long long line0, int nvalid, int lane) {
     if (L.contiguous) {
         const double* src = data + line0 * n;
         for (int l = 0; l < 32; ++l) {
             if (l < nvalid) {
-                for (int j = lane; j < n; j += 32) s[j * kPitch + l] = src[static_cast<long long>(l) * n + j];
+                for (int j = lane; j < n; j += 32) async_copy8(s + j * kPitch + l, src + static_cast<long long>(l) * n + j);
             } else {
                 for (int j = lane; j < n; j += 32) s[j * kPitch + l] = 0.0;
             }
         }
     } else {
         const long long g = line0 + lane;
-        const bool ok = lane < nvalid;
-        const long long base = ok ? (g % L.a) * L.sa + (g / L.a) * L.sb : 0;
-        for (int j = 0; j < n; ++j) s[j * kPitch + lane] = ok ? data[base + j * L.elem_stride] : 0.0;
+        if (lane < nvalid) {
+            const double* src = data + (g % L.a) * L.sa + (g / L.a) * L.sb;
+            for (int j = 0; j < n; ++j) async_copy8(s + j * kPitch + lane, src + j * L.elem_stride);
+        } else {
+            for (int j = 0; j < n; ++j) s[j * kPitch + lane] = 0.0;
+        }
     }
+    async_wait_all();
 }
 
 __device__ __forceinline__ void stage_out(double* __restrict__ data, const double* s, const line_layout& L,
@@ -168,15 +181,18 @@ __device__ __forceinline__ void stage_out(double* __restrict__ data, const doubl
     } else {
         if (lane < nvalid) {
             const long long g = line0 + lane;
-            const long long base = (g % L.a) * L.sa + (g / L.a) * L.sb;
-            for (int j = 0; j < n; ++j) data[base + j * L.elem_stride] = s[j * kPitch + lane];
+            double* dst = data + (g % L.a) * L.sa + (g / L.a) * L.sb;
+#pragma unroll 8
+            for (int j = 0; j < n; ++j) dst[j * L.elem_stride] = s[j * kPitch + lane];
         }
     }
 }
 
-// dgbtrs 'N': L-solve with row exchanges (dgbtrs forward loop + dger), then
-// U-solve (dtbsv 'Upper','N','Non-unit') with the diagonal as a reciprocal.
-__device__ __forceinline__ void sweep_n(double* x, const dim_dev& D) {
+// dgbtrs 'N' on one staged line x[j*kPitch] (generic bands): the L-solve with
+// row exchanges (dgbtrs's forward loop), then the U-solve (dtbsv 'Upper','N',
+// 'Non-unit') with the diagonal applied as a reciprocal, column by column in
+// LAPACK's order, through shared memory.
+__device__ __forceinline__ void sweep_n_generic(double* x, const dim_dev& D) {
     const int n = D.n, kl = D.kl, w = D.w;
     for (int j = 0; j < n - 1; ++j) {
         const int l = __ldg(D.piv + j);
@@ -195,8 +211,150 @@ __device__ __forceinline__ void sweep_n(double* x, const dim_dev& D) {
         x[j * kPitch] = v;
         const int ext = __ldg(D.uext + j);
         const double* uj = D.ucol + static_cast<long long>(j) * w;
+        for (int dd = 1; dd <= ext; ++dd) x[(j - dd) * kPitch] = fma(-v, __ldg(uj + dd - 1), x[(j - dd) * kPitch]);
+    }
+}
+
+// The same substitution with both sweeps held in registers.  One warp-wide
+// FP64 instruction occupies a GB300 SM sub-partition's FP64 unit for ~64
+// cycles, and a line solve has one warp per sub-partition at typical sizes,
+// so every latency on the recurrence stalls the pipe: the forward sweep keeps
+// rows j..j+KL, the backward sweep rows j..j-WW, in registers, the next row
+// is loaded from shared memory (zero padding above and below the line makes
+// every step identical) and the next column's coefficients are fetched a
+// step ahead.  The order of the updates is LAPACK's: row i receives its
+// forward updates from columns i-KL..i-1 and its backward updates from
+// columns i+WW..i+1, in that order.  Columns whose U extent exceeds KU (fill
+// from row exchanges) take a warp-uniform branch for the extra terms.
+template <int KL, int KU, int UNR>
+__device__ __forceinline__ void sweep_n_reg(double* x, const dim_dev& D) {
+    constexpr int WW = KL + KU;
+    const int n = D.n;
+    const int w = D.w;  // U table stride (>= KU); the L table stride equals KL
+    // ---- forward: window f[t] = x[j+t] ----
+    double f[KL + 1];
+#pragma unroll
+    for (int t = 0; t <= KL; ++t) f[t] = x[t * kPitch];
+    int j = 0;
+    // head: columns with row exchanges
+    for (; j < D.fwd_fast; ++j) {
+        const int pc = __ldg(D.piv + j);
+        const double incoming = x[(j + KL + 1) * kPitch];
+        if (pc != j) {
+            const int dsw = pc - j;
+#pragma unroll
+            for (int t = 1; t <= KL; ++t)
+                if (t == dsw) {
+                    const double tmp = f[0];
+                    f[0] = f[t];
+                    f[t] = tmp;
+                }
+        }
+        x[j * kPitch] = f[0];
+        const double ny = -f[0];
+#pragma unroll
+        for (int t = 1; t <= KL; ++t) f[t] = fma(ny, __ldg(D.lmul + static_cast<long long>(j) * KL + t - 1), f[t]);
+#pragma unroll
+        for (int t = 0; t < KL; ++t) f[t] = f[t + 1];
+        f[KL] = incoming;
+    }
+    // body: no exchanges; UNR columns per iteration, coefficients a block ahead
+    {
+        double lnx[UNR * KL];
+        const double* lp = D.lmul + static_cast<long long>(j) * KL;
+#pragma unroll
+        for (int k = 0; k < UNR * KL; ++k) lnx[k] = __ldg(lp + k);  // table padded by UNR columns
+        for (; j + UNR <= n; j += UNR) {
+            double lc[UNR * KL];
+#pragma unroll
+            for (int k = 0; k < UNR * KL; ++k) lc[k] = lnx[k];
+            lp += UNR * KL;
+#pragma unroll
+            for (int k = 0; k < UNR * KL; ++k) lnx[k] = __ldg(lp + k);
+            double inc[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) inc[u] = x[(j + u + KL + 1) * kPitch];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                x[(j + u) * kPitch] = f[0];
+                const double ny = -f[0];
+#pragma unroll
+                for (int t = 1; t <= KL; ++t) f[t] = fma(ny, lc[u * KL + t - 1], f[t]);
+#pragma unroll
+                for (int t = 0; t < KL; ++t) f[t] = f[t + 1];
+                f[KL] = inc[u];
+            }
+        }
+    }
+    for (; j < n; ++j) {
+        const double incoming = x[(j + KL + 1) * kPitch];
+        x[j * kPitch] = f[0];
+        const double ny = -f[0];
+#pragma unroll
+        for (int t = 1; t <= KL; ++t) f[t] = fma(ny, __ldg(D.lmul + static_cast<long long>(j) * KL + t - 1), f[t]);
+#pragma unroll
+        for (int t = 0; t < KL; ++t) f[t] = f[t + 1];
+        f[KL] = incoming;
+    }
+    // ---- backward: window b[d] = x[j-d] (pending) ----
+    double b[WW + 1];
+#pragma unroll
+    for (int d = 0; d <= WW; ++d) b[d] = x[(n - 1 - d) * kPitch];
+    j = n - 1;
+    // body: columns whose U extent is <= KU, UNR per iteration
+    {
+        double rnx[UNR], unx[UNR * KU];
+        auto load_block = [&](int jj, double* r, double* uu) {
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const int c = max(jj - u, 0);
+                r[u] = __ldg(D.rdiag + c);
+#pragma unroll
+                for (int d = 0; d < KU; ++d) uu[u * KU + d] = __ldg(D.ucol + static_cast<long long>(c) * w + d);
+            }
+        };
+        load_block(j, rnx, unx);
+        for (; j - UNR + 1 >= D.bwd_fast; j -= UNR) {
+            double rc[UNR], uc[UNR * KU];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) rc[u] = rnx[u];
+#pragma unroll
+            for (int k = 0; k < UNR * KU; ++k) uc[k] = unx[k];
+            load_block(j - UNR, rnx, unx);
+            double inc[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) inc[u] = x[(j - u - WW - 1) * kPitch];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const double v = b[0] * rc[u];
+                x[(j - u) * kPitch] = v;
+                const double nv = -v;
+#pragma unroll
+                for (int d = 1; d <= KU; ++d) b[d] = fma(nv, uc[u * KU + d - 1], b[d]);
+#pragma unroll
+                for (int d = 0; d < WW; ++d) b[d] = b[d + 1];
+                b[WW] = inc[u];
+            }
+        }
+    }
+    // tail: remaining columns, including the ones with row-exchange fill
+    for (; j >= 0; --j) {
+        const double incoming = x[(j - WW - 1) * kPitch];
+        const double v = b[0] * __ldg(D.rdiag + j);
+        x[j * kPitch] = v;
         const double nv = -v;
-        for (int dd = 1; dd <= ext; ++dd) x[(j - dd) * kPitch] = fma(nv, __ldg(uj + dd - 1), x[(j - dd) * kPitch]);
+        const int ec = __ldg(D.uext + j);
+        const double* uj = D.ucol + static_cast<long long>(j) * w;
+#pragma unroll
+        for (int d = 1; d <= KU; ++d) b[d] = fma(nv, __ldg(uj + d - 1), b[d]);
+        if (ec > KU) {
+#pragma unroll
+            for (int d = KU + 1; d <= WW; ++d)
+                if (d <= ec) b[d] = fma(nv, __ldg(uj + d - 1), b[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < WW; ++d) b[d] = b[d + 1];
+        b[WW] = incoming;
     }
 }
 
@@ -226,6 +384,12 @@ __device__ __forceinline__ void sweep_t(double* x, const dim_dev& D) {
     }
 }
 
+// Shared-memory rows reserved above and below each staged line (zeros).
+constexpr int kPadLo = 16, kPadHi = 16;
+
+// KL/KU > 0: register sweeps for bands with kl <= KL, regular U extent <= KU;
+// KL == 0: generic shared-memory sweeps.
+template <int KL, int KU>
 __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ data, dim_dev D, line_layout L,
                                                         int trans) {
     extern __shared__ double smem[];
@@ -233,30 +397,49 @@ __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ dat
     const long long line0 = static_cast<long long>(blockIdx.x) * 32;
     if (line0 >= L.nlines) return;
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
-    double* s = smem;
+    double* s = smem + kPadLo * kPitch;
+    for (int r = 0; r < kPadLo; ++r) smem[r * kPitch + lane] = 0.0;
+    for (int r = 0; r < kPadHi; ++r) s[(D.n + r) * kPitch + lane] = 0.0;
     stage_in(data, s, L, D.n, line0, nvalid, lane);
     __syncwarp();
     if (trans)
         sweep_t(s + lane, D);
+    else if (KL > 0)
+        sweep_n_reg<(KL > 0 ? KL : 1), (KU > 0 ? KU : 1), (KL > 2 ? 4 : 8)>(s + lane, D);
     else
-        sweep_n(s + lane, D);
+        sweep_n_generic(s + lane, D);
     __syncwarp();
     stage_out(data, s, L, D.n, line0, nvalid, lane);
 }
 
-cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
-    if (L.nlines <= 0) return cudaSuccess;
+size_t line_solve_smem_per_warp(int n) { return static_cast<size_t>(n + kPadLo + kPadHi) * kPitch * sizeof(double); }
+
+template <int KL, int KU>
+static cudaError_t line_solve_t(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
     const size_t smem = line_solve_smem_per_warp(d.n);
-    static thread_local size_t configured = 0;
+    static size_t configured = 0;  // per instantiation; set before first use above 48 KB
     if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(line_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(line_solve_kernel<KL, KU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     const long long blocks = (L.nlines + 31) / 32;
-    line_solve_kernel<<<blocks, 32, smem, s>>>(data, d, L, trans);
+    line_solve_kernel<KL, KU><<<blocks, 32, smem, s>>>(data, d, L, trans);
     return cudaGetLastError();
+}
+
+cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
+    if (L.nlines <= 0) return cudaSuccess;
+    // the register sweeps need the L table stride to equal KL and a regular
+    // U extent (columns beyond it take the wide-column branch)
+    const int kl = d.kl, ku = d.ku_regular, w = d.w;
+    if (kl == 1 && ku <= 1 && w <= 2 && w >= 1) return line_solve_t<1, 1>(data, d, L, trans, s);
+    if (kl == 1 && ku <= 2 && w <= 3 && w >= 2) return line_solve_t<1, 2>(data, d, L, trans, s);
+    if (kl == 2 && ku <= 2 && w <= 4 && w >= 2) return line_solve_t<2, 2>(data, d, L, trans, s);
+    if (kl == 3 && ku <= 3 && w <= 6 && w >= 3) return line_solve_t<3, 3>(data, d, L, trans, s);
+    if (kl == 4 && ku <= 4 && w <= 8 && w >= 4) return line_solve_t<4, 4>(data, d, L, trans, s);
+    return line_solve_t<0, 0>(data, d, L, trans, s);
 }
 
 }  // namespace adsg

@@ -10,12 +10,15 @@ namespace adsg {
 // for columns r-p .. r+p (zero outside the matrix).
 struct dim_dev {
     int n = 0, p = 0, kl = 0, w = 0;  // w = kl + ku: widest upper extent of U
+    int ku_regular = 0;               // U extent of all columns but a few (row-exchange fill)
+    int fwd_fast = 0;                 // no row exchange in columns >= fwd_fast
+    int bwd_fast = 0;                 // U extent <= ku_regular in columns >= bwd_fast
     int elements = 0, q = 0;
     const double* mrow = nullptr;   // [n][2p+1] 1D mass matrix
     const double* krow = nullptr;   // [n][2p+1] 1D stiffness matrix
     const double* nrow = nullptr;   // [n][2p+1] M - dt K     (per dt)
     const double* kdt = nullptr;    // [n][2p+1] -dt K        (per dt)
-    const double* lmul = nullptr;   // [n][kl] L multipliers of column j (dgbtrf)
+    const double* lmul = nullptr;   // [n + 16][kl] L multipliers of column j (dgbtrf), zero padded
     const int* piv = nullptr;       // [n] 0-based row exchanged with row j
     const double* ucol = nullptr;   // [n][w] U(j-d, j), d = 1..w
     const int* uext = nullptr;      // [n] number of non-zero U(j-d, j) to apply

@@ -1,0 +1,136 @@
+// ads/gpu.hpp -- header-only C++ bridge from the reference's types to the
+// GB300 engine (include/ads_gb300.h).
+//
+// A C++ program written against marcinlos/iga-ads keeps its ads::dimension
+// objects (src/ads/simulation/dimension.cpp) and swaps the two hot calls:
+//
+//     ads::gpu::context gpu{x, y, z};             // once, after prepare_matrices()
+//     gpu.compute_rhs_heat(u_prev, u, steps.dt);  // instead of heat_3d::compute_rhs
+//     gpu.solve(u);                               // instead of ads_solve(u, buffer, x, y, z)
+//
+// where u / u_prev are ads::lin::tensor objects (anything with data() and
+// size()).  The bridge is duck-typed: a Dimension needs `basis` (basis_data:
+// elements, quad_order, degree, dofs, b[e][q][d][a], w, J, first_dof(e)), `M`
+// (the factorised lin::band_matrix: kl, ku, cols, column_size(),
+// full_buffer()) and `ctx` (lin::solver_ctx: pivot_vector), which is what the
+// reference's ads::dimension has after factorize_matrix().
+//
+// The heavy data stays on the GPU between calls; the host-tensor overloads
+// copy in and out (adsg_*_host).  Device-pointer overloads are available for
+// callers that keep their state in HBM.
+#ifndef ADS_GPU_HPP
+#define ADS_GPU_HPP
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/ads_gb300.h"
+
+namespace ads::gpu {
+
+inline void check(int code) {
+    if (code != 0) throw std::runtime_error("ads_gb300: " + std::to_string(code) + ": " + adsg_last_error());
+}
+
+// Flattened copy of one dimension's tables (basis_data keeps b as nested
+// pointers; the C-ABI takes contiguous arrays).
+struct flat_dim {
+    std::vector<double> btab, w, J, lu;
+    std::vector<int> first, ipiv;
+    adsg_dim_desc desc{};
+
+    template <typename Dimension>
+    explicit flat_dim(const Dimension& d) {
+        const auto& B = d.basis;
+        const int E = B.elements, Q = B.quad_order, P = B.degree;
+        btab.resize(static_cast<size_t>(E) * Q * 2 * (P + 1));
+        for (int e = 0; e < E; ++e)
+            for (int q = 0; q < Q; ++q)
+                for (int k = 0; k < 2; ++k)
+                    for (int a = 0; a <= P; ++a)
+                        btab[((static_cast<size_t>(e) * Q + q) * 2 + k) * (P + 1) + a] = B.b[e][q][k][a];
+        w.assign(B.w, B.w + Q);
+        J.assign(B.J, B.J + E);
+        first.resize(E);
+        for (int e = 0; e < E; ++e) first[e] = B.first_dof(e);
+        const auto& M = d.M;
+        const int ldab = M.column_size();
+        lu.assign(M.full_buffer(), M.full_buffer() + static_cast<size_t>(ldab) * M.cols);
+        ipiv = d.ctx.pivot_vector;
+        desc.p = P;
+        desc.elements = E;
+        desc.quad_order = Q;
+        desc.n = B.dofs;
+        desc.btab = btab.data();
+        desc.w = w.data();
+        desc.J = J.data();
+        desc.first_dofs = first.data();
+        desc.kl = M.kl;
+        desc.ku = M.ku;
+        desc.ldab = ldab;
+        desc.lu = lu.data();
+        desc.ipiv = ipiv.data();
+    }
+};
+
+class context {
+public:
+    template <typename... Dims>
+    explicit context(const Dims&... dims) {
+        std::vector<flat_dim> flat{flat_dim{dims}...};
+        std::vector<adsg_dim_desc> descs;
+        for (auto& f : flat) descs.push_back(f.desc);
+        check(adsg_ctx_create(static_cast<int>(descs.size()), descs.data(), &ctx_));
+    }
+    explicit context(const std::vector<adsg_dim_desc>& descs) {
+        check(adsg_ctx_create(static_cast<int>(descs.size()), descs.data(), &ctx_));
+    }
+    context(const context&) = delete;
+    context& operator=(const context&) = delete;
+    ~context() { adsg_ctx_destroy(ctx_); }
+
+    long long size() const { return adsg_ctx_size(ctx_); }
+    adsg_ctx* handle() { return ctx_; }
+
+    // host tensors (reference lin::tensor or anything with data()/size())
+    template <typename Tensor>
+    void compute_rhs_heat(const Tensor& u_prev, Tensor& rhs, double dt) {
+        require(u_prev.size());
+        require(rhs.size());
+        check(adsg_heat_rhs_host(ctx_, u_prev.data(), rhs.data(), dt));
+    }
+    template <typename Tensor>
+    void solve(Tensor& rhs) {
+        require(rhs.size());
+        check(adsg_ads_solve_host(ctx_, rhs.data()));
+    }
+    template <typename Tensor>
+    void heat_steps(Tensor& u, double dt, int nsteps) {
+        require(u.size());
+        check(adsg_heat_steps_host(ctx_, u.data(), dt, nsteps));
+    }
+
+    // device buffers
+    void compute_rhs_heat_dev(const double* u_prev, double* rhs, double dt) { check(adsg_heat_rhs(ctx_, u_prev, rhs, dt)); }
+    void solve_dev(double* rhs) { check(adsg_ads_solve(ctx_, rhs, nullptr)); }
+    void heat_steps_dev(double* u, double dt, int nsteps) { check(adsg_heat_steps(ctx_, u, dt, nsteps)); }
+    void synchronize() { check(adsg_ctx_synchronize(ctx_)); }
+
+private:
+    void require(long long n) const {
+        if (n != adsg_ctx_size(ctx_)) throw std::invalid_argument("ads::gpu: tensor size does not match the context");
+    }
+    adsg_ctx* ctx_ = nullptr;
+};
+
+// ads_solve(rhs, buf, dims...) of the reference with a GPU context in place
+// of the dim_data pack: the solution is left in rhs (buf is not needed).
+template <typename Tensor>
+void ads_solve(context& gpu, Tensor& rhs) {
+    gpu.solve(rhs);
+}
+
+}  // namespace ads::gpu
+
+#endif  // ADS_GPU_HPP
