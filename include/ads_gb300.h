@@ -169,6 +169,30 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
                  const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
                  int* info);
 
+/* ---- the heat RHS without any allocation --------------------------------
+ * No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc -- code running inside a host application that owns every
+ * device allocation through its own pool, or a latency-critical loop that
+ * must not hit cudaMalloc's implicit device synchronisation.
+ * Computes exactly what adsg_heat_rhs computes, but needs no context: the
+ * dimensions are passed as host descriptors on every call, and the scratch
+ * (four intermediate tensors and the 1D band tables) lives in a file-scope
+ * device array of fixed size (about 17.6 MiB) that every GPU which loads the
+ * library holds until the process exits.  The call enqueues on cuda_stream
+ * (NULL: the legacy default stream) and allocates nothing, neither device nor
+ * host memory.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - All calls share the array: calls whose work overlaps on the GPU race and
+ *    must be serialised by the caller.  Nothing carries over between calls.
+ *  - Tensors above ADSG_NOALLOC_MAX_DOFS dofs or dimensions above
+ *    ADSG_NOALLOC_MAX_N dofs are rejected with -2 and a message. */
+#define ADSG_NOALLOC_MAX_DOFS (1 << 19)
+#define ADSG_NOALLOC_MAX_N 1024
+int adsg_heat_rhs_noalloc(int ndim, const adsg_dim_desc* dims, const double* u_prev_dev, double* rhs_dev,
+                          double dt, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

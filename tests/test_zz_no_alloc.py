@@ -1,0 +1,67 @@
+"""adsg_heat_rhs_noalloc: the heat RHS for callers that cannot allocate device
+memory (a host application that owns all device memory through its own pool,
+or a loop that must not pay cudaMalloc's implicit synchronisation).  It must
+give what adsg_heat_rhs gives, call after call, through the C-ABI.
+
+This file is collected last on purpose: the entry point keeps a process-wide
+device array, and the test must pass both alone in a fresh process and after
+every other test."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import ads_gb300 as ads
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc():
+    fn = ads.library().adsg_heat_rhs_noalloc
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.POINTER(ads.DimDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                   ctypes.c_void_p]
+    return fn
+
+
+def _descs(dims):
+    return (ads.DimDesc * len(dims))(*[d.descriptor() for d in dims])
+
+
+@pytest.mark.parametrize("p,elements", [((2, 2, 2), (30, 24, 20)), ((4, 3), (60, 41)), ((3,), (100,))])
+def test_noalloc_matches_context_rhs_on_consecutive_calls(p, elements, cuda):
+    import torch
+
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    descs = _descs(dims)
+    fn = _noalloc()
+    rng = np.random.default_rng(sum(elements))
+    for call, dt in enumerate((1e-5, 3e-4)):  # two calls in a row, different inputs and dt
+        u = torch.from_numpy(rng.uniform(-1, 1, ctx.size)).to(cuda)
+        ref = torch.empty_like(u)
+        got = torch.full_like(u, float("nan"))
+        ctx.heat_rhs(u, ref, dt)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        code = fn(len(dims), descs, u.data_ptr(), got.data_ptr(), dt, None)
+        assert code == 0, ads.library().adsg_last_error()
+        torch.cuda.synchronize()
+        assert oracle.rel_l2(got.cpu().numpy(), ref.cpu().numpy()) <= 1e-13, f"call {call}"
+
+
+def test_noalloc_rejects_sizes_beyond_its_array(cuda):
+    import torch
+
+    fn = _noalloc()
+    big = [ads.Dimension(2, 98) for _ in range(3)]  # 100^3 dofs > 2^19
+    u = torch.zeros(8, dtype=torch.float64, device=cuda)
+    r = torch.zeros(8, dtype=torch.float64, device=cuda)
+    assert fn(3, _descs(big), u.data_ptr(), r.data_ptr(), 1e-6, None) == -2
+    assert b"ADSG_NOALLOC_MAX_DOFS" in ads.library().adsg_last_error()
+    wide = [ads.Dimension(2, 1100)]  # 1102 dofs along x > 1024
+    assert fn(1, _descs(wide), u.data_ptr(), r.data_ptr(), 1e-6, None) == -2
+    assert b"ADSG_NOALLOC_MAX_N" in ads.library().adsg_last_error()
