@@ -92,6 +92,16 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_enable_stage_timers": (i, [vp, i]),
         "adsg_ctx_stage_times": (i, [vp, _c_double_p, ctypes.POINTER(ctypes.c_longlong)]),
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
+        "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
+        "adsg_batch_create": (i, [i, _c_int_p, _c_int_p, _c_int_p, _c_double_p, ctypes.POINTER(vp)]),
+        "adsg_batch_destroy": (i, [vp]),
+        "adsg_batch_dofs": (ll, [vp, i]),
+        "adsg_batch_set_state": (i, [vp, i, _c_double_p]),
+        "adsg_batch_get_state": (i, [vp, i, _c_double_p]),
+        "adsg_batch_steps": (i, [vp, i]),
+        "adsg_batch_steps_looped": (i, [vp, i]),
+        "adsg_batch_synchronize": (i, [vp]),
+        "adsg_batch_tuning": (i, [vp, _c_int_p, _c_int_p]),
         "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
     }
@@ -260,6 +270,12 @@ class Context:
         _check(library().adsg_ctx_stage_times(self._h, _dptr(ms), n))
         return {STAGES[i]: (float(ms[i]), int(n[i])) for i in range(NSTAGES)}
 
+    def solve_variants(self) -> list:
+        """Line-solve variant per direction picked by the autotuner (see ads_gb300.h)."""
+        v = np.zeros(3, np.int32)
+        _check(library().adsg_ctx_solve_variants(self._h, _iptr(v)))
+        return [int(x) for x in v[: len(self.dims)]]
+
     def stage_work(self) -> dict:
         """{stage: (fp64_flops, hbm_bytes)} of one launch of each stage."""
         f = np.zeros(NSTAGES)
@@ -307,6 +323,71 @@ class Heat:
         self.ctx.heat_steps_host(u, self.dt, steps)
 
 
+class Batch:
+    """Many independent cubic heat problems advanced by one persistent launch
+    per call (adsg_batch_*).  specs: iterable of (ndim, p, elements, dt)."""
+
+    def __init__(self, specs):
+        specs = list(specs)
+        self.specs = specs
+        nd = np.array([s[0] for s in specs], np.int32)
+        pp = np.array([s[1] for s in specs], np.int32)
+        el = np.array([s[2] for s in specs], np.int32)
+        dt = np.array([s[3] for s in specs], np.float64)
+        h = ctypes.c_void_p()
+        _check(library().adsg_batch_create(len(specs), _iptr(nd), _iptr(pp), _iptr(el), _dptr(dt), ctypes.byref(h)))
+        self._h = h
+        self.sizes = [int(library().adsg_batch_dofs(h, i)) for i in range(len(specs))]
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.adsg_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, i: int, u: np.ndarray) -> None:
+        _check(library().adsg_batch_set_state(self._h, i, _dptr(_host(u))))
+
+    def get_state(self, i: int) -> np.ndarray:
+        out = np.empty(self.sizes[i])
+        _check(library().adsg_batch_get_state(self._h, i, _dptr(out)))
+        return out
+
+    def steps(self, nsteps: int) -> None:
+        _check(library().adsg_batch_steps(self._h, int(nsteps)))
+
+    def steps_looped(self, nsteps: int) -> None:
+        _check(library().adsg_batch_steps_looped(self._h, int(nsteps)))
+
+    def synchronize(self) -> None:
+        _check(library().adsg_batch_synchronize(self._h))
+
+    def tuning(self) -> dict:
+        b = ctypes.c_int()
+        g = ctypes.c_int()
+        _check(library().adsg_batch_tuning(self._h, ctypes.byref(b), ctypes.byref(g)))
+        return {"blocks_per_sm": b.value, "graph": bool(g.value)}
+
+
+def batch_specs(seed: int = 0, n2d: int = 32, n3d: int = 32, dt: float = 1e-6):
+    """The mixed batch: n2d 2D instances with 32..512 elements per side and n3d
+    3D instances with 16..96, degrees uniform in {2, 3, 4}, drawn from a seed."""
+    from .inputs import splitmix_uniform
+
+    r = splitmix_uniform(seed, 2 * (n2d + n3d))
+    specs = []
+    for i in range(n2d + n3d):
+        two = i < n2d
+        lo, hi = (32, 512) if two else (16, 96)
+        e = lo + min(int(r[2 * i] * (hi - lo + 1)), hi - lo)
+        p = 2 + min(int(r[2 * i + 1] * 3), 2)
+        specs.append((2 if two else 3, p, e, dt))
+    return specs
+
+
 def ads_solve(ctx: Context, rhs, buf=None) -> None:
     """ads::ads_solve(rhs, buf, dims...) on a device tensor; the solution is left in rhs."""
     ctx.ads_solve(rhs, buf)
@@ -329,4 +410,4 @@ def dgbtrs(trans: str, n: int, kl: int, ku: int, nrhs: int, ab: np.ndarray, ldab
     return info.value
 
 
-__all__ = ["AdsError", "Context", "DimDesc", "Dimension", "Heat", "ads_solve", "dgbtrs", "library", "LIB_PATH"]
+__all__ = ["AdsError", "Batch", "batch_specs", "Context", "DimDesc", "Dimension", "Heat", "ads_solve", "dgbtrs", "library", "LIB_PATH"]

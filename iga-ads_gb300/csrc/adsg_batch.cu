@@ -1,0 +1,386 @@
+// Batched engine: many independent heat simulations of uneven sizes and
+// degrees advanced together.  Each run of steps is ONE persistent cooperative
+// launch (all stages of all instances, grid barriers between stages),
+// replayed from a CUDA graph; its grid size is chosen by an autotuner that
+// times every feasible blocks-per-SM count on the batch itself.  The
+// reference has no batched form: its unit of work is one simulation object
+// driven by simulation_base::run (src/ads/simulation/simulation_base.cpp:11-20).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "adsg_internal.hpp"
+#include "adsg_kernels.cuh"
+
+using namespace adsg;
+
+namespace {
+
+struct arena {
+    std::vector<void*> blocks;
+    ~arena() {
+        for (void* p : blocks) cudaFree(p);
+    }
+    template <typename T>
+    cudaError_t alloc(T** out, size_t count) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        blocks.push_back(p);
+        *out = static_cast<T*>(p);
+        return cudaSuccess;
+    }
+    template <typename T>
+    cudaError_t upload(T** out, const T* src, size_t count, cudaStream_t s) {
+        cudaError_t e = alloc(out, count);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpyAsync(*out, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+};
+
+constexpr int kUnitsPerItem = 256;
+
+}  // namespace
+
+struct adsg_batch {
+    int count = 0;
+    std::vector<dim_host> dims;
+    std::vector<batch_inst> inst;  // host copies (device pointers inside)
+    std::vector<double> dt;
+    batch_dev B;
+    arena mem;
+    cudaStream_t stream = nullptr;
+    int par = 0;            // which buffer holds the state
+    int blocks_per_sm = 1;  // autotuned
+    int sms = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = -1, graph_par = -1;
+    bool graph_ok = true;
+    std::vector<adsg_ctx*> ctxs;  // plain contexts for the per-instance loop (created on demand)
+
+    ~adsg_batch() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto* c : ctxs) adsg_ctx_destroy(c);
+        if (graph) cudaGraphExecDestroy(graph);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int launch_steps(adsg_batch* b, int nsteps, int blocks_per_sm) {
+    void* args[] = {&b->B, &nsteps, &b->par};
+    const dim3 grid(b->sms * blocks_per_sm), block(256);
+    cudaError_t e = cudaLaunchCooperativeKernel(batch_kernel_symbol(), grid, block, args, 0, b->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "cooperative launch");
+    return 0;
+}
+
+int check_error_word(adsg_batch* b) {
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, b->B.err, sizeof(int), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "batch synchronize");
+    if (err) {
+        cudaMemsetAsync(b->B.err, 0, sizeof(int), b->stream);
+        cudaMemsetAsync(b->B.bar_count, 0, sizeof(unsigned), b->stream);
+        cudaStreamSynchronize(b->stream);
+        return fail(ADSG_ERR_DEVICE, "a grid barrier of the batched kernel timed out");
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int adsg_batch_create(int count, const int* ndim, const int* p, const int* elements, const double* dt,
+                      adsg_batch** out) {
+    if (count < 1) return fail(-1, "count must be >= 1");
+    if (!ndim) return fail(-2, "ndim is NULL");
+    if (!p) return fail(-3, "p is NULL");
+    if (!elements) return fail(-4, "elements is NULL");
+    if (!dt) return fail(-5, "dt is NULL");
+    if (!out) return fail(-6, "out is NULL");
+    *out = nullptr;
+    for (int i = 0; i < count; ++i) {
+        if (ndim[i] != 2 && ndim[i] != 3) return fail(-2, "batched instances are 2D or 3D");
+        if (p[i] < 1 || p[i] > 4) return fail(-3, "batched instances need 1 <= p <= 4");
+        if (elements[i] < 1) return fail(-4, "elements must be >= 1");
+        if (!std::isfinite(dt[i])) return fail(-5, "dt must be finite");
+    }
+    auto* b = new (std::nothrow) adsg_batch;
+    if (!b) return fail(ADSG_ERR_NOMEM, "host allocation failed");
+    b->count = count;
+    b->dims.resize(count);
+    b->inst.resize(count);
+    b->dt.assign(dt, dt + count);
+    auto bail = [&](int code) {
+        delete b;
+        return code;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamDefault);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "stream"));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return bail(fail(ADSG_ERR_UNSUPPORTED, "device lacks cooperative launch"));
+
+    std::vector<int> prefix(6 * (count + 1), 0);
+    for (int i = 0; i < count; ++i) {
+        dim_host& h = b->dims[i];
+        if (!build_dimension(h, p[i], elements[i], 0.0, 1.0, p[i] + 1))
+            return bail(fail(ADSG_ERR_SINGULAR, "dimension set-up failed"));
+        adsg_dim_desc d{};
+        d.p = h.p;
+        d.elements = h.elements;
+        d.quad_order = h.q;
+        d.n = h.n;
+        d.btab = h.btab.data();
+        d.w = h.w.data();
+        d.J = h.J.data();
+        d.first_dofs = h.first_dofs.data();
+        d.kl = h.kl;
+        d.ku = h.ku;
+        d.ldab = h.ldab;
+        d.lu = h.lu.data();
+        d.ipiv = h.ipiv.data();
+        solve_tables t;
+        if (make_solve_tables(h.n, h.kl, h.ku, h.ldab, h.lu.data(), h.ipiv.data(), t))
+            return bail(fail(ADSG_ERR_SINGULAR, "zero pivot"));
+        std::vector<double> m = row_band(d, 0), k = row_band(d, 1), nr(m.size()), kd(m.size());
+        for (size_t q = 0; q < m.size(); ++q) {
+            nr[q] = std::fma(-dt[i], k[q], m[q]);
+            kd[q] = -dt[i] * k[q];
+        }
+        batch_inst& I = b->inst[i];
+        I.ndim = ndim[i];
+        I.p = p[i];
+        I.n = h.n;
+        I.size = ndim[i] == 3 ? static_cast<long long>(h.n) * h.n * h.n : static_cast<long long>(h.n) * h.n;
+        dim_dev& D = I.dim;
+        D.n = h.n;
+        D.p = h.p;
+        D.kl = t.kl;
+        D.w = t.w;
+        D.ku_regular = h.ku;
+        D.fwd_fast = t.fwd_fast;
+        D.bwd_fast = t.bwd_fast;
+        D.elements = h.elements;
+        D.q = h.q;
+        double *mrow, *krow, *nrow, *kdt, *lmul, *ucol, *rdiag;
+        int *piv, *uext;
+        arena& A = b->mem;
+        cudaStream_t s = b->stream;
+        e = A.upload(&mrow, m.data(), m.size(), s);
+        if (e == cudaSuccess) e = A.upload(&krow, k.data(), k.size(), s);
+        if (e == cudaSuccess) e = A.upload(&nrow, nr.data(), nr.size(), s);
+        if (e == cudaSuccess) e = A.upload(&kdt, kd.data(), kd.size(), s);
+        if (e == cudaSuccess) e = A.upload(&lmul, t.lmul.data(), t.lmul.size(), s);
+        if (e == cudaSuccess) e = A.upload(&ucol, t.ucol.data(), t.ucol.size(), s);
+        if (e == cudaSuccess) e = A.upload(&rdiag, t.rdiag.data(), t.rdiag.size(), s);
+        if (e == cudaSuccess) e = A.upload(&piv, t.piv.data(), t.piv.size(), s);
+        if (e == cudaSuccess) e = A.upload(&uext, t.uext.data(), t.uext.size(), s);
+        if (e == cudaSuccess) e = A.alloc(&I.buf[0], I.size);
+        if (e == cudaSuccess) e = A.alloc(&I.buf[1], I.size);
+        for (int q = 0; q < (ndim[i] == 3 ? 4 : 2) && e == cudaSuccess; ++q) e = A.alloc(&I.T[q], I.size);
+        if (e == cudaSuccess) e = cudaMemsetAsync(I.buf[0], 0, sizeof(double) * I.size, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // host staging above dies with this iteration
+        if (e != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
+        D.mrow = mrow;
+        D.krow = krow;
+        D.nrow = nrow;
+        D.kdt = kdt;
+        D.lmul = lmul;
+        D.ucol = ucol;
+        D.rdiag = rdiag;
+        D.piv = piv;
+        D.uext = uext;
+        const long long lines = I.size / I.n;
+        if (I.ndim == 3) {
+            const long long u[6] = {I.size, I.size, I.size, lines, lines, lines};
+            std::copy(u, u + 6, I.units);
+        } else {
+            const long long u[6] = {I.size, 0, I.size, lines, lines, 0};
+            std::copy(u, u + 6, I.units);
+        }
+    }
+    for (int st = 0; st < 6; ++st)
+        for (int i = 0; i < count; ++i) {
+            const long long items = (b->inst[i].units[st] + kUnitsPerItem - 1) / kUnitsPerItem;
+            prefix[st * (count + 1) + i + 1] = prefix[st * (count + 1) + i] + static_cast<int>(items);
+        }
+    batch_inst* dinst = nullptr;
+    int* dprefix = nullptr;
+    unsigned* bar = nullptr;
+    int* err = nullptr;
+    e = b->mem.upload(&dinst, b->inst.data(), b->inst.size(), b->stream);
+    if (e == cudaSuccess) e = b->mem.upload(&dprefix, prefix.data(), prefix.size(), b->stream);
+    if (e == cudaSuccess) e = b->mem.alloc(&bar, 2);
+    if (e == cudaSuccess) e = b->mem.alloc(&err, 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
+    b->B.count = count;
+    b->B.inst = dinst;
+    b->B.prefix = dprefix;
+    b->B.bar_count = bar;
+    b->B.bar_gen = bar + 1;
+    b->B.err = err;
+
+    // autotune the persistent grid on the zero state (the state is reset after)
+    const int maxb = std::max(1, batch_max_blocks_per_sm());
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best = 1e30f;
+    for (int bps = 1; bps <= maxb; ++bps) {
+        int st = launch_steps(b, 1, bps);  // warm-up
+        if (st) break;
+        cudaEventRecord(t0, b->stream);
+        st = launch_steps(b, 2, bps);
+        cudaEventRecord(t1, b->stream);
+        if (st || cudaEventSynchronize(t1) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        if (ms < best) {
+            best = ms;
+            b->blocks_per_sm = bps;
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (int st = check_error_word(b)) return bail(st);
+    for (int i = 0; i < count; ++i) {
+        cudaMemsetAsync(b->inst[i].buf[0], 0, sizeof(double) * b->inst[i].size, b->stream);
+        cudaMemsetAsync(b->inst[i].buf[1], 0, sizeof(double) * b->inst[i].size, b->stream);
+    }
+    b->par = 0;
+    if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
+    *out = b;
+    return 0;
+}
+
+int adsg_batch_destroy(adsg_batch* b) {
+    delete b;
+    return 0;
+}
+
+long long adsg_batch_dofs(const adsg_batch* b, int i) {
+    if (!b || i < 0 || i >= b->count) return -1;
+    return b->inst[i].size;
+}
+
+int adsg_batch_set_state(adsg_batch* b, int i, const double* u_host) {
+    if (!b) return fail(-1, "batch is NULL");
+    if (i < 0 || i >= b->count) return fail(-2, "instance index out of range");
+    if (!u_host) return fail(-3, "u is NULL");
+    cudaError_t e = cudaMemcpyAsync(b->inst[i].buf[b->par], u_host, sizeof(double) * b->inst[i].size,
+                                    cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    return e == cudaSuccess ? 0 : fail_cuda(e, "set state");
+}
+
+int adsg_batch_get_state(adsg_batch* b, int i, double* u_host) {
+    if (!b) return fail(-1, "batch is NULL");
+    if (i < 0 || i >= b->count) return fail(-2, "instance index out of range");
+    if (!u_host) return fail(-3, "u is NULL");
+    cudaError_t e = cudaMemcpyAsync(u_host, b->inst[i].buf[b->par], sizeof(double) * b->inst[i].size,
+                                    cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    return e == cudaSuccess ? 0 : fail_cuda(e, "get state");
+}
+
+int adsg_batch_steps(adsg_batch* b, int nsteps) {
+    if (!b) return fail(-1, "batch is NULL");
+    if (nsteps < 0) return fail(-2, "nsteps must be >= 0");
+    if (nsteps == 0) return 0;
+    if (b->graph_ok && !(b->graph && b->graph_steps == nsteps && b->graph_par == b->par)) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            const int st = launch_steps(b, nsteps, b->blocks_per_sm);
+            const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+            if (st == 0 && ec == cudaSuccess && g && cudaGraphInstantiate(&b->graph, g, 0) == cudaSuccess) {
+                b->graph_steps = nsteps;
+                b->graph_par = b->par;
+            } else {
+                b->graph = nullptr;
+                b->graph_ok = false;  // fall back to direct cooperative launches
+            }
+            if (g) cudaGraphDestroy(g);
+        } else {
+            b->graph_ok = false;
+        }
+        cudaGetLastError();
+    }
+    if (b->graph) {
+        cudaError_t e = cudaGraphLaunch(b->graph, b->stream);
+        if (e != cudaSuccess) return fail_cuda(e, "graph launch");
+    } else {
+        if (int st = launch_steps(b, nsteps, b->blocks_per_sm)) return st;
+    }
+    b->par ^= (nsteps & 1);
+    return 0;
+}
+
+int adsg_batch_steps_looped(adsg_batch* b, int nsteps) {
+    if (!b) return fail(-1, "batch is NULL");
+    if (nsteps < 0) return fail(-2, "nsteps must be >= 0");
+    if (b->ctxs.empty()) {
+        b->ctxs.assign(b->count, nullptr);
+        for (int i = 0; i < b->count; ++i) {
+            const dim_host& h = b->dims[i];
+            adsg_dim_desc d{};
+            d.p = h.p;
+            d.elements = h.elements;
+            d.quad_order = h.q;
+            d.n = h.n;
+            d.btab = h.btab.data();
+            d.w = h.w.data();
+            d.J = h.J.data();
+            d.first_dofs = h.first_dofs.data();
+            d.kl = h.kl;
+            d.ku = h.ku;
+            d.ldab = h.ldab;
+            d.lu = h.lu.data();
+            d.ipiv = h.ipiv.data();
+            const adsg_dim_desc descs[3] = {d, d, d};
+            if (int st = adsg_ctx_create(b->inst[i].ndim, descs, &b->ctxs[i])) return st;
+            if (int st = adsg_ctx_set_stream(b->ctxs[i], b->stream)) return st;
+        }
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        for (int i = 0; i < b->count; ++i) {
+            double* cur = b->inst[i].buf[b->par];
+            double* nxt = b->inst[i].buf[b->par ^ 1];
+            if (int st = adsg_heat_rhs(b->ctxs[i], cur, nxt, b->dt[i])) return st;
+            if (int st = adsg_ads_solve(b->ctxs[i], nxt, nullptr)) return st;
+        }
+        b->par ^= 1;
+    }
+    return 0;
+}
+
+int adsg_batch_synchronize(adsg_batch* b) {
+    if (!b) return fail(-1, "batch is NULL");
+    return check_error_word(b);
+}
+
+int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captured) {
+    if (!b) return fail(-1, "batch is NULL");
+    if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
+    if (graph_captured) *graph_captured = b->graph ? 1 : 0;
+    return 0;
+}
+
+}  // extern "C"

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -25,6 +26,70 @@ int fail(int code, const char* msg) {
 int fail_cuda(int err, const char* where) {
     g_last_error = std::string(where) + ": " + cudaGetErrorString(static_cast<cudaError_t>(err));
     return ADSG_ERR_CUDA;
+}
+
+// Row-format band (n rows x (2p+1)) of sum_e sum_q B_a B_b w_q J_e with the
+// basis values (which = 0) or derivatives (which = 1) of a descriptor.
+std::vector<double> row_band(const adsg_dim_desc& d, int which) {
+    const int p = d.p, bw = 2 * p + 1;
+    std::vector<double> rows(static_cast<size_t>(d.n) * bw, 0.0);
+    for (int e = 0; e < d.elements; ++e) {
+        const int f = d.first_dofs[e];
+        for (int k = 0; k < d.quad_order; ++k) {
+            const double* v = d.btab + ((static_cast<size_t>(e) * d.quad_order + k) * 2 + which) * (p + 1);
+            for (int a = 0; a <= p; ++a)
+                for (int b = 0; b <= p; ++b) rows[static_cast<size_t>(f + a) * bw + (b - a + p)] += v[a] * v[b] * d.w[k] * d.J[e];
+        }
+    }
+    return rows;
+}
+
+bool valid_desc(const adsg_dim_desc& d) {
+    if (d.p < 1 || d.p > ADSG_MAX_DEGREE || d.elements < 1 || d.quad_order < 1 || d.n < 1) return false;
+    if (!d.btab || !d.w || !d.J || !d.first_dofs || !d.lu || !d.ipiv) return false;
+    if (d.kl < 0 || d.ku < 0 || d.ldab < 2 * d.kl + d.ku + 1) return false;
+    if (d.kl > 16 || d.kl + d.ku > 32) return false;
+    for (int e = 0; e < d.elements; ++e)
+        if (d.first_dofs[e] < 0 || d.first_dofs[e] + d.p >= d.n) return false;
+    for (int j = 0; j < d.n; ++j)
+        if (d.ipiv[j] < j + 1 || d.ipiv[j] > std::min(d.n, j + 1 + d.kl)) return false;
+    return true;
+}
+
+// Solve tables extracted from a dgbtrf band.
+
+int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t) {
+    const int kv = kl + ku;
+    t.kl = std::max(kl, 1);
+    t.w = std::max(kv, 1);
+    t.lmul.assign(static_cast<size_t>(n + 16) * t.kl, 0.0);  // padded for block-wise prefetch
+    t.ucol.assign(static_cast<size_t>(n) * t.w, 0.0);
+    t.rdiag.assign(n, 0.0);
+    t.piv.assign(n, 0);
+    t.uext.assign(n, 0);
+    for (int j = 0; j < n; ++j) {
+        const double* col = ab + static_cast<size_t>(j) * ldab;
+        const double diag = col[kv];
+        if (diag == 0.0) return j + 1;
+        t.rdiag[j] = 1.0 / diag;
+        t.piv[j] = ipiv[j] - 1;
+        for (int i = 1; i <= kl && j + i < n; ++i) t.lmul[static_cast<size_t>(j) * t.kl + i - 1] = col[kv + i];
+        int ext = 0;
+        for (int d = 1; d <= kv && d <= j; ++d) {
+            const double u = col[kv - d];
+            t.ucol[static_cast<size_t>(j) * t.w + d - 1] = u;
+            if (u != 0.0) ext = d;
+        }
+        t.uext[j] = ext;
+    }
+    // columns from which the sweeps need no exchange / no extra U terms
+    t.fwd_fast = 0;
+    for (int j = 0; j < n; ++j)
+        if (t.piv[j] != j) t.fwd_fast = j + 1;
+    t.bwd_fast = 0;
+    for (int j = 0; j < n; ++j)
+        if (t.uext[j] > ku) t.bwd_fast = j + 1;
+    return 0;
 }
 
 }  // namespace adsg
@@ -61,76 +126,6 @@ struct dev_arena {
         return cudaMemcpyAsync(*out, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
     }
 };
-
-// Row-format band (n rows x (2p+1)) of sum_e sum_q B_a B_b w_q J_e with the
-// basis values (which = 0) or derivatives (which = 1) of a descriptor.
-std::vector<double> row_band(const adsg_dim_desc& d, int which) {
-    const int p = d.p, bw = 2 * p + 1;
-    std::vector<double> rows(static_cast<size_t>(d.n) * bw, 0.0);
-    for (int e = 0; e < d.elements; ++e) {
-        const int f = d.first_dofs[e];
-        for (int k = 0; k < d.quad_order; ++k) {
-            const double* v = d.btab + ((static_cast<size_t>(e) * d.quad_order + k) * 2 + which) * (p + 1);
-            for (int a = 0; a <= p; ++a)
-                for (int b = 0; b <= p; ++b) rows[static_cast<size_t>(f + a) * bw + (b - a + p)] += v[a] * v[b] * d.w[k] * d.J[e];
-        }
-    }
-    return rows;
-}
-
-bool valid_desc(const adsg_dim_desc& d) {
-    if (d.p < 1 || d.p > ADSG_MAX_DEGREE || d.elements < 1 || d.quad_order < 1 || d.n < 1) return false;
-    if (!d.btab || !d.w || !d.J || !d.first_dofs || !d.lu || !d.ipiv) return false;
-    if (d.kl < 0 || d.ku < 0 || d.ldab < 2 * d.kl + d.ku + 1) return false;
-    if (d.kl > 16 || d.kl + d.ku > 32) return false;
-    for (int e = 0; e < d.elements; ++e)
-        if (d.first_dofs[e] < 0 || d.first_dofs[e] + d.p >= d.n) return false;
-    for (int j = 0; j < d.n; ++j)
-        if (d.ipiv[j] < j + 1 || d.ipiv[j] > std::min(d.n, j + 1 + d.kl)) return false;
-    return true;
-}
-
-// Solve tables extracted from a dgbtrf band.
-struct solve_tables {
-    std::vector<double> lmul, ucol, rdiag;
-    std::vector<int> piv, uext;
-    int kl = 0, w = 0;
-    int fwd_fast = 0, bwd_fast = 0;
-};
-
-int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t) {
-    const int kv = kl + ku;
-    t.kl = std::max(kl, 1);
-    t.w = std::max(kv, 1);
-    t.lmul.assign(static_cast<size_t>(n + 16) * t.kl, 0.0);  // padded for block-wise prefetch
-    t.ucol.assign(static_cast<size_t>(n) * t.w, 0.0);
-    t.rdiag.assign(n, 0.0);
-    t.piv.assign(n, 0);
-    t.uext.assign(n, 0);
-    for (int j = 0; j < n; ++j) {
-        const double* col = ab + static_cast<size_t>(j) * ldab;
-        const double diag = col[kv];
-        if (diag == 0.0) return j + 1;
-        t.rdiag[j] = 1.0 / diag;
-        t.piv[j] = ipiv[j] - 1;
-        for (int i = 1; i <= kl && j + i < n; ++i) t.lmul[static_cast<size_t>(j) * t.kl + i - 1] = col[kv + i];
-        int ext = 0;
-        for (int d = 1; d <= kv && d <= j; ++d) {
-            const double u = col[kv - d];
-            t.ucol[static_cast<size_t>(j) * t.w + d - 1] = u;
-            if (u != 0.0) ext = d;
-        }
-        t.uext[j] = ext;
-    }
-    // columns from which the sweeps need no exchange / no extra U terms
-    t.fwd_fast = 0;
-    for (int j = 0; j < n; ++j)
-        if (t.piv[j] != j) t.fwd_fast = j + 1;
-    t.bwd_fast = 0;
-    for (int j = 0; j < n; ++j)
-        if (t.uext[j] > ku) t.bwd_fast = j + 1;
-    return 0;
-}
 
 }  // namespace
 
@@ -286,6 +281,54 @@ int enqueue_solve(adsg_ctx* c, double* x, int trans) {
     return 0;
 }
 
+// Autotuner: time every applicable line-solve variant per direction on the
+// context's own state buffer (zeros) and keep the fastest.  ADSG_SOLVE_VARIANT
+// (0..3) forces one variant where applicable.
+int autotune_solves(adsg_ctx* c) {
+    const char* force = std::getenv("ADSG_SOLVE_VARIANT");
+    int forced = -1;
+    if (force && *force) forced = std::atoi(force);
+    ADSG_CUDA_TRY(cudaMemsetAsync(c->ping, 0, sizeof(double) * c->size, c->stream), "autotune memset");
+    cudaEvent_t a, b;
+    ADSG_CUDA_TRY(cudaEventCreate(&a), "event");
+    ADSG_CUDA_TRY(cudaEventCreate(&b), "event");
+    int rc = 0;
+    for (int d = 0; d < c->ndim && rc == 0; ++d) {
+        dim_dev& D = c->dims[d];
+        const line_layout L = make_line_layout(c->n, c->ndim, d);
+        if (forced >= 0 && forced < SOLVE_NVARIANTS && line_solve_variant_ok(forced, D)) {
+            D.solve_variant = forced;
+            continue;
+        }
+        float best = 1e30f;
+        int best_v = SOLVE_STAGED_1;
+        for (int v = 0; v < SOLVE_NVARIANTS; ++v) {
+            if (!line_solve_variant_ok(v, D)) continue;
+            D.solve_variant = v;
+            cudaError_t e = launch_line_solve(c->ping, D, L, 0, c->stream);  // warm-up
+            if (e != cudaSuccess) continue;
+            cudaEventRecord(a, c->stream);
+            for (int r = 0; r < 3; ++r) launch_line_solve(c->ping, D, L, 0, c->stream);
+            cudaEventRecord(b, c->stream);
+            if (cudaEventSynchronize(b) != cudaSuccess) {
+                rc = fail_cuda(cudaGetLastError(), "autotune");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best) {
+                best = ms;
+                best_v = v;
+            }
+        }
+        D.solve_variant = best_v;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaGetLastError();
+    return rc;
+}
+
 int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     int st = enqueue_rhs(c, prev, next, dt);
     if (st) return st;
@@ -394,6 +437,10 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         if ((e = c->arena.alloc(&c->scratch[i], c->size)) != cudaSuccess) return bail(e, "scratch alloc");
     if ((e = c->arena.alloc(&c->ping, c->size)) != cudaSuccess) return bail(e, "state alloc");
     if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return bail(e, "set-up copies");
+    if (int st = autotune_solves(c)) {
+        delete c;
+        return st;
+    }
     *out = c;
     return 0;
 }
@@ -531,6 +578,13 @@ int adsg_ctx_stage_times(adsg_ctx* ctx, double* ms, long long* launches) {
         ctx->stage_ms[i] = 0.0;
         ctx->stage_launches[i] = 0;
     }
+    return 0;
+}
+
+int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!variants) return fail(-2, "variants is NULL");
+    for (int d = 0; d < 3; ++d) variants[d] = d < ctx->ndim ? ctx->dims[d].solve_variant : -1;
     return 0;
 }
 

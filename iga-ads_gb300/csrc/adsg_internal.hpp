@@ -30,6 +30,20 @@ bool build_dimension(dim_host& d, int p, int elements, double a, double b, int q
 void form_band(const dim_host& d, int which, std::vector<double>& ab);
 int factorize(dim_host& d);
 
+// Solve tables extracted from a dgbtrf band (see make_solve_tables).
+struct solve_tables {
+    std::vector<double> lmul, ucol, rdiag;  // lmul padded by 16 columns
+    std::vector<int> piv, uext;
+    int kl = 0, w = 0;
+    int fwd_fast = 0, bwd_fast = 0;
+};
+
+// Row-format band [n][2p+1] of sum_e sum_q B_a B_b w_q J_e (which: 0 values, 1 derivatives).
+std::vector<double> row_band(const adsg_dim_desc& d, int which);
+bool valid_desc(const adsg_dim_desc& d);
+// 0 on success, else the 1-based column of a zero diagonal.
+int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t);
+
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const char* msg);
 int fail_cuda(int err, const char* where);

@@ -414,6 +414,167 @@ __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ dat
 
 size_t line_solve_smem_per_warp(int n) { return static_cast<size_t>(n + kPadLo + kPadHi) * kPitch * sizeof(double); }
 
+// ---------------------------------------------------------------------------
+// Line solve without shared memory: each lane sweeps its own line directly in
+// global memory (forward results written in place and read back by the same
+// lane in the backward sweep), with the same register windows and column
+// order as sweep_n_reg and the incoming rows prefetched UNR rows ahead.  No
+// shared memory means no occupancy limit from long lines, so short lines and
+// long lines alike fill every sub-partition.
+// ---------------------------------------------------------------------------
+// CG: read the line with L1-bypassing loads (for data written by other blocks
+// earlier in the same launch).
+template <int KL, int KU, int UNR, bool CG = false>
+__device__ __forceinline__ void sweep_global(double* __restrict__ x, const long long es, const dim_dev& D) {
+    constexpr int WW = KL + KU;
+    const int n = D.n;
+    const int w = D.w;
+    auto ld = [&](int r) -> double {
+        if (r < 0 || r >= n) return 0.0;
+        return CG ? __ldcg(x + r * es) : x[r * es];
+    };
+
+    // ---- forward ----
+    double f[KL + 1];
+#pragma unroll
+    for (int t = 0; t <= KL; ++t) f[t] = ld(t);
+    int j = 0;
+    for (; j < D.fwd_fast; ++j) {
+        const int pc = __ldg(D.piv + j);
+        const double incoming = ld(j + KL + 1);
+        if (pc != j) {
+            const int dsw = pc - j;
+#pragma unroll
+            for (int t = 1; t <= KL; ++t)
+                if (t == dsw) {
+                    const double tmp = f[0];
+                    f[0] = f[t];
+                    f[t] = tmp;
+                }
+        }
+        x[j * es] = f[0];
+        const double ny = -f[0];
+#pragma unroll
+        for (int t = 1; t <= KL; ++t) f[t] = fma(ny, __ldg(D.lmul + static_cast<long long>(j) * KL + t - 1), f[t]);
+#pragma unroll
+        for (int t = 0; t < KL; ++t) f[t] = f[t + 1];
+        f[KL] = incoming;
+    }
+    {
+        double pre[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) pre[u] = ld(j + KL + 1 + u);
+        const double* lp = D.lmul + static_cast<long long>(j) * KL;
+        double lnx[UNR * KL];
+#pragma unroll
+        for (int k = 0; k < UNR * KL; ++k) lnx[k] = __ldg(lp + k);
+        for (; j + UNR <= n; j += UNR) {
+            double inc[UNR], lc[UNR * KL];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) inc[u] = pre[u];
+#pragma unroll
+            for (int k = 0; k < UNR * KL; ++k) lc[k] = lnx[k];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) pre[u] = ld(j + UNR + KL + 1 + u);
+            lp += UNR * KL;
+#pragma unroll
+            for (int k = 0; k < UNR * KL; ++k) lnx[k] = __ldg(lp + k);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                x[(j + u) * es] = f[0];
+                const double ny = -f[0];
+#pragma unroll
+                for (int t = 1; t <= KL; ++t) f[t] = fma(ny, lc[u * KL + t - 1], f[t]);
+#pragma unroll
+                for (int t = 0; t < KL; ++t) f[t] = f[t + 1];
+                f[KL] = inc[u];
+            }
+        }
+    }
+    for (; j < n; ++j) {
+        const double incoming = ld(j + KL + 1);
+        x[j * es] = f[0];
+        const double ny = -f[0];
+#pragma unroll
+        for (int t = 1; t <= KL; ++t) f[t] = fma(ny, __ldg(D.lmul + static_cast<long long>(j) * KL + t - 1), f[t]);
+#pragma unroll
+        for (int t = 0; t < KL; ++t) f[t] = f[t + 1];
+        f[KL] = incoming;
+    }
+    // ---- backward ----
+    double b[WW + 1];
+#pragma unroll
+    for (int d = 0; d <= WW; ++d) b[d] = ld(n - 1 - d);
+    j = n - 1;
+    {
+        double pre[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) pre[u] = ld(j - WW - 1 - u);
+        double rnx[UNR], unx[UNR * KU];
+        auto load_block = [&](int jj, double* r, double* uu) {
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const int c = max(jj - u, 0);
+                r[u] = __ldg(D.rdiag + c);
+#pragma unroll
+                for (int d = 0; d < KU; ++d) uu[u * KU + d] = __ldg(D.ucol + static_cast<long long>(c) * w + d);
+            }
+        };
+        load_block(j, rnx, unx);
+        for (; j - UNR + 1 >= D.bwd_fast; j -= UNR) {
+            double inc[UNR], rc[UNR], uc[UNR * KU];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                inc[u] = pre[u];
+                rc[u] = rnx[u];
+            }
+#pragma unroll
+            for (int k = 0; k < UNR * KU; ++k) uc[k] = unx[k];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) pre[u] = ld(j - UNR - WW - 1 - u);
+            load_block(j - UNR, rnx, unx);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const double v = b[0] * rc[u];
+                x[(j - u) * es] = v;
+                const double nv = -v;
+#pragma unroll
+                for (int d = 1; d <= KU; ++d) b[d] = fma(nv, uc[u * KU + d - 1], b[d]);
+#pragma unroll
+                for (int d = 0; d < WW; ++d) b[d] = b[d + 1];
+                b[WW] = inc[u];
+            }
+        }
+    }
+    for (; j >= 0; --j) {
+        const double incoming = ld(j - WW - 1);
+        const double v = b[0] * __ldg(D.rdiag + j);
+        x[j * es] = v;
+        const double nv = -v;
+        const int ec = __ldg(D.uext + j);
+        const double* uj = D.ucol + static_cast<long long>(j) * w;
+#pragma unroll
+        for (int d = 1; d <= KU; ++d) b[d] = fma(nv, __ldg(uj + d - 1), b[d]);
+        if (ec > KU) {
+#pragma unroll
+            for (int d = KU + 1; d <= WW; ++d)
+                if (d <= ec) b[d] = fma(nv, __ldg(uj + d - 1), b[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < WW; ++d) b[d] = b[d + 1];
+        b[WW] = incoming;
+    }
+}
+
+template <int KL, int KU, int UNR>
+__global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restrict__ data, dim_dev D, line_layout L) {
+    const int lane = threadIdx.x & 31;
+    const long long g = static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) * 32 + (threadIdx.x >> 5) * 32 + lane;
+    if (g >= L.nlines) return;
+    double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    sweep_global<KL, KU, UNR>(x, L.elem_stride, D);
+}
+
 template <int KL, int KU>
 static cudaError_t line_solve_t(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
     const size_t smem = line_solve_smem_per_warp(d.n);
@@ -429,17 +590,222 @@ static cudaError_t line_solve_t(double* data, const dim_dev& d, const line_layou
     return cudaGetLastError();
 }
 
+// staged kernel with several warps (one tile each) per block
+template <int KL, int KU, int WPB>
+__global__ void __launch_bounds__(32 * WPB) line_solve_staged_kernel(double* __restrict__ data, dim_dev D, line_layout L) {
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long line0 = (static_cast<long long>(blockIdx.x) * WPB + warp) * 32;
+    if (line0 >= L.nlines) return;
+    const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
+    double* base = smem + static_cast<size_t>(warp) * (D.n + kPadLo + kPadHi) * kPitch;
+    double* s = base + kPadLo * kPitch;
+    for (int r = 0; r < kPadLo; ++r) base[r * kPitch + lane] = 0.0;
+    for (int r = 0; r < kPadHi; ++r) s[(D.n + r) * kPitch + lane] = 0.0;
+    stage_in(data, s, L, D.n, line0, nvalid, lane);
+    __syncwarp();
+    sweep_n_reg<KL, KU, (KL > 2 ? 4 : 8)>(s + lane, D);
+    __syncwarp();
+    stage_out(data, s, L, D.n, line0, nvalid, lane);
+}
+
+template <int KL, int KU, int WPB>
+static cudaError_t staged_t(double* data, const dim_dev& d, const line_layout& L, cudaStream_t s) {
+    const size_t smem = line_solve_smem_per_warp(d.n) * WPB;
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(line_solve_staged_kernel<KL, KU, WPB>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const long long per = 32LL * WPB;
+    line_solve_staged_kernel<KL, KU, WPB><<<(L.nlines + per - 1) / per, 32 * WPB, smem, s>>>(data, d, L);
+    return cudaGetLastError();
+}
+
+template <int KL, int KU>
+static cudaError_t line_solve_variant(int variant, double* data, const dim_dev& d, const line_layout& L, cudaStream_t s) {
+    switch (variant) {
+        case SOLVE_STAGED_1:
+            return line_solve_t<KL, KU>(data, d, L, 0, s);
+        case SOLVE_STAGED_2:
+            return staged_t<KL, KU, 2>(data, d, L, s);
+        case SOLVE_STAGED_4:
+            return staged_t<KL, KU, 4>(data, d, L, s);
+        case SOLVE_GLOBAL_4:
+        default: {
+            const long long per = 128;
+            line_solve_global_kernel<KL, KU, (KL > 2 ? 4 : 8)><<<(L.nlines + per - 1) / per, 128, 0, s>>>(data, d, L);
+            return cudaGetLastError();
+        }
+    }
+}
+
+bool line_solve_variant_ok(int variant, const dim_dev& d) {
+    const int kl = d.kl, ku = d.ku_regular, w = d.w;
+    const bool reg = (kl == 1 && ku <= 2 && w <= 3 && w >= 1) || (kl == 2 && ku <= 2 && w <= 4 && w >= 2) ||
+                     (kl == 3 && ku <= 3 && w <= 6 && w >= 3) || (kl == 4 && ku <= 4 && w <= 8 && w >= 4);
+    if (variant == SOLVE_STAGED_1) return line_solve_smem_per_warp(d.n) <= 227 * 1024;
+    if (!reg) return false;
+    if (variant == SOLVE_STAGED_2) return line_solve_smem_per_warp(d.n) * 2 <= 227 * 1024;
+    if (variant == SOLVE_STAGED_4) return line_solve_smem_per_warp(d.n) * 4 <= 227 * 1024;
+    return true;
+}
+
 cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
     if (L.nlines <= 0) return cudaSuccess;
     // the register sweeps need the L table stride to equal KL and a regular
     // U extent (columns beyond it take the wide-column branch)
     const int kl = d.kl, ku = d.ku_regular, w = d.w;
+    const int v = trans ? SOLVE_STAGED_1 : d.solve_variant;
+    if (!trans && v != SOLVE_STAGED_1 && line_solve_variant_ok(v, d)) {
+        if (kl == 1 && ku <= 1 && w <= 2) return line_solve_variant<1, 1>(v, data, d, L, s);
+        if (kl == 1 && ku <= 2 && w <= 3) return line_solve_variant<1, 2>(v, data, d, L, s);
+        if (kl == 2) return line_solve_variant<2, 2>(v, data, d, L, s);
+        if (kl == 3) return line_solve_variant<3, 3>(v, data, d, L, s);
+        if (kl == 4) return line_solve_variant<4, 4>(v, data, d, L, s);
+    }
     if (kl == 1 && ku <= 1 && w <= 2 && w >= 1) return line_solve_t<1, 1>(data, d, L, trans, s);
     if (kl == 1 && ku <= 2 && w <= 3 && w >= 2) return line_solve_t<1, 2>(data, d, L, trans, s);
     if (kl == 2 && ku <= 2 && w <= 4 && w >= 2) return line_solve_t<2, 2>(data, d, L, trans, s);
     if (kl == 3 && ku <= 3 && w <= 6 && w >= 3) return line_solve_t<3, 3>(data, d, L, trans, s);
     if (kl == 4 && ku <= 4 && w <= 8 && w >= 4) return line_solve_t<4, 4>(data, d, L, trans, s);
     return line_solve_t<0, 0>(data, d, L, trans, s);
+}
+
+// ---------------------------------------------------------------------------
+// Batched engine: many independent cubic heat problems (2D or 3D, p <= 4)
+// advanced by one persistent cooperative launch.  A step is six stages (RHS
+// passes outer / middle / x, then the x, y, z line solves); every stage's work
+// is cut into items of 256 units (outputs for a pass, lines for a solve) over
+// all instances, blocks take items round-robin, and a grid barrier separates
+// the stages.  Inputs written earlier in the same launch are read with
+// L1-bypassing loads.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int P>
+__device__ __forceinline__ void band_one_cg(long long g, const double* in0, const double* in1, double* out0, double* out1,
+                                            const double* A0, const double* A1, const double* B0, int n_axis,
+                                            long long stride) {
+    constexpr int BW = 2 * P + 1;
+    const int r = static_cast<int>((g / stride) % n_axis);
+    const double* a0 = A0 + static_cast<long long>(r) * BW;
+    double acc0 = 0.0, acc1 = 0.0;
+#pragma unroll
+    for (int t = 0; t < BW; ++t) {
+        const int c = r - P + t;
+        if (c >= 0 && c < n_axis) {
+            const long long at = g + static_cast<long long>(t - P) * stride;
+            const double v0 = __ldcg(in0 + at);
+            acc0 = fma(__ldg(a0 + t), v0, acc0);
+            if (out1) acc1 = fma(__ldg(B0 + static_cast<long long>(r) * BW + t), v0, acc1);
+            if (in1) acc0 = fma(__ldg(A1 + static_cast<long long>(r) * BW + t), __ldcg(in1 + at), acc0);
+        }
+    }
+    out0[g] = acc0;
+    if (out1) out1[g] = acc1;
+}
+
+template <int P>
+__device__ __forceinline__ void batch_unit(const batch_inst& I, int stage, long long u, int par) {
+    const double* cur = I.buf[par];
+    double* nxt = I.buf[par ^ 1];
+    const int n = I.n;
+    const dim_dev& D = I.dim;
+    const long long nn = static_cast<long long>(n) * n;
+    if (I.ndim == 3) {
+        switch (stage) {
+            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn); return;
+            case 1: band_one_cg<P>(u, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n); return;
+            case 2: band_one_cg<P>(u, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1); return;
+            case 3: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D); return;
+            case 4: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + (u % n) + (u / n) * nn, n, D); return;
+            default: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, nn, D); return;
+        }
+    } else {
+        switch (stage) {
+            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n); return;
+            case 2: band_one_cg<P>(u, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1); return;
+            case 3: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D); return;
+            case 4: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, n, D); return;
+            default: return;
+        }
+    }
+}
+
+// Grid barrier with a bounded wait: thread 0 of each block arrives on a
+// counter; the last arrival resets it and advances the generation; the
+// others poll the generation with a spin limit, after which they set the
+// error word and the kernel winds down instead of waiting forever.
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err, unsigned nblocks) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned g = atomicAdd(gen, 0u);
+        __threadfence();
+        const unsigned arrived = atomicAdd(count, 1u) + 1u;
+        if (arrived == nblocks) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            long long spins = 0;
+            while (atomicAdd(gen, 0u) == g) {
+                if (++spins > (1LL << 26) || atomicAdd(reinterpret_cast<unsigned*>(err), 0u) != 0u) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__global__ void __launch_bounds__(256) batch_steps_kernel(batch_dev B, int nsteps, int par0) {
+    const unsigned nblocks = gridDim.x;
+    for (int step = 0; step < nsteps; ++step) {
+        const int par = (par0 + step) & 1;
+        for (int stage = 0; stage < 6; ++stage) {
+            const int* pre = B.prefix + stage * (B.count + 1);
+            const int total = pre[B.count];
+            for (int item = blockIdx.x; item < total; item += nblocks) {
+                int lo = 0, hi = B.count;  // find i with pre[i] <= item < pre[i+1]
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (pre[mid] <= item) lo = mid; else hi = mid;
+                }
+                const batch_inst& I = B.inst[lo];
+                const long long u = static_cast<long long>(item - pre[lo]) * 256 + threadIdx.x;
+                if (u < I.units[stage]) {
+                    switch (I.p) {
+                        case 1: batch_unit<1>(I, stage, u, par); break;
+                        case 2: batch_unit<2>(I, stage, u, par); break;
+                        case 3: batch_unit<3>(I, stage, u, par); break;
+                        default: batch_unit<4>(I, stage, u, par); break;
+                    }
+                }
+            }
+            if (!grid_barrier(B.bar_count, B.bar_gen, B.err, nblocks)) return;
+        }
+    }
+}
+
+}  // namespace
+
+const void* batch_kernel_symbol() { return reinterpret_cast<const void*>(batch_steps_kernel); }
+
+int batch_max_blocks_per_sm() {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_steps_kernel, 256, 0);
+    return nb;
 }
 
 }  // namespace adsg

@@ -8,11 +8,15 @@ namespace adsg {
 
 // Per-dimension device tables.  Band rows hold the 2p+1 coefficients of row r
 // for columns r-p .. r+p (zero outside the matrix).
+// Line-solve kernel variants chosen per direction by the context's autotuner.
+enum solve_variant_id { SOLVE_STAGED_1 = 0, SOLVE_STAGED_2 = 1, SOLVE_STAGED_4 = 2, SOLVE_GLOBAL_4 = 3, SOLVE_NVARIANTS = 4 };
+
 struct dim_dev {
     int n = 0, p = 0, kl = 0, w = 0;  // w = kl + ku: widest upper extent of U
     int ku_regular = 0;               // U extent of all columns but a few (row-exchange fill)
     int fwd_fast = 0;                 // no row exchange in columns >= fwd_fast
     int bwd_fast = 0;                 // U extent <= ku_regular in columns >= bwd_fast
+    int solve_variant = SOLVE_STAGED_1;
     int elements = 0, q = 0;
     const double* mrow = nullptr;   // [n][2p+1] 1D mass matrix
     const double* krow = nullptr;   // [n][2p+1] 1D stiffness matrix
@@ -40,6 +44,28 @@ struct line_layout {
 
 line_layout make_line_layout(const int* n, int ndim, int d);
 
+// One instance of the batched engine (cubic: the same dimension in every direction).
+struct batch_inst {
+    int ndim = 0, p = 0, n = 0;
+    long long size = 0;
+    long long units[6] = {};  // outputs (passes) or lines (solves) per stage; 0 = no work
+    double* buf[2] = {nullptr, nullptr};
+    double* T[4] = {nullptr, nullptr, nullptr, nullptr};
+    dim_dev dim;
+};
+
+struct batch_dev {
+    int count = 0;
+    const batch_inst* inst = nullptr;  // device array [count]
+    const int* prefix = nullptr;       // device array [6][count+1]: items (256 units) before instance i
+    unsigned* bar_count = nullptr;
+    unsigned* bar_gen = nullptr;
+    int* err = nullptr;
+};
+
+const void* batch_kernel_symbol();
+int batch_max_blocks_per_sm();
+
 // rhs passes -------------------------------------------------------------
 // out0 = A0 (.) in0 [+ A1 (.) in1],  out1 = B0 (.) in0  along one axis, where
 // (.) applies a band with rows of 2p+1 coefficients.
@@ -55,6 +81,7 @@ cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* k
 cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans,
                               cudaStream_t s);
 size_t line_solve_smem_per_warp(int n);
+bool line_solve_variant_ok(int variant, const dim_dev& d);
 
 // element-wise sum-factorised quadrature (optional kappa field) -----------
 cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev, const double* kappa,

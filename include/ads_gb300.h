@@ -146,6 +146,13 @@ int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps);
 int adsg_ctx_enable_stage_timers(adsg_ctx* ctx, int enable);
 int adsg_ctx_stage_times(adsg_ctx* ctx, double* ms, long long* launches);
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
+/* Line-solve kernel chosen per direction when the context was created (the
+ * autotuner times each applicable variant on the context's own buffers):
+ * 0 one 32-line tile per block staged in shared memory, 1 and 2 the same with
+ * two / four tiles per block, 3 lines swept in place in global memory, four
+ * warps per block.  variants has 3 entries (-1 for absent dimensions).  The
+ * environment variable ADSG_SOLVE_VARIANT forces a variant where it applies. */
+int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants);
 
 /* ---- host-buffer entry points (the reference-facing boundary) ------------- */
 
@@ -168,6 +175,33 @@ int adsg_heat_rhs_host(adsg_ctx* ctx, const double* u_prev_host, double* rhs_hos
 int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs,
                  const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
                  int* info);
+
+/* ---- batched simulations ---------------------------------------------------
+ * No single counterpart in the reference, whose unit of work is one
+ * simulation object run by simulation_base::run (simulation_base.cpp:11-20):
+ * here many independent heat problems -- each 2D or 3D, cubic (the same
+ * elements and degree in every direction), 1 <= p <= 4, its own dt, open
+ * uniform knots on [0,1] -- advance together.  adsg_batch_steps runs nsteps
+ * of every instance as ONE persistent cooperative launch (all RHS passes and
+ * line solves of all instances, grid barriers with bounded waits between
+ * stages), replayed from a CUDA graph; the grid size is chosen at creation by
+ * timing every feasible blocks-per-SM count on the batch.  States start at
+ * zero.  adsg_batch_steps_looped advances the same states with the plain
+ * per-instance entry points (adsg_heat_rhs + adsg_ads_solve per instance and
+ * step), the reference point for the batched launch. */
+typedef struct adsg_batch adsg_batch;
+int adsg_batch_create(int count, const int* ndim, const int* p, const int* elements, const double* dt,
+                      adsg_batch** out);
+int adsg_batch_destroy(adsg_batch* b);
+long long adsg_batch_dofs(const adsg_batch* b, int i);
+int adsg_batch_set_state(adsg_batch* b, int i, const double* u_host);  /* synchronises */
+int adsg_batch_get_state(adsg_batch* b, int i, double* u_host);        /* synchronises */
+int adsg_batch_steps(adsg_batch* b, int nsteps);
+int adsg_batch_steps_looped(adsg_batch* b, int nsteps);
+/* Waits for the batch's work; ADSG_ERR_DEVICE if a grid barrier timed out. */
+int adsg_batch_synchronize(adsg_batch* b);
+/* Autotuned blocks per SM and whether the launch is replayed from a graph. */
+int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captured);
 
 /* ---- the heat RHS without any allocation --------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

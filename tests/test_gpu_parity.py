@@ -277,3 +277,32 @@ def test_full_size_against_oracle_one_step_sampled(big):
     got = u0.copy()
     ctx.heat_steps_host(got, 1e-6, 1)
     assert oracle.rel_l2(got, ref) <= step_tol(_conds(dims))
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("p,elements", [
+    ((2, 2, 2), (30, 7, 9)),
+    ((4, 4, 4), (12, 9, 6)),
+    ((3, 3), (50, 33)),
+    ((1, 2, 4), (5, 6, 7)),
+    ((2,), (200,)),
+])
+def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypatch):
+    """The autotuner's candidates (staged 1/2/4 tiles per block, in-place
+    global sweep) each match the oracle's dgbtrs-based ADS solve."""
+    monkeypatch.setenv("ADSG_SOLVE_VARIANT", str(variant))
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    pr = oracle.Problem(list(p), list(elements))
+    rng = np.random.default_rng(variant + 17 * len(p))
+    u = rng.uniform(-1, 1, pr.size)
+    x = u.copy()
+    ctx.ads_solve_host(x)
+    assert oracle.rel_l2(x, pr.ads_solve(u)) <= step_tol(_conds(dims)) / 10
+    s = u.copy()
+    ctx.heat_steps_host(s, 1e-5, 2)
+    assert oracle.rel_l2(s, pr.heat_steps(u, 1e-5, 2)) <= step_tol(_conds(dims)) * 2
+    chosen = ctx.solve_variants()
+    assert all(0 <= v <= 3 for v in chosen)
+    if variant in (0, 3):  # always applicable for p <= 4
+        assert chosen == [variant] * len(p)
