@@ -39,6 +39,7 @@ WORKLOADS = {
     "heat3d_p2_128": (3, 2, 128, 1e-6),
     "heat2d_p2_32": (2, 2, 32, 1e-5),
     "heat3d_p4_256": (3, 4, 256, 1e-6),
+    "batch64": None,  # 32 2D + 32 3D instances, seeded sizes and degrees (ads_gb300.batch_specs)
 }
 METRIC = "DOF-updates/s per explicit step (RHS+ADS solve, FP64, <=1e-12 rel L2)"
 
@@ -62,6 +63,15 @@ def dist_env():
 
 
 def workload_config(name):
+    if name == "batch64":
+        import ads_gb300 as ads
+
+        specs = ads.batch_specs(seed=0)
+        dofs = sum((e + p) ** nd for nd, p, e, _ in specs)
+        return {"workload": "64 independent heat simulations (32 2D with 32-512 elements per side, 32 3D with "
+                            "16-96, p in {2,3,4} drawn from seed 0), dt=1e-6, one persistent launch per call",
+                "instances": len(specs), "dofs": dofs, "dt": 1e-6,
+                "specs": [list(x[:3]) for x in specs]}
     nd, p, E, dt = WORKLOADS[name]
     n = E + p
     return {"workload": f"{nd}D heat, p={p}, {E}^{nd} elements ({n}^{nd} = {n ** nd} dofs), "
@@ -372,9 +382,73 @@ def run_ours(args, cfg):
     return 0
 
 
+def run_batch(args, cfg):
+    """Batched form: all 64 instances advance `steps` steps in one persistent
+    launch (graph-replayed), timed against looping the plain kernels per
+    instance over the same states."""
+    import numpy as np
+    import torch
+
+    import ads_gb300 as ads
+    from ads_gb300 import inputs
+
+    torch.cuda.set_device(0)
+    specs = ads.batch_specs(seed=0)
+    b = ads.Batch(specs)
+    for i, (nd, p, e, _) in enumerate(specs):
+        dims = [ads.Dimension(p, e) for _ in range(nd)]
+        b.set_state(i, inputs.initial_field(dims, seed=1000 + i))
+    dofs = sum(b.sizes)
+    k = max(1, args.steps)
+    b.steps(max(args.warmup, 3))
+    b.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the batch runs on its own (blocking) stream, ordered with the default stream's events
+    torch.cuda.synchronize()
+    e0.record()
+    b.steps(k)
+    e1.record()
+    b.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    kl = max(1, min(k, 20))
+    b.steps_looped(1)  # creates the per-instance contexts (autotuned) outside the timing
+    b.synchronize()
+    torch.cuda.synchronize()
+    e0.record()
+    b.steps_looped(kl)
+    e1.record()
+    b.synchronize()
+    torch.cuda.synchronize()
+    ms_loop = e0.elapsed_time(e1)
+    value = dofs * k / (ms * 1e-3)
+    loop_value = dofs * kl / (ms_loop * 1e-3)
+    line = {"metric": METRIC + " [batched form]", "value": value, "unit": "DOF-updates/s", "n_gpus": 1,
+            "steps": k, "warmup": max(args.warmup, 3), "ms_per_step": ms / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: per-instance sin projection + seeded noise",
+            "config": {**{kk: v for kk, v in cfg.items() if kk != "specs"}, "tuning": b.tuning(),
+                       "l2": "working set larger than L2 (all instances' state and scratch)"},
+            "looped_plain_kernels": {"value": loop_value, "ms_per_step": ms_loop / kl, "steps": kl},
+            "speedup_vs_loop": value / loop_value, "gpu_launches": 1, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
 def main():
     args = parse()
     cfg = workload_config(args.workload)
+    if args.workload == "batch64":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched form; its CPU "
+                              "step is benchmarked on the single-grid workloads"}))
+            return 0
+        return run_batch(args, cfg)
     if args.impl == "reference":
         return run_reference(args, cfg)
     return run_ours(args, cfg)

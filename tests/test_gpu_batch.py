@@ -1,0 +1,82 @@
+"""The batched engine (one persistent cooperative launch for many uneven
+instances) against the CPU oracle and against the plain per-instance path."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import ads_gb300 as ads
+import oracle
+from _tol import mass_condition, step_tol
+
+pytestmark = pytest.mark.gpu
+
+SMALL = [(2, 2, 17, 1e-5), (3, 4, 7, 1e-6), (2, 4, 40, 2e-6), (3, 2, 12, 1e-6), (3, 3, 9, 1e-6), (2, 3, 5, 1e-4),
+         (3, 1, 6, 1e-5), (2, 1, 33, 1e-5)]
+
+
+def _cond(p, e):
+    return mass_condition(ads.Dimension(p, e).form_band(0).ravel(), p)
+
+
+def test_batch_against_oracle_and_loop(cuda):
+    b = ads.Batch(SMALL)
+    rng = np.random.default_rng(7)
+    u0 = [rng.uniform(-1, 1, n) for n in b.sizes]
+    for i, u in enumerate(u0):
+        b.set_state(i, u)
+    b.steps(3)
+    b.synchronize()
+    got = [b.get_state(i) for i in range(len(SMALL))]
+    for i, (nd, p, e, dt) in enumerate(SMALL):
+        ref = oracle.Problem([p] * nd, [e] * nd).heat_steps(u0[i], dt, 3)
+        assert oracle.rel_l2(got[i], ref) <= 3 * step_tol([_cond(p, e)] * nd), (i, SMALL[i])
+    # the same three steps through the plain per-instance kernels
+    for i, u in enumerate(u0):
+        b.set_state(i, u)
+    b.steps_looped(3)
+    b.synchronize()
+    for i in range(len(SMALL)):
+        assert oracle.rel_l2(b.get_state(i), got[i]) <= 1e-14
+
+
+def test_batch_repeated_calls_and_parity(cuda):
+    b = ads.Batch(SMALL[:4])
+    rng = np.random.default_rng(8)
+    u0 = [rng.uniform(-1, 1, n) for n in b.sizes]
+    for i, u in enumerate(u0):
+        b.set_state(i, u)
+    for n in (1, 2, 1, 3):  # odd counts flip the state buffer, graphs are re-captured
+        b.steps(n)
+    b.synchronize()
+    for i, (nd, p, e, dt) in enumerate(SMALL[:4]):
+        ref = oracle.Problem([p] * nd, [e] * nd).heat_steps(u0[i], dt, 7)
+        assert oracle.rel_l2(b.get_state(i), ref) <= 7 * step_tol([_cond(p, e)] * nd)
+    t = b.tuning()
+    assert t["blocks_per_sm"] >= 1
+
+
+def test_mixed_64_batch_matches_plain_kernels(cuda):
+    specs = ads.batch_specs(seed=0)
+    assert len(specs) == 64 and sum(s[0] == 2 for s in specs) == 32
+    b = ads.Batch(specs)
+    rng = np.random.default_rng(9)
+    u0 = [rng.uniform(-1e-2, 1e-2, n) for n in b.sizes]
+    for i, u in enumerate(u0):
+        b.set_state(i, u)
+    b.steps(2)
+    b.synchronize()
+    got = [b.get_state(i) for i in range(64)]
+    for i, u in enumerate(u0):
+        b.set_state(i, u)
+    b.steps_looped(2)
+    b.synchronize()
+    for i in range(64):
+        assert oracle.rel_l2(b.get_state(i), got[i]) <= 1e-13, specs[i]
+
+
+def test_batch_rejects_bad_specs():
+    with pytest.raises(ads.AdsError):
+        ads.Batch([(4, 2, 8, 1e-6)])
+    with pytest.raises(ads.AdsError):
+        ads.Batch([(3, 5, 8, 1e-6)])
