@@ -40,6 +40,7 @@ WORKLOADS = {
     "heat2d_p2_32": (2, 2, 32, 1e-5),
     "heat3d_p4_256": (3, 4, 256, 1e-6),
     "batch64": None,  # 32 2D + 32 3D instances, seeded sizes and degrees (ads_gb300.batch_specs)
+    "adjoint_p2_96": (3, 2, 96, 1e-6),  # kappa field, 200 steps, sqrt(N) checkpoints
 }
 METRIC = "DOF-updates/s per explicit step (RHS+ADS solve, FP64, <=1e-12 rel L2)"
 
@@ -232,13 +233,15 @@ def measured_peaks():
         return {}
 
 
-def profiled_traffic(stage):
-    """DRAM bytes per launch of a stage from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "traffic.md")
+def profiled_traffic(stage, dofs):
+    """DRAM bytes per launch of a stage: the bytes per dof measured by ncu
+    (dram__bytes_read.sum + dram__bytes_write.sum, committed in
+    profiles/traffic_per_dof.md) times this workload's dofs, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_dof.md")
     try:
         for ln in open(path):
             if ln.startswith(f"| {stage} |"):
-                return float(ln.split("|")[3].strip())
+                return float(ln.split("|")[3].strip()) * dofs
     except (OSError, ValueError, IndexError):
         pass
     return None
@@ -305,13 +308,27 @@ def run_ours(args, cfg):
         torch.distributed.barrier()
     clocks = sampler.stop()
     stage = ctx.stage_times()
-    ctx.enable_stage_timers(False)
     step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     if world > 1:
         t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         step_ms = float(t.item())
     value = world * size * args.steps / (step_ms * 1e-3)
+
+    # --- element-wise sum-factorised quadrature (the general RHS path), timed alone ---
+    elem = None
+    if nd >= 2:
+        ctx.stage_times()
+        for _ in range(3):
+            ctx.heat_rhs_elem(bufs[0], bufs[1], dt)
+        ctx.stage_times()
+        for _ in range(5):
+            ctx.heat_rhs_elem(bufs[0], bufs[1], dt)
+        t = ctx.stage_times()["rhs_elem"]
+        fl = ctx.stage_work()["rhs_elem"][0]
+        elem = {"avg_us": 1e3 * t[0] / t[1], "tflops": fl / (t[0] / t[1] * 1e-3) / 1e12,
+                "gflop_per_launch": fl / 1e9, "note": "(p+1)^d colour launches per evaluation"}
+    ctx.enable_stage_timers(False)
 
     # --- e2e: the reference-facing host entry point with pinned host buffers ---
     ctx.set_stream(None)
@@ -348,7 +365,7 @@ def run_ours(args, cfg):
     peaks = measured_peaks()
     roof = {"bound": "fp64", "kernel": dom, "achieved": d["tflops"], "peak": peak_fp64, "unit": "TFLOP/s",
             "frac": d["tflops"] / peak_fp64,
-            "traffic": profiled_traffic(dom),
+            "traffic": profiled_traffic(dom, size),
             "peak_source": "cuBLAS DGEMM 4096^3 measured live in bench.py (GB300 FP64 is not in "
                            "MEASURED_PEAKS.json)",
             "algorithmic_bytes_per_launch": work[dom][1], "hbm_gbs": d["gbs"],
@@ -368,6 +385,7 @@ def run_ours(args, cfg):
         "gpu_launches": sum(v["launches"] for v in per_stage.values()),
         "roofline": roof,
         "stages": per_stage,
+        "element_rhs": elem,
         "step_tflops": step_flops / (step_ms / args.steps * 1e-3) / 1e12,
         "clocks": clocks,
         "wall_s": wall,
@@ -440,9 +458,96 @@ def run_batch(args, cfg):
     return 0
 
 
+def run_adjoint(args, cfg):
+    """Reverse mode: forward 200 steps of the kappa-weighted step with sqrt(N)
+    checkpoints, mass-norm loss against a second seeded field, gradients with
+    respect to u0 and kappa; checked by central differences along 16 seeded
+    directions (8 in u0, 8 in kappa) and the dot-product identity."""
+    import numpy as np
+    import torch
+
+    import ads_gb300 as ads
+    from ads_gb300 import inputs
+
+    torch.cuda.set_device(0)
+    nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
+    nsteps = 200
+    dims = [ads.Dimension(p, E) for _ in range(nd)]
+    ctx = ads.Context(dims)
+    adj = ads.Adjoint(ctx, nsteps, dt)
+    dev = lambda a: torch.from_numpy(a).cuda()
+    u0 = dev(inputs.initial_field(dims, seed=11))
+    kappa = dev(inputs.kappa_field(dims, seed=12))
+    target = dev(inputs.initial_field(dims, seed=13))
+    uT, scratch, dL, gu, gk = (torch.empty_like(u0) for _ in range(5))
+
+    def forward(u, k):
+        adj.forward(u, k, uT)
+        return ads.mass_loss(ctx, uT, target, scratch, dL)
+
+    forward(u0, kappa)  # warm-up (also compiles nothing: all kernels are prebuilt)
+    adj.backward(dL, gu, gk)
+    ctx.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    torch.cuda.synchronize()
+    e[0].record()
+    adj.forward(u0, kappa, uT)
+    e[1].record()
+    torch.cuda.synchronize()
+    loss = ads.mass_loss(ctx, uT, target, scratch, dL)
+    torch.cuda.synchronize()
+    e[2].record()
+    adj.backward(dL, gu, gk)
+    e[3].record()
+    torch.cuda.synchronize()
+    t_fwd = e[0].elapsed_time(e[1])
+    t_bwd = e[2].elapsed_time(e[3])
+    # finite differences along seeded directions (central, exact for the u0 part)
+    fd = []
+    rng = np.random.default_rng(2024)
+    for i in range(16):
+        which = "u0" if i < 8 else "kappa"
+        d = dev(rng.standard_normal(ctx.size))
+        h = 1e-4
+        if which == "u0":
+            lp, lm = forward(u0 + h * d, kappa), forward(u0 - h * d, kappa)
+            an = float(gu @ d)
+        else:
+            lp, lm = forward(u0, kappa + h * d), forward(u0, kappa - h * d)
+            an = float(gk @ d)
+        num = (lp - lm) / (2 * h)
+        fd.append(abs(num - an) / max(abs(num), abs(an), 1e-300))
+    # dot-product identity of the linear map u0 -> u(T)
+    x, y = dev(rng.standard_normal(ctx.size)), dev(rng.standard_normal(ctx.size))
+    adj.forward(x, kappa, uT)
+    lhs = float(uT @ y)
+    adj.backward(y, gu, gk)
+    ctx.synchronize()
+    rhs = float(x @ gu)
+    every, count = adj.checkpoints()
+    dofs = ctx.size
+    line = {"metric": METRIC + " [adjoint form]", "value": dofs * nsteps / (t_fwd * 1e-3), "unit": "DOF-updates/s",
+            "n_gpus": 1, "steps": nsteps, "warmup": 1, "ms_per_step": t_fwd / nsteps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: sin projection + seeded noise (u0, target), 8-mode seeded Fourier kappa in [0.5, 1.5]",
+            "config": {**cfg, "nsteps": nsteps, "checkpoint_every": every, "checkpoints": count,
+                       "rhs": "element-wise sum-factorised quadrature with kappa"},
+            "forward_ms": t_fwd, "gradient_ms": t_bwd, "gradient_over_forward": t_bwd / t_fwd,
+            "loss": loss, "fd_max_rel_err": max(fd), "fd_rel_errs": fd,
+            "dot_product_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     cfg = workload_config(args.workload)
+    if args.workload == "adjoint_p2_96":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint; its CPU step is "
+                              "benchmarked on the single-grid workloads"}))
+            return 0
+        return run_adjoint(args, cfg)
     if args.workload == "batch64":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched form; its CPU "

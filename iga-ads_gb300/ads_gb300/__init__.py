@@ -93,6 +93,12 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_stage_times": (i, [vp, _c_double_p, ctypes.POINTER(ctypes.c_longlong)]),
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
+        "adsg_adjoint_create": (i, [vp, i, d, i, ctypes.POINTER(vp)]),
+        "adsg_adjoint_destroy": (i, [vp]),
+        "adsg_adjoint_checkpoints": (i, [vp, _c_int_p, _c_int_p]),
+        "adsg_adjoint_forward": (i, [vp, vp, vp, vp]),
+        "adsg_adjoint_backward": (i, [vp, vp, vp, vp]),
+        "adsg_mass_loss": (i, [vp, vp, vp, vp, _c_double_p, vp]),
         "adsg_batch_create": (i, [i, _c_int_p, _c_int_p, _c_int_p, _c_double_p, ctypes.POINTER(vp)]),
         "adsg_batch_destroy": (i, [vp]),
         "adsg_batch_dofs": (ll, [vp, i]),
@@ -323,6 +329,48 @@ class Heat:
         self.ctx.heat_steps_host(u, self.dt, steps)
 
 
+class Adjoint:
+    """Reverse-mode gradients of the kappa-weighted explicit heat run
+    (adsg_adjoint_*): forward(u0, kappa) -> u(T) keeps sqrt(N) checkpoints;
+    backward(dL/du(T)) -> (dL/du0, dL/dkappa).  Device tensors (torch)."""
+
+    def __init__(self, ctx: Context, nsteps: int, dt: float, checkpoint_every: int = 0):
+        h = ctypes.c_void_p()
+        _check(library().adsg_adjoint_create(ctx.handle, int(nsteps), float(dt), int(checkpoint_every), ctypes.byref(h)))
+        self._h = h
+        self.ctx = ctx
+        self.nsteps = nsteps
+        self.dt = dt
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.adsg_adjoint_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def checkpoints(self) -> tuple:
+        e, c = ctypes.c_int(), ctypes.c_int()
+        _check(library().adsg_adjoint_checkpoints(self._h, ctypes.byref(e), ctypes.byref(c)))
+        return e.value, c.value
+
+    def forward(self, u0, kappa, uT) -> None:
+        _check(library().adsg_adjoint_forward(self._h, _devptr(u0), _devptr(kappa), _devptr(uT)))
+
+    def backward(self, dL_duT, grad_u0, grad_kappa) -> None:
+        _check(library().adsg_adjoint_backward(self._h, _devptr(dL_duT), _devptr(grad_u0), _devptr(grad_kappa)))
+
+
+def mass_loss(ctx: Context, u, target, scratch, grad) -> float:
+    """(u - target)^T M (u - target) and grad = 2 M (u - target) (adsg_mass_loss)."""
+    out = ctypes.c_double()
+    _check(library().adsg_mass_loss(ctx.handle, _devptr(u), _devptr(target), _devptr(scratch), ctypes.byref(out),
+                                    _devptr(grad)))
+    return out.value
+
+
 class Batch:
     """Many independent cubic heat problems advanced by one persistent launch
     per call (adsg_batch_*).  specs: iterable of (ndim, p, elements, dt)."""
@@ -410,4 +458,4 @@ def dgbtrs(trans: str, n: int, kl: int, ku: int, nrhs: int, ab: np.ndarray, ldab
     return info.value
 
 
-__all__ = ["AdsError", "Batch", "batch_specs", "Context", "DimDesc", "Dimension", "Heat", "ads_solve", "dgbtrs", "library", "LIB_PATH"]
+__all__ = ["AdsError", "Adjoint", "mass_loss", "Batch", "batch_specs", "Context", "DimDesc", "Dimension", "Heat", "ads_solve", "dgbtrs", "library", "LIB_PATH"]

@@ -70,3 +70,24 @@ def initial_field(dims, seed: int = 0, amp: float = 1e-2) -> np.ndarray:
     u = np.ascontiguousarray(u.ravel())
     u += (2.0 * splitmix_uniform(seed, u.size) - 1.0) * amp
     return u
+
+
+def kappa_field(dims, seed: int = 0, modes: int = 8, amp: float = 0.5) -> np.ndarray:
+    """Diffusion-field coefficients 1 + amp * f with f a sum of `modes` seeded
+    Fourier modes normalised to max |f| = 1, sampled at the coefficients'
+    parametric positions i/(n-1) (x-fastest, like the state)."""
+    r = splitmix_uniform(seed, modes * (len(dims) + 2))
+    axes = [np.linspace(0.0, 1.0, d.dofs()) for d in dims]
+    grids = np.meshgrid(*axes[::-1], indexing="ij")[::-1]  # x varies fastest in the flattened array
+    f = np.zeros(grids[0].shape)
+    for m in range(modes):
+        base = m * (len(dims) + 2)
+        phase = 2 * np.pi * r[base]
+        weight = 2 * r[base + 1] - 1
+        arg = phase
+        for d, g in enumerate(grids):
+            k = 1 + int(r[base + 2 + d] * 4)  # wave numbers 1..4
+            arg = arg + 2 * np.pi * k * g
+        f += weight * np.cos(arg)
+    f /= max(np.abs(f).max(), 1e-300)
+    return np.ascontiguousarray((1.0 + amp * f).ravel())

@@ -75,7 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             list(ex.map(_compile, jobs))
     if force or jobs or _stale(LIB, objs):
-        _compile([nv, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs])
+        _compile([nv, *ARCH, "-shared", "-cudart", "static", "-Xlinker", "-soname=libads_gb300.so", "-o", LIB, *objs])
     if verbose:
         print("built", LIB)
     return LIB

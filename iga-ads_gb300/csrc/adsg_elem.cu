@@ -50,7 +50,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     const int iy = static_cast<int>((wid / mz) % my);
     const int ix = static_cast<int>(wid / (static_cast<long long>(mz) * my));
     const int e[3] = {cx + ix * N, cy + iy * N, cz + iz * N};
-    const dim_dev* D[3] = {&X, &Y, &Z};
     const int f0 = X.first[e[0]], f1 = Y.first[e[1]], f2 = Z.first[e[2]];
     const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
 
@@ -61,11 +60,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.c[t] = u[g];
         S.kc[t] = kappa ? kappa[g] : 0.0;
     }
-    for (int t = lane; t < 3 * Q * N; t += 32) {
-        const int d = t / (Q * N), r = t % (Q * N), q = r / N, a = r % N;
-        const double* bt = D[d]->btab + ((static_cast<long long>(e[d]) * Q + q) * 2) * N;
-        S.B[d][r] = bt[a];
-        S.dB[d][r] = bt[N + a];
+    for (int t = lane; t < Q * N; t += 32) {
+        const int q = t / N, a = t % N;
+        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
+        const double* bz = Z.btab + ((static_cast<long long>(e[2]) * Q + q) * 2) * N;
+        S.B[0][t] = bx[a];
+        S.dB[0][t] = bx[N + a];
+        S.B[1][t] = by[a];
+        S.dB[1][t] = by[N + a];
+        S.B[2][t] = bz[a];
+        S.dB[2][t] = bz[N + a];
     }
     __syncwarp();
     // x: T0/T1[bz][by][qx]
@@ -197,7 +202,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     const int iy = static_cast<int>(wid % my);
     const int ix = static_cast<int>(wid / my);
     const int e[2] = {cx + ix * N, cy + iy * N};
-    const dim_dev* D[2] = {&X, &Y};
     const int f0 = X.first[e[0]], f1 = Y.first[e[1]];
     const long long nx = X.n;
     for (int t = lane; t < N * N; t += 32) {
@@ -205,11 +209,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.c[t] = u[g];
         S.kc[t] = kappa ? kappa[g] : 0.0;
     }
-    for (int t = lane; t < 2 * Q * N; t += 32) {
-        const int d = t / (Q * N), r = t % (Q * N), q = r / N, a = r % N;
-        const double* bt = D[d]->btab + ((static_cast<long long>(e[d]) * Q + q) * 2) * N;
-        S.B[d][r] = bt[a];
-        S.dB[d][r] = bt[N + a];
+    for (int t = lane; t < Q * N; t += 32) {
+        const int q = t / N, a = t % N;
+        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
+        S.B[0][t] = bx[a];
+        S.dB[0][t] = bx[N + a];
+        S.B[1][t] = by[a];
+        S.dB[1][t] = by[N + a];
     }
     __syncwarp();
     for (int t = lane; t < N * Q; t += 32) {
@@ -272,6 +279,230 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Gradient of a quadratic functional with respect to the diffusion field:
+//     g_c += -dt sum_e sum_q W B_c(x_q) grad u(x_q) . grad mu(x_q)
+// i.e. mu^T (dR/dkappa_c) u for the operator R(kappa) applied by the element
+// kernel above.  Same warp-per-element sum factorisation and colouring:
+// gradients of u and mu are interpolated direction by direction, the
+// pointwise product is formed and projected onto the value factors.
+// ---------------------------------------------------------------------------
+template <int N, int Q>
+struct kg3_smem {
+    double c[N * N * N], m[N * N * N];
+    double B[3][Q * N], dB[3][Q * N];
+    double Tu0[N * N * Q], Tu1[N * N * Q], Tm0[N * N * Q], Tm1[N * N * Q];  // [bz][by][qx]
+    double Vu00[N * Q * Q], Vu01[N * Q * Q], Vu10[N * Q * Q];              // [bz][qy][qx]
+    double Vm00[N * Q * Q], Vm01[N * Q * Q], Vm10[N * Q * Q];
+    double s[Q * Q * Q];
+};
+
+template <int P, int Q, int kWarpsPerBlock = warps_for<kg3_smem<P + 1, Q>>()>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    kgrad3_kernel(const double* __restrict__ u, const double* __restrict__ mu, double* __restrict__ g, dim_dev X,
+                  dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt) {
+    constexpr int N = P + 1;
+    __shared__ kg3_smem<N, Q> sm_all[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
+    if (wid >= static_cast<long long>(mx) * my * mz) return;
+    kg3_smem<N, Q>& S = sm_all[warp];
+    const int iz = static_cast<int>(wid % mz);
+    const int iy = static_cast<int>((wid / mz) % my);
+    const int ix = static_cast<int>(wid / (static_cast<long long>(mz) * my));
+    const int e[3] = {cx + ix * N, cy + iy * N, cz + iz * N};
+    const int f0 = X.first[e[0]], f1 = Y.first[e[1]], f2 = Z.first[e[2]];
+    const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
+    for (int t = lane; t < N * N * N; t += 32) {
+        const long long gi = (f0 + t % N) + nx * (f1 + (t / N) % N) + nxy * (f2 + t / (N * N));
+        S.c[t] = u[gi];
+        S.m[t] = mu[gi];
+    }
+    for (int t = lane; t < Q * N; t += 32) {
+        const int q = t / N, a = t % N;
+        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
+        const double* bz = Z.btab + ((static_cast<long long>(e[2]) * Q + q) * 2) * N;
+        S.B[0][t] = bx[a];
+        S.dB[0][t] = bx[N + a];
+        S.B[1][t] = by[a];
+        S.dB[1][t] = by[N + a];
+        S.B[2][t] = bz[a];
+        S.dB[2][t] = bz[N + a];
+    }
+    __syncwarp();
+    for (int t = lane; t < N * N * Q; t += 32) {
+        const int qx = t % Q, byz = t / Q;
+        double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const double bv = S.B[0][qx * N + b], dv = S.dB[0][qx * N + b];
+            a0 = fma(bv, S.c[byz * N + b], a0);
+            a1 = fma(dv, S.c[byz * N + b], a1);
+            b0 = fma(bv, S.m[byz * N + b], b0);
+            b1 = fma(dv, S.m[byz * N + b], b1);
+        }
+        S.Tu0[t] = a0;
+        S.Tu1[t] = a1;
+        S.Tm0[t] = b0;
+        S.Tm1[t] = b1;
+    }
+    __syncwarp();
+    for (int t = lane; t < N * Q * Q; t += 32) {
+        const int qx = t % Q, qy = (t / Q) % Q, bz = t / (Q * Q);
+        double u00 = 0.0, u01 = 0.0, u10 = 0.0, m00 = 0.0, m01 = 0.0, m10 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const int src = (bz * N + b) * Q + qx;
+            const double by = S.B[1][qy * N + b], dby = S.dB[1][qy * N + b];
+            u00 = fma(by, S.Tu0[src], u00);
+            u01 = fma(dby, S.Tu0[src], u01);
+            u10 = fma(by, S.Tu1[src], u10);
+            m00 = fma(by, S.Tm0[src], m00);
+            m01 = fma(dby, S.Tm0[src], m01);
+            m10 = fma(by, S.Tm1[src], m10);
+        }
+        S.Vu00[t] = u00;
+        S.Vu01[t] = u01;
+        S.Vu10[t] = u10;
+        S.Vm00[t] = m00;
+        S.Vm01[t] = m01;
+        S.Vm10[t] = m10;
+    }
+    __syncwarp();
+    const double J = X.jac[e[0]] * Y.jac[e[1]] * Z.jac[e[2]];
+    for (int t = lane; t < Q * Q * Q; t += 32) {
+        const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
+        double ux = 0.0, uy = 0.0, uz = 0.0, mx_ = 0.0, my_ = 0.0, mz_ = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const int src = (b * Q + qy) * Q + qx;
+            const double bz = S.B[2][qz * N + b], dbz = S.dB[2][qz * N + b];
+            uz = fma(dbz, S.Vu00[src], uz);
+            uy = fma(bz, S.Vu01[src], uy);
+            ux = fma(bz, S.Vu10[src], ux);
+            mz_ = fma(dbz, S.Vm00[src], mz_);
+            my_ = fma(bz, S.Vm01[src], my_);
+            mx_ = fma(bz, S.Vm10[src], mx_);
+        }
+        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * J;
+        S.s[t] = -dt * W * (ux * mx_ + uy * my_ + uz * mz_);
+    }
+    __syncwarp();
+    // project s onto the value factors: z, then y, then x
+    for (int t = lane; t < N * Q * Q; t += 32) {
+        const int qx = t % Q, qy = (t / Q) % Q, az = t / (Q * Q);
+        double a = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a = fma(S.B[2][q * N + az], S.s[(q * Q + qy) * Q + qx], a);
+        S.Vu00[t] = a;
+    }
+    __syncwarp();
+    for (int t = lane; t < N * N * Q; t += 32) {
+        const int qx = t % Q, ay = (t / Q) % N, az = t / (Q * N);
+        double a = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a = fma(S.B[1][q * N + ay], S.Vu00[(az * Q + q) * Q + qx], a);
+        S.Tu0[t] = a;
+    }
+    __syncwarp();
+    for (int t = lane; t < N * N * N; t += 32) {
+        const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
+        double a = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a = fma(S.B[0][q * N + ax], S.Tu0[(az * N + ay) * Q + q], a);
+        g[(f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az)] += a;
+    }
+}
+
+template <int N, int Q>
+struct kg2_smem {
+    double c[N * N], m[N * N];
+    double B[2][Q * N], dB[2][Q * N];
+    double Tu0[N * Q], Tu1[N * Q], Tm0[N * Q], Tm1[N * Q];
+    double s[Q * Q];
+};
+
+template <int P, int Q, int kWarpsPerBlock = warps_for<kg2_smem<P + 1, Q>>()>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    kgrad2_kernel(const double* __restrict__ u, const double* __restrict__ mu, double* __restrict__ g, dim_dev X,
+                  dim_dev Y, int cx, int cy, int mx, int my, double dt) {
+    constexpr int N = P + 1;
+    __shared__ kg2_smem<N, Q> sm_all[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
+    if (wid >= static_cast<long long>(mx) * my) return;
+    kg2_smem<N, Q>& S = sm_all[warp];
+    const int e[2] = {cx + static_cast<int>(wid / my) * N, cy + static_cast<int>(wid % my) * N};
+    const int f0 = X.first[e[0]], f1 = Y.first[e[1]];
+    const long long nx = X.n;
+    for (int t = lane; t < N * N; t += 32) {
+        const long long gi = (f0 + t % N) + nx * (f1 + t / N);
+        S.c[t] = u[gi];
+        S.m[t] = mu[gi];
+    }
+    for (int t = lane; t < Q * N; t += 32) {
+        const int q = t / N, a = t % N;
+        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
+        S.B[0][t] = bx[a];
+        S.dB[0][t] = bx[N + a];
+        S.B[1][t] = by[a];
+        S.dB[1][t] = by[N + a];
+    }
+    __syncwarp();
+    for (int t = lane; t < N * Q; t += 32) {
+        const int qx = t % Q, by = t / Q;
+        double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const double bv = S.B[0][qx * N + b], dv = S.dB[0][qx * N + b];
+            a0 = fma(bv, S.c[by * N + b], a0);
+            a1 = fma(dv, S.c[by * N + b], a1);
+            b0 = fma(bv, S.m[by * N + b], b0);
+            b1 = fma(dv, S.m[by * N + b], b1);
+        }
+        S.Tu0[t] = a0;
+        S.Tu1[t] = a1;
+        S.Tm0[t] = b0;
+        S.Tm1[t] = b1;
+    }
+    __syncwarp();
+    const double J = X.jac[e[0]] * Y.jac[e[1]];
+    for (int t = lane; t < Q * Q; t += 32) {
+        const int qx = t % Q, qy = t / Q;
+        double ux = 0.0, uy = 0.0, mx_ = 0.0, my_ = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const double by = S.B[1][qy * N + b], dby = S.dB[1][qy * N + b];
+            uy = fma(dby, S.Tu0[b * Q + qx], uy);
+            ux = fma(by, S.Tu1[b * Q + qx], ux);
+            my_ = fma(dby, S.Tm0[b * Q + qx], my_);
+            mx_ = fma(by, S.Tm1[b * Q + qx], mx_);
+        }
+        const double W = X.wq[qx] * Y.wq[qy] * J;
+        S.s[t] = -dt * W * (ux * mx_ + uy * my_);
+    }
+    __syncwarp();
+    for (int t = lane; t < N * Q; t += 32) {
+        const int qx = t % Q, ay = t / Q;
+        double a = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a = fma(S.B[1][q * N + ay], S.s[q * Q + qx], a);
+        S.Tu0[t] = a;
+    }
+    __syncwarp();
+    for (int t = lane; t < N * N; t += 32) {
+        const int ax = t % N, ay = t / N;
+        double a = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a = fma(S.B[0][q * N + ax], S.Tu0[ay * Q + q], a);
+        g[(f0 + ax) + nx * (f1 + ay)] += a;
+    }
+}
+
 int colour_count(int E, int c, int N) { return E > c ? (E - c + N - 1) / N : 0; }
 
 template <int P>
@@ -305,7 +536,51 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
     return cudaGetLastError();
 }
 
+template <int P>
+cudaError_t kgrad_p(int ndim, const dim_dev* d, const double* u, const double* mu, double* g, double dt,
+                    cudaStream_t s) {
+    constexpr int N = P + 1, Q = P + 1;
+    constexpr int W3 = warps_for<kg3_smem<N, Q>>();
+    constexpr int W2 = warps_for<kg2_smem<N, Q>>();
+    if (ndim == 3) {
+        for (int cx = 0; cx < N; ++cx)
+            for (int cy = 0; cy < N; ++cy)
+                for (int cz = 0; cz < N; ++cz) {
+                    const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N),
+                              mz = colour_count(d[2].elements, cz, N);
+                    const long long work = static_cast<long long>(mx) * my * mz;
+                    if (!work) continue;
+                    kgrad3_kernel<P, Q><<<(work + W3 - 1) / W3, 32 * W3, 0, s>>>(u, mu, g, d[0], d[1], d[2], cx, cy,
+                                                                              cz, mx, my, mz, dt);
+                }
+    } else {
+        for (int cx = 0; cx < N; ++cx)
+            for (int cy = 0; cy < N; ++cy) {
+                const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N);
+                const long long work = static_cast<long long>(mx) * my;
+                if (!work) continue;
+                kgrad2_kernel<P, Q><<<(work + W2 - 1) / W2, 32 * W2, 0, s>>>(u, mu, g, d[0], d[1], cx, cy, mx, my, dt);
+            }
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,
+                              cudaStream_t s) {
+    if (ndim < 2) return cudaErrorNotSupported;
+    const int p = dims[0].p;
+    for (int d = 0; d < ndim; ++d)
+        if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    switch (p) {
+        case 1: return kgrad_p<1>(ndim, dims, u, mu, g, dt, s);
+        case 2: return kgrad_p<2>(ndim, dims, u, mu, g, dt, s);
+        case 3: return kgrad_p<3>(ndim, dims, u, mu, g, dt, s);
+        case 4: return kgrad_p<4>(ndim, dims, u, mu, g, dt, s);
+        default: return cudaErrorNotSupported;
+    }
+}
 
 cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev, const double* kappa, double* rhs,
                             double dt, cudaStream_t s) {

@@ -676,6 +676,109 @@ cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout&
 }
 
 // ---------------------------------------------------------------------------
+// Generalised ADS (reference include/ads/solver.hpp:47-195): along one
+// "special" direction every grid line has its own factorised band.  Each lane
+// sweeps one line in global memory with that line's tables, in LAPACK's
+// column order (forward with row exchanges, backward over the full kl+ku U
+// band, reciprocal diagonal).  Line l is numbered as the reference numbers
+// the lines handed to its special-dimension callable: over the directions
+// that follow the special one cyclically, the first of them fastest.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) line_solve_permat_kernel(double* __restrict__ data, line_tables T,
+                                                                line_layout L, const int* __restrict__ line_matrix,
+                                                                int nx, int nz, int special, int ndim) {
+    const long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= L.nlines) return;
+    // reference line number of my line
+    long long ref = g;
+    if (ndim == 3 && special == 1) ref = (g / nx) + static_cast<long long>(nz) * (g % nx);
+    const long long m = line_matrix[ref];
+    const int n = T.n, kl = T.kl, w = T.w;
+    const double* lmul = T.lmul + m * static_cast<long long>(n) * kl;
+    const double* ucol = T.ucol + m * static_cast<long long>(n) * w;
+    const double* rdiag = T.rdiag + m * static_cast<long long>(n);
+    const int* piv = T.piv + m * static_cast<long long>(n);
+    const int* uext = T.uext + m * static_cast<long long>(n);
+    double* x = data + (L.contiguous ? g * n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    const long long es = L.elem_stride;
+    for (int j = 0; j < n - 1; ++j) {
+        const int l = __ldg(piv + j);
+        if (l != j) {
+            const double t = x[l * es];
+            x[l * es] = x[j * es];
+            x[j * es] = t;
+        }
+        const double y = -x[j * es];
+        const int lm = min(kl, n - 1 - j);
+        for (int i = 1; i <= lm; ++i) x[(j + i) * es] = fma(y, __ldg(lmul + static_cast<long long>(j) * kl + i - 1), x[(j + i) * es]);
+    }
+    for (int j = n - 1; j >= 0; --j) {
+        const double v = x[j * es] * __ldg(rdiag + j);
+        x[j * es] = v;
+        const int ext = __ldg(uext + j);
+        for (int d = 1; d <= ext; ++d) x[(j - d) * es] = fma(-v, __ldg(ucol + static_cast<long long>(j) * w + d - 1), x[(j - d) * es]);
+    }
+}
+
+cudaError_t launch_line_solve_permat(double* data, const line_tables& T, const line_layout& L, const int* line_matrix,
+                                     int nx, int nz, int special, int ndim, cudaStream_t s) {
+    if (L.nlines <= 0) return cudaSuccess;
+    line_solve_permat_kernel<<<(L.nlines + 127) / 128, 128, 0, s>>>(data, T, L, line_matrix, nx, nz, special, ndim);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Vector helpers of the adjoint driver.  The dot product is deterministic: a
+// fixed grid writes block partial sums in a fixed order, one block adds them.
+// ---------------------------------------------------------------------------
+__global__ void axpby_kernel(double* __restrict__ y, double a, const double* __restrict__ x, double b, long long n) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        y[i] = fma(a, x[i], b * y[i]);
+}
+
+cudaError_t launch_axpby(double* y, double a, const double* x, double b, long long n, cudaStream_t s) {
+    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 16);
+    axpby_kernel<<<static_cast<int>(std::max<long long>(blocks, 1)), 256, 0, s>>>(y, a, x, b, n);
+    return cudaGetLastError();
+}
+
+constexpr int kDotBlocks = 1024;
+
+__global__ void dot_partial_kernel(const double* __restrict__ x, const double* __restrict__ y, long long n,
+                                   double* __restrict__ partial) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += 256LL * gridDim.x) acc = fma(x[i], y[i], acc);
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void dot_final_kernel(const double* __restrict__ partial, int m, double* __restrict__ out) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < m; i += 256) acc += partial[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+cudaError_t launch_dot(const double* x, const double* y, long long n, double* partial, double* out, cudaStream_t s) {
+    dot_partial_kernel<<<kDotBlocks, 256, 0, s>>>(x, y, n, partial);
+    dot_final_kernel<<<1, 256, 0, s>>>(partial, kDotBlocks, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Batched engine: many independent cubic heat problems (2D or 3D, p <= 4)
 // advanced by one persistent cooperative launch.  A step is six stages (RHS
 // passes outer / middle / x, then the x, y, z line solves); every stage's work

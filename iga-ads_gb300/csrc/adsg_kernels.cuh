@@ -44,6 +44,19 @@ struct line_layout {
 
 line_layout make_line_layout(const int* n, int ndim, int d);
 
+// Stacked solve tables of several factorised bands of one size (generalised ADS).
+struct line_tables {
+    int n = 0, kl = 0, w = 0, nmat = 0;
+    const double* lmul = nullptr;   // [nmat][n][kl]
+    const double* ucol = nullptr;   // [nmat][n][w]
+    const double* rdiag = nullptr;  // [nmat][n]
+    const int* piv = nullptr;       // [nmat][n]
+    const int* uext = nullptr;      // [nmat][n]
+};
+
+cudaError_t launch_line_solve_permat(double* data, const line_tables& T, const line_layout& L, const int* line_matrix,
+                                     int nx, int nz, int special, int ndim, cudaStream_t s);
+
 // One instance of the batched engine (cubic: the same dimension in every direction).
 struct batch_inst {
     int ndim = 0, p = 0, n = 0;
@@ -84,6 +97,14 @@ size_t line_solve_smem_per_warp(int n);
 bool line_solve_variant_ok(int variant, const dim_dev& d);
 
 // element-wise sum-factorised quadrature (optional kappa field) -----------
+// g += mu^T (dR/dkappa) u  (gradient of the element operator w.r.t. kappa coefficients)
+cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,
+                              cudaStream_t s);
+
+// small vector kernels of the adjoint driver
+cudaError_t launch_axpby(double* y, double a, const double* x, double b, long long n, cudaStream_t s);  // y = a*x + b*y
+cudaError_t launch_dot(const double* x, const double* y, long long n, double* partial, double* out, cudaStream_t s);
+
 cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev, const double* kappa,
                             double* rhs, double dt, cudaStream_t s);
 

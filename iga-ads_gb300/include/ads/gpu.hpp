@@ -38,39 +38,50 @@ inline void check(int code) {
 struct flat_dim {
     std::vector<double> btab, w, J, lu;
     std::vector<int> first, ipiv;
-    adsg_dim_desc desc{};
+    int p = 0, elements = 0, quad_order = 0, n = 0, kl = 0, ku = 0, ldab = 0;
 
     template <typename Dimension>
     explicit flat_dim(const Dimension& d) {
         const auto& B = d.basis;
-        const int E = B.elements, Q = B.quad_order, P = B.degree;
-        btab.resize(static_cast<size_t>(E) * Q * 2 * (P + 1));
-        for (int e = 0; e < E; ++e)
-            for (int q = 0; q < Q; ++q)
+        elements = B.elements;
+        quad_order = B.quad_order;
+        p = B.degree;
+        n = B.dofs;
+        btab.resize(static_cast<size_t>(elements) * quad_order * 2 * (p + 1));
+        for (int e = 0; e < elements; ++e)
+            for (int q = 0; q < quad_order; ++q)
                 for (int k = 0; k < 2; ++k)
-                    for (int a = 0; a <= P; ++a)
-                        btab[((static_cast<size_t>(e) * Q + q) * 2 + k) * (P + 1) + a] = B.b[e][q][k][a];
-        w.assign(B.w, B.w + Q);
-        J.assign(B.J, B.J + E);
-        first.resize(E);
-        for (int e = 0; e < E; ++e) first[e] = B.first_dof(e);
+                    for (int a = 0; a <= p; ++a)
+                        btab[((static_cast<size_t>(e) * quad_order + q) * 2 + k) * (p + 1) + a] = B.b[e][q][k][a];
+        w.assign(B.w, B.w + quad_order);
+        J.assign(B.J, B.J + elements);
+        first.resize(elements);
+        for (int e = 0; e < elements; ++e) first[e] = B.first_dof(e);
         const auto& M = d.M;
-        const int ldab = M.column_size();
+        ldab = M.column_size();
+        kl = M.kl;
+        ku = M.ku;
         lu.assign(M.full_buffer(), M.full_buffer() + static_cast<size_t>(ldab) * M.cols);
         ipiv = d.ctx.pivot_vector;
-        desc.p = P;
-        desc.elements = E;
-        desc.quad_order = Q;
-        desc.n = B.dofs;
-        desc.btab = btab.data();
-        desc.w = w.data();
-        desc.J = J.data();
-        desc.first_dofs = first.data();
-        desc.kl = M.kl;
-        desc.ku = M.ku;
-        desc.ldab = ldab;
-        desc.lu = lu.data();
-        desc.ipiv = ipiv.data();
+    }
+
+    // Descriptor pointing into this object's arrays (valid while it lives).
+    adsg_dim_desc desc() const {
+        adsg_dim_desc d{};
+        d.p = p;
+        d.elements = elements;
+        d.quad_order = quad_order;
+        d.n = n;
+        d.btab = btab.data();
+        d.w = w.data();
+        d.J = J.data();
+        d.first_dofs = first.data();
+        d.kl = kl;
+        d.ku = ku;
+        d.ldab = ldab;
+        d.lu = lu.data();
+        d.ipiv = ipiv.data();
+        return d;
     }
 };
 
@@ -78,9 +89,10 @@ class context {
 public:
     template <typename... Dims>
     explicit context(const Dims&... dims) {
-        std::vector<flat_dim> flat{flat_dim{dims}...};
+        std::vector<flat_dim> flat;
+        (flat.emplace_back(dims), ...);
         std::vector<adsg_dim_desc> descs;
-        for (auto& f : flat) descs.push_back(f.desc);
+        for (const auto& f : flat) descs.push_back(f.desc());
         check(adsg_ctx_create(static_cast<int>(descs.size()), descs.data(), &ctx_));
     }
     explicit context(const std::vector<adsg_dim_desc>& descs) {

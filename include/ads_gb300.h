@@ -176,6 +176,49 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
                  const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
                  int* info);
 
+/* ---- generalised ADS --------------------------------------------------------
+ * ads_solve(rhs, buf, dims..., callable, dims...) with one special dimension
+ * (reference include/ads/solver.hpp:47-195, used by
+ * examples/implicit/implicit.hpp:104-110): along the special direction each
+ * grid line has its own factorised band.  A line-bands object holds nmat
+ * dgbtrf factorisations of one size n (ab: nmat consecutive ldab*n bands,
+ * ipiv: nmat*n 1-based pivots) and line_matrix[l] = the band of line l, with
+ * lines numbered as the reference hands them to its callable: over the
+ * directions that follow the special one cyclically, the first fastest.
+ * adsg_ads_solve_general solves the special direction first, then the other
+ * directions with the context's bands, as the reference does. */
+typedef struct adsg_line_bands adsg_line_bands;
+int adsg_line_bands_create(int n, int kl, int ku, int ldab, int nmat, const double* ab, const int* ipiv,
+                           long long nlines, const int* line_matrix, adsg_line_bands** out);
+int adsg_line_bands_destroy(adsg_line_bands* b);
+int adsg_ads_solve_general(adsg_ctx* ctx, int special_dim, const adsg_line_bands* lines, double* rhs_dev);
+int adsg_ads_solve_general_host(adsg_ctx* ctx, int special_dim, const adsg_line_bands* lines, double* rhs_host);
+
+/* ---- adjoint (reverse mode) ------------------------------------------------
+ * No counterpart in the reference.  For the kappa-weighted explicit step
+ *     u_{k+1} = M^{-1} R(kappa) u_k,
+ *     R(kappa)_ab = sum_e sum_q w_q J_e (B_a B_b - dt kappa(x_q) grad B_a . grad B_b)
+ * (adsg_heat_rhs_elem followed by adsg_ads_solve), an adjoint object runs
+ * nsteps forward from u0 with kappa (spline coefficients on the same space),
+ * keeping checkpoints every checkpoint_every steps (0: ceil(sqrt(nsteps))),
+ * then returns dL/du0 and dL/dkappa for a given dL/du(T).  The backward sweep
+ * recomputes each segment once from its checkpoint and applies
+ *     mu = M^{-T} lambda (transposed line solves),  dL/dkappa += mu^T dR/dkappa u_k,
+ *     lambda <- R(kappa) mu (R is symmetric).
+ * Needs a 2D or 3D context with one degree p <= 4 and p+1 Gauss points.
+ * kappa is copied at forward time; buffers are device pointers of ctx's size. */
+typedef struct adsg_adjoint adsg_adjoint;
+int adsg_adjoint_create(adsg_ctx* ctx, int nsteps, double dt, int checkpoint_every, adsg_adjoint** out);
+int adsg_adjoint_destroy(adsg_adjoint* a);
+int adsg_adjoint_checkpoints(const adsg_adjoint* a, int* every, int* count);
+int adsg_adjoint_forward(adsg_adjoint* a, const double* u0_dev, const double* kappa_dev, double* uT_dev);
+int adsg_adjoint_backward(adsg_adjoint* a, const double* dL_duT_dev, double* grad_u0_dev, double* grad_kappa_dev);
+/* Mass-norm loss L = (u - target)^T (Mx (x) My (x) Mz) (u - target) on the host,
+ * and dL/du = 2 M (u - target) into grad_dev; scratch_dev holds u - target.
+ * Synchronises. */
+int adsg_mass_loss(adsg_ctx* ctx, const double* u_dev, const double* target_dev, double* scratch_dev,
+                   double* loss_host, double* grad_dev);
+
 /* ---- batched simulations ---------------------------------------------------
  * No single counterpart in the reference, whose unit of work is one
  * simulation object run by simulation_base::run (simulation_base.cpp:11-20):

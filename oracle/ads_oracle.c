@@ -663,6 +663,52 @@ int orc_heat_rhs_mt(const orc_problem* pr, const double* u_prev, double* rhs, do
     return 0;
 }
 
+/* Adjoint support (no reference counterpart): g_c += -dt sum_e sum_q W B_c(x_q)
+ * grad u(x_q) . grad mu(x_q), the derivative of mu^T R(kappa) u with respect to
+ * the kappa coefficients, element by element in the reference loop order. */
+int orc_kappa_grad(const orc_problem* pr, const double* u, const double* mu, double* g, double dt) {
+    if (pr->ndim < 2) return -1;
+    long ne = n_elements(pr);
+    int e[ORC_MAXD];
+    for (long id = 0; id < ne; ++id) {
+        element_of(pr, id, e);
+        const orc_dim* X = &pr->d[0];
+        const orc_dim* Y = &pr->d[1];
+        const orc_dim* Z = pr->ndim == 3 ? &pr->d[2] : NULL;
+        int nz = Z ? Z->p + 1 : 1, qzn = Z ? Z->q : 1;
+        long nx = X->n, ny = Y->n;
+        int fx = X->first_dofs[e[0]], fy = Y->first_dofs[e[1]], fz = Z ? Z->first_dofs[e[2]] : 0;
+        double J = X->J[e[0]] * Y->J[e[1]] * (Z ? Z->J[e[2]] : 1.0);
+        for (int qx = 0; qx < X->q; ++qx)
+            for (int qy = 0; qy < Y->q; ++qy)
+                for (int qz = 0; qz < qzn; ++qz) {
+                    double w = X->w[qx] * Y->w[qy] * (Z ? Z->w[qz] : 1.0);
+                    double gu[3] = {0, 0, 0}, gm[3] = {0, 0, 0};
+                    for (int bx = 0; bx <= X->p; ++bx)
+                        for (int by = 0; by <= Y->p; ++by)
+                            for (int bz = 0; bz < nz; ++bz) {
+                                long gi = (fx + bx) + nx * ((fy + by) + ny * (long)(fz + bz));
+                                double B1 = BT(X, e[0], qx, 0, bx), B2 = BT(Y, e[1], qy, 0, by);
+                                double dB1 = BT(X, e[0], qx, 1, bx), dB2 = BT(Y, e[1], qy, 1, by);
+                                double B3 = Z ? BT(Z, e[2], qz, 0, bz) : 1.0, dB3 = Z ? BT(Z, e[2], qz, 1, bz) : 0.0;
+                                double v[3] = {dB1 * B2 * B3, B1 * dB2 * B3, B1 * B2 * dB3};
+                                for (int k = 0; k < 3; ++k) {
+                                    gu[k] += u[gi] * v[k];
+                                    gm[k] += mu[gi] * v[k];
+                                }
+                            }
+                    double sdot = (gu[0] * gm[0] + gu[1] * gm[1] + gu[2] * gm[2]) * w * J * (-dt);
+                    for (int ax = 0; ax <= X->p; ++ax)
+                        for (int ay = 0; ay <= Y->p; ++ay)
+                            for (int az = 0; az < nz; ++az) {
+                                double B = BT(X, e[0], qx, 0, ax) * BT(Y, e[1], qy, 0, ay) * (Z ? BT(Z, e[2], qz, 0, az) : 1.0);
+                                g[(fx + ax) + nx * ((fy + ay) + ny * (long)(fz + az))] += sdot * B;
+                            }
+                }
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* ADS solve (solver.hpp:35-41, 149-160, 199-203). The reference solves all  */
 /* lines of the leading dimension with one dgbtrs (nrhs = size/n0) and then  */

@@ -85,6 +85,10 @@ int orc_heat_rhs_mt(const orc_problem* pr, const double* u_prev, double* rhs, do
 int orc_heat_rhs_kappa(const orc_problem* pr, const double* u_prev, const double* kappa,
                        double* rhs, double dt);
 
+/* Adjoint support (no reference counterpart): g += mu^T (dR/dkappa) u, i.e.
+ * g_c += -dt sum_e sum_q w J B_c(x_q) grad u . grad mu at the quadrature points. */
+int orc_kappa_grad(const orc_problem* pr, const double* u, const double* mu, double* g, double dt);
+
 /* ads_solve(rhs, buf, x.data(), y.data(), z.data()) (solver.hpp:149-160,
  * 199-203): one dgbtrs per grid line, direction by direction; result in rhs. */
 int orc_ads_solve(const orc_problem* pr, double* rhs);

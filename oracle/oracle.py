@@ -47,6 +47,7 @@ def lib() -> ctypes.CDLL:
         L.orc_ads_solve_t.argtypes = [vp, _dp]
         L.orc_heat_steps.argtypes = [vp, _dp, d, i, i]
         L.orc_projection_sin.argtypes = [vp, _dp]
+        L.orc_kappa_grad.argtypes = [vp, _dp, _dp, _dp, d]
         L.orc_gauss.argtypes = [i, _dp, _dp]
         L.orc_dgbtrf.argtypes = [i, i, i, _dp, i, _ip]
         L.orc_dgbtrs.argtypes = [ctypes.c_char, i, i, i, i, _dp, i, _ip, _dp, i]
@@ -121,6 +122,16 @@ class Problem:
         x = np.array(u, np.float64, copy=True, order="C")
         lib().orc_heat_steps(self._h, dp(x), dt, nsteps, nthreads)
         return x
+
+    def kappa_grad(self, u, mu, dt, g=None):
+        g = np.zeros(self.size) if g is None else g
+        lib().orc_kappa_grad(self._h, dp(np.ascontiguousarray(u, np.float64)), dp(np.ascontiguousarray(mu, np.float64)),
+                             dp(g), dt)
+        return g
+
+    def kappa_step(self, u, kappa, dt):
+        """One step of the kappa-weighted scheme: M^{-1} R(kappa) u."""
+        return self.ads_solve(self.heat_rhs_kappa(u, kappa, dt))
 
     def projection_sin(self):
         out = np.zeros(self.size)

@@ -136,6 +136,36 @@ def known_answers(L):
     x = b.copy()
     assert L.ref_band_solve(kl, ku, n, dp(ab), d, dp(x), dp(lu), ip(piv)) == 0
     out["band6_lu"], out["band6_ipiv"], out["band6_ref_x"] = lu, piv, x
+
+    # generalised ADS, tests/ads/solver_test.cpp:257-534: per-line bands along a
+    # special dimension; factorised here by the reference's lin::factorize
+    def fact(rows, n):
+        ab = band_from_rows(1, 1, n, rows)
+        lu = np.zeros_like(ab)
+        pv = np.zeros(n, np.int32)
+        assert L.ref_band_solve(1, 1, n, dp(ab), 0, dp(np.zeros(n)), dp(lu), ip(pv)) == 0
+        return lu, pv
+
+    g2 = {"A": ([[1, 2], [3, 4]], 2), "B1": ([[2, 3], [1, 2, -3], [2, 2]], 3), "B2": ([[1, 2], [3, 1, 2], [2, -1]], 3)}
+    g3 = {"A": ([[2, 3], [1, 2, -3], [2, 2]], 3), "B": ([[1, 2], [3, 4]], 2),
+          "C11": ([[1, 2], [2, 3, 1], [1, -4, 0], [1, 3]], 4), "C21": ([[1, 3], [2, -2, 1], [3, -2, 1], [1, 1]], 4),
+          "C31": ([[3, 0], [1, 2, 1], [2, -1, 3], [3, 1]], 4), "C12": ([[2, 3], [-1, 3, 2], [2, 4, 1], [-2, 1]], 4),
+          "C22": ([[-1, -2], [3, 2, 1], [2, -1, 1], [1, 1]], 4), "C32": ([[2, 1], [-1, 3, 2], [4, 2, 1], [-3, 2]], 4)}
+    for pre, table in (("gen2_", g2), ("gen3_", g3)):
+        for name, (rows, n) in table.items():
+            lu, pv = fact(rows, n)
+            out[pre + "lu_" + name], out[pre + "ipiv_" + name] = lu, pv
+    # right-hand sides of the sections, x-fastest, and their expected solutions
+    out["gen2_rhs_second"] = np.array([43.0, 61, -24, 136, 56, 11])    # sizes {na=2, nb=3}, special = 1
+    out["gen2_rhs_first"] = np.array([54.0, -12, 54, 71, 149, 19])     # sizes {nb=3, na=2}, special = 0
+    out["gen2_expected"] = np.arange(1.0, 7.0)
+    out["gen3_rhs_first"] = np.array([543.0, 1101, -618, 849, -192, -48, -96, -96, 540, 768, 828, 828,
+                                      1900, 1681, 2968, -394, 336, -672, -224, -224, 1192, 1748, 3024, -388])
+    out["gen3_rhs_second"] = np.array([351.0, 1325, 732, 1382, -501, 2471, 718, -293, -384, 672, -96, -1344,
+                                       -192, -448, -192, -448, 492, 1196, 752, 1912, 872, 3276, 872, -380])
+    out["gen3_rhs_third"] = np.array([342.0, -48, 162, 1210, 84, 522, 774, -12, 504, 1934, -168, 1648,
+                                      -792, -24, 864, 3542, -56, 2674, 1206, -24, 864, -326, -56, -118])
+    out["gen3_expected"] = np.arange(1.0, 25.0)
     return out
 
 

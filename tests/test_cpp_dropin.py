@@ -1,0 +1,47 @@
+"""C++ host code drops in: (1) a program built against the reference's own
+classes (ads::simulation_3d, ads::dimension, lin::tensor) drives the GPU
+through ads/gpu.hpp -- built where the reference sources exist; (2) a
+standalone C++ program over the C-ABI reproduces the reference test's 3D
+known-answer ADS system on the GPU."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+REF = "/root/reference/src"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present on this machine")
+def test_reference_program_builds_against_the_bridge():
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    exe = os.path.join(ROOT, "oracle", "_ref", "dropin")
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith(("no-gpu", "ok")), out.stdout
+
+
+def _build_standalone(tmp_path):
+    exe = str(tmp_path / "capi_known_answers")
+    lib_dir = os.path.join(ROOT, "iga-ads_gb300", "ads_gb300")
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "iga-ads_gb300", "include"), "-I",
+           os.path.join(ROOT, "include"), "-o", exe, os.path.join(ROOT, "tests", "cpp", "capi_known_answers.cpp"),
+           os.path.join(lib_dir, "libads_gb300.so"), f"-Wl,-rpath,{lib_dir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return exe
+
+
+def test_standalone_program_compiles(tmp_path):
+    _build_standalone(tmp_path)
+
+
+@pytest.mark.gpu
+def test_standalone_program_known_answers_on_gpu(tmp_path, cuda):
+    exe = _build_standalone(tmp_path)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout + out.stderr

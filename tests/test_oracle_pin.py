@@ -139,3 +139,28 @@ def test_kappa_one_reduces_to_heat():
     kappa = np.ones(pr.size)
     a = pr.heat_rhs_kappa(g["u0"], kappa, float(g["dt"]))
     assert oracle.rel_l2(a, g["rhs"]) <= 1e-13
+
+
+def test_oracle_adjoint_matches_finite_differences():
+    """The oracle's adjoint (transposed solves, R(kappa) symmetric, kappa
+    gradient assembly) against central differences of the oracle forward."""
+    import _adjoint_ref as ar
+
+    pr = oracle.Problem([2, 3], [5, 4])
+    rng = np.random.default_rng(4)
+    u0 = rng.uniform(-1, 1, pr.size)
+    kappa = 1 + 0.3 * rng.uniform(-1, 1, pr.size)
+    target = rng.uniform(-1, 1, pr.size)
+    dt, N = 2e-3, 4
+    L, gu, gk = ar.gradients(pr, u0, kappa, dt, N, target)
+
+    def loss(u, k):
+        return ar.mass_loss(pr, ar.forward(pr, u, k, dt, N)[-1], target)[0]
+
+    for seed in range(3):
+        d = np.random.default_rng(100 + seed).standard_normal(pr.size)
+        h = 1e-5
+        fd_u = (loss(u0 + h * d, kappa) - loss(u0 - h * d, kappa)) / (2 * h)
+        assert abs(fd_u - gu @ d) <= 1e-7 * max(abs(fd_u), 1e-30)
+        fd_k = (loss(u0, kappa + h * d) - loss(u0, kappa - h * d)) / (2 * h)
+        assert abs(fd_k - gk @ d) <= 1e-6 * max(abs(fd_k), 1e-30)
