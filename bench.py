@@ -63,6 +63,27 @@ def dist_env():
     return rank, world, local
 
 
+def dist_max(x: float, device=None) -> float:
+    """Maximum of x over all ranks (x itself without a process group)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, steps: int, seconds_per_rank: float, device=None) -> float:
+    """Whole-job throughput of N independent replicas: all units over the
+    slowest rank's time (each rank runs the same workload)."""
+    import torch.distributed as dist
+
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    return world * units_per_rank * steps / dist_max(seconds_per_rank, device)
+
+
 def workload_config(name):
     if name == "batch64":
         import ads_gb300 as ads
@@ -308,12 +329,8 @@ def run_ours(args, cfg):
         torch.distributed.barrier()
     clocks = sampler.stop()
     stage = ctx.stage_times()
-    step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if world > 1:
-        t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = world * size * args.steps / (step_ms * 1e-3)
+    step_ms = dist_max(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), dev)
+    value = replica_throughput(size, args.steps, step_ms * 1e-3, dev)
 
     # --- element-wise sum-factorised quadrature (the general RHS path), timed alone ---
     elem = None
@@ -340,12 +357,8 @@ def run_ours(args, cfg):
     t0 = time.perf_counter()
     for _ in range(ke):
         ctx.heat_steps_host(hnp, dt, 1)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * size * ke / e2e_s
+    e2e_s = dist_max(time.perf_counter() - t0, dev)
+    e2e = replica_throughput(size, ke, e2e_s, dev)
 
     # --- roofline of the dominant kernel ---
     work = ctx.stage_work()

@@ -52,6 +52,7 @@ class DimDesc(ctypes.Structure):
         ("ldab", ctypes.c_int),
         ("lu", _c_double_p),
         ("ipiv", _c_int_p),
+        ("xq", _c_double_p),
     ]
 
 
@@ -93,6 +94,13 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_stage_times": (i, [vp, _c_double_p, ctypes.POINTER(ctypes.c_longlong)]),
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
+        "adsg_quad_size": (ll, [vp]),
+        "adsg_load_vector": (i, [vp, vp, vp]),
+        "adsg_projection": (i, [vp, vp, vp]),
+        "adsg_eval_quad": (i, [vp, vp, vp, vp]),
+        "adsg_norms": (i, [vp, vp, _c_double_p, _c_double_p]),
+        "adsg_errors": (i, [vp, vp, vp, vp, _c_double_p, _c_double_p]),
+        "adsg_quad_points": (i, [vp, i, _c_double_p]),
         "adsg_adjoint_create": (i, [vp, i, d, i, ctypes.POINTER(vp)]),
         "adsg_adjoint_destroy": (i, [vp]),
         "adsg_adjoint_checkpoints": (i, [vp, _c_int_p, _c_int_p]),
@@ -224,6 +232,7 @@ class Dimension:
             "first_dofs": np.ctypeslib.as_array(d.first_dofs, (d.elements,)).copy(),
             "lu": np.ctypeslib.as_array(d.lu, (d.ldab * d.n,)).copy(),
             "ipiv": np.ctypeslib.as_array(d.ipiv, (d.n,)).copy(),
+            "xq": np.ctypeslib.as_array(d.xq, (d.elements * d.quad_order,)).copy(),
             "kl": d.kl,
             "ku": d.ku,
             "ldab": d.ldab,
@@ -304,6 +313,37 @@ class Context:
 
     def heat_steps(self, u, dt: float, nsteps: int) -> None:
         _check(library().adsg_heat_steps(self._h, _devptr(u), float(dt), int(nsteps)))
+
+    # --- Gauss-point utilities ------------------------------------------
+    @property
+    def quad_size(self) -> int:
+        return int(library().adsg_quad_size(self._h))
+
+    def quad_points(self, d: int) -> np.ndarray:
+        dim = self.dims[d]
+        out = np.empty(dim.elements * dim.quad_order)
+        _check(library().adsg_quad_points(self._h, d, _dptr(out)))
+        return out
+
+    def load_vector(self, fq, out) -> None:
+        _check(library().adsg_load_vector(self._h, _devptr(fq), _devptr(out)))
+
+    def projection(self, fq, out) -> None:
+        _check(library().adsg_projection(self._h, _devptr(fq), _devptr(out)))
+
+    def eval_quad(self, u, val, grad=None) -> None:
+        _check(library().adsg_eval_quad(self._h, _devptr(u), _devptr(val), _devptr(grad)))
+
+    def norms(self, u) -> tuple:
+        l2, h1 = ctypes.c_double(), ctypes.c_double()
+        _check(library().adsg_norms(self._h, _devptr(u), ctypes.byref(l2), ctypes.byref(h1)))
+        return l2.value, h1.value
+
+    def errors(self, u, fq, fgrad=None) -> tuple:
+        l2, h1 = ctypes.c_double(), ctypes.c_double()
+        _check(library().adsg_errors(self._h, _devptr(u), _devptr(fq), _devptr(fgrad), ctypes.byref(l2),
+                                     ctypes.byref(h1)))
+        return l2.value, (h1.value if h1.value >= 0 else None)
 
     # --- host-buffer entry points ---------------------------------------
     def heat_steps_host(self, u: np.ndarray, dt: float, nsteps: int) -> None:

@@ -281,6 +281,7 @@ int adsg_dim_describe(const adsg_dim* d, adsg_dim_desc* out) {
     out->ldab = h.ldab;
     out->lu = h.lu.data();
     out->ipiv = h.ipiv.data();
+    out->xq = h.xq.data();
     return 0;
 }
 

@@ -772,6 +772,11 @@ __global__ void dot_final_kernel(const double* __restrict__ partial, int m, doub
     if (threadIdx.x == 0) *out = sh[0];
 }
 
+cudaError_t launch_sum(const double* partial, int m, double* out, cudaStream_t s) {
+    dot_final_kernel<<<1, 256, 0, s>>>(partial, m, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_dot(const double* x, const double* y, long long n, double* partial, double* out, cudaStream_t s) {
     dot_partial_kernel<<<kDotBlocks, 256, 0, s>>>(x, y, n, partial);
     dot_final_kernel<<<1, 256, 0, s>>>(partial, kDotBlocks, out);

@@ -31,6 +31,7 @@ struct dim_dev {
     const double* wq = nullptr;     // [q]
     const double* jac = nullptr;    // [E]
     const int* first = nullptr;     // [E]
+    const int* erange = nullptr;    // [n][2] first and last element supporting each dof
 };
 
 // Where the grid lines of one direction sit in a tensor of extents n[0..2]
@@ -104,6 +105,23 @@ cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, co
 // small vector kernels of the adjoint driver
 cudaError_t launch_axpby(double* y, double a, const double* x, double b, long long n, cudaStream_t s);  // y = a*x + b*y
 cudaError_t launch_dot(const double* x, const double* y, long long n, double* partial, double* out, cudaStream_t s);
+
+cudaError_t launch_sum(const double* partial, int m, double* out, cudaStream_t s);  // deterministic sum
+
+// quadrature-point passes (adsg_quad.cu); tensors are x-fastest, the pass acts
+// on the axis with `inner` faster entries and `outer` slower ones
+cudaError_t launch_quad_interp(const double* in, double* out0, double* out1, const dim_dev& d, long long inner,
+                               long long outer, cudaStream_t s);
+cudaError_t launch_quad_project(const double* in, double* out, const dim_dev& d, const int* erange, long long inner,
+                                long long outer, cudaStream_t s);
+struct field_set {
+    int nf = 0;
+    const double* a[4] = {nullptr, nullptr, nullptr, nullptr};
+    const double* b[4] = {nullptr, nullptr, nullptr, nullptr};  // NULL: compare with zero
+};
+// sum over Gauss points of W * sum_k (a_k - b_k)^2 into out (device scalar)
+cudaError_t launch_quad_wdiff(const field_set& F, const dim_dev* dims, int ndim, long long total, double* partial,
+                              double* out, cudaStream_t s);
 
 cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev, const double* kappa,
                             double* rhs, double dt, cudaStream_t s);

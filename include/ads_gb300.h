@@ -57,6 +57,8 @@ typedef struct adsg_dim_desc {
     int kl, ku, ldab;       /* band parameters of the factorised matrix */
     const double* lu;       /* dgbtrf output, ldab*n doubles */
     const int* ipiv;        /* [n] 1-based pivots */
+    const double* xq;       /* [elements][quad_order] Gauss points (basis_data::x);
+                               optional (NULL): only adsg_quad_points needs it */
 } adsg_dim_desc;
 
 /* Build a dimension on the host exactly as the reference's dimension ctor
@@ -175,6 +177,32 @@ int adsg_heat_rhs_host(adsg_ctx* ctx, const double* u_prev_host, double* rhs_hos
 int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs,
                  const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
                  int* info);
+
+/* ---- Gauss-point utilities: projection, norms, errors -----------------------
+ * Point tensors are x-fastest over the Gauss points of all elements of every
+ * direction: point (rx, ry, rz) with rd = e_d * q_d + k_d.
+ *  - adsg_load_vector: b_a = sum_e sum_q f(x_q) B_a(x_q) w_q J_e, the load
+ *    vector of compute_projection (reference include/ads/projection.hpp:55-107);
+ *  - adsg_projection: the load vector followed by adsg_ads_solve (the
+ *    reference's projection(u, f); solve(u), heat_3d.hpp:35-36);
+ *  - adsg_eval_quad: values and (grad_dev != NULL) the ndim first derivatives
+ *    of a spline at every Gauss point (eval / eval_fun of simulation_3d.hpp);
+ *  - adsg_norms: normL2 and normH1 of a spline (basic_simulation_3d.hpp:309-335),
+ *    computed as sqrt(u^T M u) and sqrt(u^T (M + K) u) with the Kronecker
+ *    mass/stiffness operators of the heat RHS;
+ *  - adsg_errors: errorL2 / errorH1 against point values (and gradients) of a
+ *    reference function (basic_simulation_3d.hpp:337-397); h1_out is set to -1
+ *    when fgrad_dev is NULL;
+ *  - adsg_quad_points: the Gauss points of direction d (needs desc.xq).
+ * All synchronise except adsg_load_vector, adsg_projection, adsg_eval_quad. */
+long long adsg_quad_size(const adsg_ctx* ctx);
+int adsg_load_vector(adsg_ctx* ctx, const double* fq_dev, double* out_dev);
+int adsg_projection(adsg_ctx* ctx, const double* fq_dev, double* out_dev);
+int adsg_eval_quad(adsg_ctx* ctx, const double* u_dev, double* val_dev, double* grad_dev);
+int adsg_norms(adsg_ctx* ctx, const double* u_dev, double* l2_out, double* h1_out);
+int adsg_errors(adsg_ctx* ctx, const double* u_dev, const double* fq_dev, const double* fgrad_dev, double* l2_out,
+                double* h1_out);
+int adsg_quad_points(const adsg_ctx* ctx, int d, double* xq_host);
 
 /* ---- generalised ADS --------------------------------------------------------
  * ads_solve(rhs, buf, dims..., callable, dims...) with one special dimension
