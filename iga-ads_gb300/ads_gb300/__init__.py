@@ -95,6 +95,7 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
         "adsg_quad_size": (ll, [vp]),
+        "adsg_count_nonfinite": (i, [vp, vp, ctypes.POINTER(ll)]),
         "adsg_load_vector": (i, [vp, vp, vp]),
         "adsg_projection": (i, [vp, vp, vp]),
         "adsg_eval_quad": (i, [vp, vp, vp, vp]),
@@ -313,6 +314,12 @@ class Context:
 
     def heat_steps(self, u, dt: float, nsteps: int) -> None:
         _check(library().adsg_heat_steps(self._h, _devptr(u), float(dt), int(nsteps)))
+
+    def count_nonfinite(self, u) -> int:
+        """Number of NaN / Inf entries of a device tensor (failure detection)."""
+        c = ctypes.c_longlong()
+        _check(library().adsg_count_nonfinite(self._h, _devptr(u), ctypes.byref(c)))
+        return c.value
 
     # --- Gauss-point utilities ------------------------------------------
     @property

@@ -928,6 +928,20 @@ int enqueue_load_vector(adsg_ctx* c, const double* fq, double* out) {
 
 long long adsg_quad_size(const adsg_ctx* ctx) { return ctx ? quad_total(ctx) : 0; }
 
+int adsg_count_nonfinite(adsg_ctx* ctx, const double* u_dev, long long* count_out) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_dev) return fail(-2, "u is NULL");
+    if (!count_out) return fail(-3, "count is NULL");
+    if (!ctx->red) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->red, 1025), "reduction alloc");
+    auto* cnt = reinterpret_cast<unsigned long long*>(ctx->red + 1024);
+    ADSG_CUDA_TRY(launch_count_nonfinite(u_dev, ctx->size, cnt, ctx->stream), "count");
+    unsigned long long host = 0;
+    ADSG_CUDA_TRY(cudaMemcpyAsync(&host, cnt, sizeof(host), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    *count_out = static_cast<long long>(host);
+    return 0;
+}
+
 int adsg_load_vector(adsg_ctx* ctx, const double* fq_dev, double* out_dev) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!fq_dev) return fail(-2, "fq is NULL");

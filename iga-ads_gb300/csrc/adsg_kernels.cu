@@ -772,6 +772,21 @@ __global__ void dot_final_kernel(const double* __restrict__ partial, int m, doub
     if (threadIdx.x == 0) *out = sh[0];
 }
 
+__global__ void count_nonfinite_kernel(const double* __restrict__ x, long long n, unsigned long long* __restrict__ count) {
+    unsigned long long local = 0;
+    for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += 256LL * gridDim.x) local += isfinite(x[i]) ? 0 : 1;
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+cudaError_t launch_count_nonfinite(const double* x, long long n, unsigned long long* count, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 8);
+    count_nonfinite_kernel<<<static_cast<int>(std::max<long long>(blocks, 1)), 256, 0, s>>>(x, n, count);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sum(const double* partial, int m, double* out, cudaStream_t s) {
     dot_final_kernel<<<1, 256, 0, s>>>(partial, m, out);
     return cudaGetLastError();

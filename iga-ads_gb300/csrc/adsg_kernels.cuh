@@ -107,6 +107,7 @@ cudaError_t launch_axpby(double* y, double a, const double* x, double b, long lo
 cudaError_t launch_dot(const double* x, const double* y, long long n, double* partial, double* out, cudaStream_t s);
 
 cudaError_t launch_sum(const double* partial, int m, double* out, cudaStream_t s);  // deterministic sum
+cudaError_t launch_count_nonfinite(const double* x, long long n, unsigned long long* count, cudaStream_t s);
 
 // quadrature-point passes (adsg_quad.cu); tensors are x-fastest, the pass acts
 // on the axis with `inner` faster entries and `outer` slower ones

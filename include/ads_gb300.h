@@ -196,6 +196,10 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
  *  - adsg_quad_points: the Gauss points of direction d (needs desc.xq).
  * All synchronise except adsg_load_vector, adsg_projection, adsg_eval_quad. */
 long long adsg_quad_size(const adsg_ctx* ctx);
+/* Failure detection: the number of NaN / Inf coefficients of a device tensor
+ * of the context's size (an explicit step that is unstable for its dt grows
+ * until it overflows).  Synchronises. */
+int adsg_count_nonfinite(adsg_ctx* ctx, const double* u_dev, long long* count_out);
 int adsg_load_vector(adsg_ctx* ctx, const double* fq_dev, double* out_dev);
 int adsg_projection(adsg_ctx* ctx, const double* fq_dev, double* out_dev);
 int adsg_eval_quad(adsg_ctx* ctx, const double* u_dev, double* val_dev, double* grad_dev);

@@ -306,3 +306,21 @@ def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypa
     assert all(0 <= v <= 3 for v in chosen)
     if variant in (0, 3):  # always applicable for p <= 4
         assert chosen == [variant] * len(p)
+
+
+def test_failure_detection_counts_nonfinite(cuda):
+    """An unstable dt drives the explicit step to overflow; the device count of
+    non-finite coefficients reports it (failure made on the host side: only
+    the data diverges, no kernel misbehaves)."""
+    import torch
+
+    dims, ctx = _ctx(2, 4, 24)
+    u = torch.from_numpy(np.random.default_rng(0).uniform(-1, 1, ctx.size)).cuda()
+    assert ctx.count_nonfinite(u) == 0
+    u[5] = float("nan")
+    u[7] = float("inf")
+    assert ctx.count_nonfinite(u) == 2
+    v = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, ctx.size)).cuda()
+    ctx.heat_steps(v, 1e-1, 400)  # far above the stability limit
+    ctx.synchronize()
+    assert ctx.count_nonfinite(v) > 0

@@ -11,6 +11,7 @@ import pytest
 
 import ads_gb300 as ads
 import oracle
+from _tol import mass_condition
 
 pytestmark = pytest.mark.gpu
 
@@ -49,7 +50,9 @@ def test_projection_matches_reference_projection(nd, p, E, cuda):
         pr = oracle.Problem([p] * nd, [E] * nd)
         ref_b = pr.projection_sin()  # bit-identical to the reference's compute_projection
         assert oracle.rel_l2(b.cpu().numpy(), ref_b) <= 1e-14
-        assert oracle.rel_l2(u.cpu().numpy(), pr.ads_solve(ref_b)) <= 1e-13
+        # the solve amplifies the load vector's rounding by up to cond(Mx (x) My (x) Mz)
+        cond = np.prod([mass_condition(d.form_band(0).ravel(), p) for d in dims])
+        assert oracle.rel_l2(u.cpu().numpy(), pr.ads_solve(ref_b)) <= max(1e-13, 1e-14 * cond)
 
 
 @pytest.mark.parametrize("nd,p,E", [(2, 2, 7), (3, 3, 5), (3, 2, 8)])
