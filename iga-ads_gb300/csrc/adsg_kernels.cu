@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "adsg_kernels.cuh"
 
@@ -111,6 +113,27 @@ cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* k
 // direction's lines where they lie.
 // ---------------------------------------------------------------------------
 constexpr int kPitch = 33;
+
+// Raise a kernel's dynamic shared-memory limit on the current device once
+// (the attribute is per device; a small table remembers what was set).
+cudaError_t ensure_smem_attribute(const void* func, size_t bytes) {
+    struct entry {
+        const void* func;
+        int device;
+        size_t bytes;
+    };
+    static std::mutex lock;
+    static std::vector<entry> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(lock);
+    for (const entry& x : done)
+        if (x.func == func && x.device == dev && x.bytes >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (e == cudaSuccess) done.push_back({func, dev, bytes});
+    return e;
+}
 
 
 line_layout make_line_layout(const int* n, int ndim, int d) {
@@ -578,12 +601,9 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
 template <int KL, int KU>
 static cudaError_t line_solve_t(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
     const size_t smem = line_solve_smem_per_warp(d.n);
-    static size_t configured = 0;  // per instantiation; set before first use above 48 KB
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(line_solve_kernel<KL, KU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem));
+    if (smem > 48 * 1024) {
+        cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(line_solve_kernel<KL, KU>), smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
     }
     const long long blocks = (L.nlines + 31) / 32;
     line_solve_kernel<KL, KU><<<blocks, 32, smem, s>>>(data, d, L, trans);
@@ -613,12 +633,9 @@ template <int KL, int KU, int WPB>
 static cudaError_t staged_t(double* data, const dim_dev& d, const line_layout& L, cudaStream_t s) {
     const size_t smem = line_solve_smem_per_warp(d.n) * WPB;
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(line_solve_staged_kernel<KL, KU, WPB>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (smem > 48 * 1024) {
+        cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(line_solve_staged_kernel<KL, KU, WPB>), smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
     }
     const long long per = 32LL * WPB;
     line_solve_staged_kernel<KL, KU, WPB><<<(L.nlines + per - 1) / per, 32 * WPB, smem, s>>>(data, d, L);
