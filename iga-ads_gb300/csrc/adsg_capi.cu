@@ -7,6 +7,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -92,6 +94,208 @@ int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const i
     return 0;
 }
 
+namespace {
+
+// LAPACK dgbtrs order ('N') on one right-hand side, for the twisted self-check.
+void host_band_solve(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, double* b) {
+    const int kv = kl + ku;
+    for (int j = 0; j + 1 < n; ++j) {
+        const int p = ipiv[j] - 1;
+        if (p != j) std::swap(b[p], b[j]);
+        for (int i = 1; i <= kl && j + i < n; ++i) b[j + i] -= ab[static_cast<size_t>(j) * ldab + kv + i] * b[j];
+    }
+    for (int j = n - 1; j >= 0; --j) {
+        const double* col = ab + static_cast<size_t>(j) * ldab;
+        b[j] /= col[kv];
+        for (int d = 1; d <= kv && d <= j; ++d) b[j - d] -= col[kv - d] * b[j];
+    }
+}
+
+// One chain of the twisted solve, in the kernel's operation order: x points
+// at chain-local row 0, rows advance by es.  own/other: the chains' tails.
+void host_twisted_forward(const twisted_tables& t, int chain, double* x, long long es) {
+    const int k = t.k, nc = chain ? t.n2 : t.n1;
+    const double* l = t.lmul.data() + static_cast<size_t>(chain) * t.rows * k;
+    for (int j = 0; j < nc; ++j)
+        for (int i = 1; i <= k && j + i < nc; ++i) x[(j + i) * es] -= l[static_cast<size_t>(j) * k + i - 1] * x[j * es];
+}
+
+void host_twisted_backward(const twisted_tables& t, int chain, double* x, long long es, const double* other_tail) {
+    const int k = t.k, nc = chain ? t.n2 : t.n1;
+    const double* u = t.ucol.data() + static_cast<size_t>(chain) * t.rows * k;
+    const double* r = t.rdiag.data() + static_cast<size_t>(chain) * t.rows;
+    const double* g = t.g.data() + static_cast<size_t>(chain) * 2 * k * k;
+    std::vector<double> own(k), z(k);
+    for (int i = 0; i < k; ++i) own[i] = x[(nc - k + i) * es];
+    for (int a = 0; a < k; ++a) {
+        double s = 0.0;
+        for (int i = 0; i < k; ++i) s += g[a * 2 * k + i] * own[i];
+        for (int i = 0; i < k; ++i) s += g[a * 2 * k + k + i] * other_tail[i];
+        z[a] = s;
+    }
+    for (int c = nc - 1; c >= 0; --c) {
+        const double v = c >= nc - k ? z[c - (nc - k)] : x[c * es] * r[c];
+        x[c * es] = v;
+        for (int d = 1; d <= k && c - d >= 0; ++d) x[(c - d) * es] -= v * u[static_cast<size_t>(c) * k + d - 1];
+    }
+}
+
+}  // namespace
+
+int make_twisted_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, twisted_tables& t) {
+    const int k = kl;
+    if (kl != ku || k < 1 || k > 4 || n < 4 * k + 2) return 1;
+    const int kv = kl + ku;
+    // 1. the matrix itself, A = P0 L0 P1 L1 ... U, rebuilt densely from the factors
+    std::vector<double> A(static_cast<size_t>(n) * n, 0.0);
+    auto at = [&](int i, int j) -> double& { return A[static_cast<size_t>(i) * n + j]; };
+    for (int j = 0; j < n; ++j)
+        for (int d = 0; d <= kv && d <= j; ++d) at(j - d, j) = ab[static_cast<size_t>(j) * ldab + kv - d];
+    for (int j = n - 1; j >= 0; --j) {
+        const double* col = ab + static_cast<size_t>(j) * ldab;
+        for (int i = 1; i <= kl && j + i < n; ++i) {
+            const double l = col[kv + i];
+            if (l == 0.0) continue;
+            for (int c = j; c < n && c <= j + kv; ++c) at(j + i, c) += l * at(j, c);
+        }
+        const int p = ipiv[j] - 1;
+        if (p != j)
+            for (int c = 0; c < n; ++c) std::swap(at(j, c), at(p, c));
+    }
+    double amax = 0.0, outside = 0.0;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const double v = std::fabs(at(i, j));
+            if (j - i > ku || i - j > kl) {
+                outside = std::max(outside, v);
+                at(i, j) = 0.0;
+            } else {
+                amax = std::max(amax, v);
+            }
+        }
+    if (!(amax > 0.0) || outside > 1e-12 * amax) return 2;
+
+    // 2. chain 0: rows [0, n1) eliminated top-down over columns [0, n1 + k)
+    const int n1 = n / 2, n2 = n - n1, rows = n2 + 16;
+    t.k = k;
+    t.n1 = n1;
+    t.n2 = n2;
+    t.rows = rows;
+    t.lmul.assign(2 * static_cast<size_t>(rows) * k, 0.0);
+    t.ucol.assign(2 * static_cast<size_t>(rows) * k, 0.0);
+    t.rdiag.assign(2 * static_cast<size_t>(rows), 0.0);
+    t.g.assign(2 * static_cast<size_t>(k) * 2 * k, 0.0);
+    std::vector<double> S(static_cast<size_t>(2 * k) * 2 * k, 0.0);  // interface rows over x[n1-k .. n1+k)
+    for (int chain = 0; chain < 2; ++chain) {
+        const int nc = chain ? n2 : n1;
+        const int width = nc + k;
+        // B(i, j): chain-local entries; chain 1 reads A with rows and columns reversed
+        std::vector<double> B(static_cast<size_t>(nc) * width, 0.0);
+        for (int i = 0; i < nc; ++i)
+            for (int j = std::max(0, i - k); j < width && j <= i + k; ++j)
+                B[static_cast<size_t>(i) * width + j] = chain ? at(n - 1 - i, n - 1 - j) : at(i, j);
+        double* l = t.lmul.data() + static_cast<size_t>(chain) * rows * k;
+        double* u = t.ucol.data() + static_cast<size_t>(chain) * rows * k;
+        double* r = t.rdiag.data() + static_cast<size_t>(chain) * rows;
+        for (int j = 0; j < nc; ++j) {
+            const double piv = B[static_cast<size_t>(j) * width + j];
+            if (!(std::fabs(piv) > 1e-8 * amax)) return 3;
+            for (int i = j + 1; i < nc && i <= j + k; ++i) {
+                const double m = B[static_cast<size_t>(i) * width + j] / piv;
+                l[static_cast<size_t>(j) * k + (i - j - 1)] = m;
+                B[static_cast<size_t>(i) * width + j] = 0.0;
+                for (int c = j + 1; c < width && c <= j + k; ++c)
+                    B[static_cast<size_t>(i) * width + c] -= m * B[static_cast<size_t>(j) * width + c];
+            }
+        }
+        double umax = 0.0;
+        for (int c = 0; c < nc; ++c) {
+            r[c] = 1.0 / B[static_cast<size_t>(c) * width + c];
+            for (int d = 0; d <= k && c - d >= 0; ++d) {
+                const double v = B[static_cast<size_t>(c - d) * width + c];
+                umax = std::max(umax, std::fabs(v));
+                if (d > 0) u[static_cast<size_t>(c) * k + d - 1] = v;
+            }
+        }
+        if (umax > 1e4 * amax) return 4;  // element growth: unpivoted elimination not trusted
+        // tail rows -> interface rows; chain-local column c is x[c] (chain 0) or x[n-1-c] (chain 1)
+        for (int rr = 0; rr < k; ++rr) {
+            const int i = nc - k + rr;
+            for (int c = nc - k; c < nc + k; ++c) {
+                const int xi = chain ? n - 1 - c : c;
+                S[static_cast<size_t>(chain * k + rr) * 2 * k + (xi - (n1 - k))] = B[static_cast<size_t>(i) * width + c];
+            }
+        }
+    }
+    // 3. inverse of the 2k x 2k interface matrix (Gauss-Jordan, partial pivoting)
+    const int m2 = 2 * k;
+    std::vector<double> W(S), Inv(static_cast<size_t>(m2) * m2, 0.0);
+    for (int i = 0; i < m2; ++i) Inv[static_cast<size_t>(i) * m2 + i] = 1.0;
+    double smax = 0.0;
+    for (double v : S) smax = std::max(smax, std::fabs(v));
+    for (int c = 0; c < m2; ++c) {
+        int pr = c;
+        for (int i = c + 1; i < m2; ++i)
+            if (std::fabs(W[static_cast<size_t>(i) * m2 + c]) > std::fabs(W[static_cast<size_t>(pr) * m2 + c])) pr = i;
+        if (!(std::fabs(W[static_cast<size_t>(pr) * m2 + c]) > 1e-10 * smax)) return 5;
+        for (int j = 0; j < m2; ++j) {
+            std::swap(W[static_cast<size_t>(c) * m2 + j], W[static_cast<size_t>(pr) * m2 + j]);
+            std::swap(Inv[static_cast<size_t>(c) * m2 + j], Inv[static_cast<size_t>(pr) * m2 + j]);
+        }
+        const double d = W[static_cast<size_t>(c) * m2 + c];
+        for (int j = 0; j < m2; ++j) {
+            W[static_cast<size_t>(c) * m2 + j] /= d;
+            Inv[static_cast<size_t>(c) * m2 + j] /= d;
+        }
+        for (int i = 0; i < m2; ++i) {
+            if (i == c) continue;
+            const double f = W[static_cast<size_t>(i) * m2 + c];
+            if (f == 0.0) continue;
+            for (int j = 0; j < m2; ++j) {
+                W[static_cast<size_t>(i) * m2 + j] -= f * W[static_cast<size_t>(c) * m2 + j];
+                Inv[static_cast<size_t>(i) * m2 + j] -= f * Inv[static_cast<size_t>(c) * m2 + j];
+            }
+        }
+    }
+    // z = Inv [tail0; tail1] with z over x[n1-k .. n1+k).  Chain 0 owns z[0..k)
+    // (its rows n1-k..n1-1); chain 1 owns z[k..2k) in reverse (its local row
+    // n2-k+a is x[n1+k-1-a] = z[2k-1-a]).  Each chain's g row lists its own
+    // tail's coefficients first.
+    for (int a = 0; a < k; ++a)
+        for (int i = 0; i < k; ++i) {
+            t.g[static_cast<size_t>(a) * m2 + i] = Inv[static_cast<size_t>(a) * m2 + i];
+            t.g[static_cast<size_t>(a) * m2 + k + i] = Inv[static_cast<size_t>(a) * m2 + k + i];
+            const size_t row1 = static_cast<size_t>(m2 - 1 - a) * m2;
+            t.g[static_cast<size_t>(k) * m2 + static_cast<size_t>(a) * m2 + i] = Inv[row1 + k + i];
+            t.g[static_cast<size_t>(k) * m2 + static_cast<size_t>(a) * m2 + k + i] = Inv[row1 + i];
+        }
+    // 4. self-check against the LAPACK-order solve on a fixed pseudo-random right-hand side
+    std::vector<double> b(n), x(n);
+    unsigned long long state = 0x9E3779B97F4A7C15ULL;
+    for (int i = 0; i < n; ++i) {
+        state = state * 6364136223846793005ULL + 1442695040888963407ULL;
+        b[i] = static_cast<double>(state >> 11) * 0x1.0p-53 - 0.5;
+    }
+    x = b;
+    host_band_solve(n, kl, ku, ldab, ab, ipiv, b.data());
+    host_twisted_forward(t, 0, x.data(), 1);
+    host_twisted_forward(t, 1, x.data() + n - 1, -1);
+    std::vector<double> tail0(k), tail1(k);
+    for (int i = 0; i < k; ++i) {
+        tail0[i] = x[n1 - k + i];
+        tail1[i] = x[n - 1 - (n2 - k + i)];
+    }
+    host_twisted_backward(t, 0, x.data(), 1, tail1.data());
+    host_twisted_backward(t, 1, x.data() + n - 1, -1, tail0.data());
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i < n; ++i) {
+        num += (x[i] - b[i]) * (x[i] - b[i]);
+        den += b[i] * b[i];
+    }
+    if (!(num <= 1e-24 * den)) return 6;
+    return 0;
+}
+
 }  // namespace adsg
 
 using namespace adsg;
@@ -129,6 +333,10 @@ struct dev_arena {
 
 }  // namespace
 
+namespace adsg {
+void detach_adjoints(adsg_ctx* c);
+}
+
 struct adsg_ctx {
     int ndim = 0;
     int n[3] = {1, 1, 1};
@@ -160,6 +368,8 @@ struct adsg_ctx {
     std::vector<cudaEvent_t> spare;
     double stage_ms[ADSG_NSTAGES] = {};
     long long stage_launches[ADSG_NSTAGES] = {};
+    // adjoints created on this context (detached when the context goes first)
+    std::vector<adsg_adjoint*> adjoints;
 
     cudaEvent_t take_event() {
         if (!spare.empty()) {
@@ -286,47 +496,97 @@ int enqueue_solve(adsg_ctx* c, double* x, int trans) {
     return 0;
 }
 
+std::mutex g_autotune_lock;
+std::map<std::string, int> g_autotune_cache;
+
 // Autotuner: time every applicable line-solve variant per direction on the
 // context's own state buffer (zeros) and keep the fastest.  ADSG_SOLVE_VARIANT
-// (0..3) forces one variant where applicable.
+// (0..5) forces one variant where applicable; ADSG_AUTOTUNE_LOG=1 prints each
+// candidate's time to stderr.  A candidate whose launch reports an error is
+// dropped (the error is cleared so that it cannot leak into the next one).
 int autotune_solves(adsg_ctx* c) {
     const char* force = std::getenv("ADSG_SOLVE_VARIANT");
     int forced = -1;
     if (force && *force) forced = std::atoi(force);
+    const char* logv = std::getenv("ADSG_AUTOTUNE_LOG");
+    const bool log = logv && *logv && *logv != '0';
     ADSG_CUDA_TRY(cudaMemsetAsync(c->ping, 0, sizeof(double) * c->size, c->stream), "autotune memset");
+    ADSG_CUDA_TRY(cudaStreamSynchronize(c->stream), "autotune memset");
     cudaEvent_t a, b;
     ADSG_CUDA_TRY(cudaEventCreate(&a), "event");
-    ADSG_CUDA_TRY(cudaEventCreate(&b), "event");
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return fail_cuda(cudaGetLastError(), "event");
+    }
     int rc = 0;
     for (int d = 0; d < c->ndim && rc == 0; ++d) {
         dim_dev& D = c->dims[d];
         const line_layout L = make_line_layout(c->n, c->ndim, d);
         if (forced >= 0 && forced < SOLVE_NVARIANTS && line_solve_variant_ok(forced, D)) {
             D.solve_variant = forced;
+            if (log) std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d forced variant %d\n", d, D.n, forced);
             continue;
         }
-        float best = 1e30f;
-        int best_v = SOLVE_STAGED_1;
+        // one decision per (device, shape, direction) and process, so that
+        // contexts of the same shape run the same kernels (bitwise equal results)
+        int dev = 0;
+        cudaGetDevice(&dev);
+        char key[192];
+        std::snprintf(key, sizeof key, "%d|%d|%d,%d,%d|%d|%d,%d,%d,%d,%d,%d,%d", dev, c->ndim, c->n[0], c->n[1], c->n[2], d,
+                      D.p, D.kl, D.w, D.ku_regular, D.fwd_fast, D.bwd_fast, D.tw_k);
+        {
+            std::lock_guard<std::mutex> g(g_autotune_lock);
+            auto it = g_autotune_cache.find(key);
+            if (it != g_autotune_cache.end() && line_solve_variant_ok(it->second, D)) {
+                D.solve_variant = it->second;
+                if (log) std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d cached variant %d\n", d, D.n, it->second);
+                continue;
+            }
+        }
+        float best = 1e30f, best_tw = 1e30f;
+        int best_v = SOLVE_STAGED_1, best_twv = SOLVE_TWISTED;
         for (int v = 0; v < SOLVE_NVARIANTS; ++v) {
             if (!line_solve_variant_ok(v, D)) continue;
             D.solve_variant = v;
+            cudaGetLastError();
             cudaError_t e = launch_line_solve(c->ping, D, L, 0, c->stream);  // warm-up
-            if (e != cudaSuccess) continue;
-            cudaEventRecord(a, c->stream);
-            for (int r = 0; r < 3; ++r) launch_line_solve(c->ping, D, L, 0, c->stream);
-            cudaEventRecord(b, c->stream);
-            if (cudaEventSynchronize(b) != cudaSuccess) {
-                rc = fail_cuda(cudaGetLastError(), "autotune");
-                break;
-            }
+            if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
+            for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_line_solve(c->ping, D, L, 0, c->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
             float ms = 0.f;
-            cudaEventElapsedTime(&ms, a, b);
-            if (ms < best) {
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (e != cudaSuccess) {
+                if (log)
+                    std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d variant %d dropped: %s\n", d, D.n, v,
+                                 cudaGetErrorString(e));
+                cudaGetLastError();
+                // an error that persists (the context is unusable) ends set-up
+                const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+                if (e2 != cudaSuccess) {
+                    rc = fail_cuda(e2, "autotune");
+                    break;
+                }
+                continue;
+            }
+            if (log) std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d variant %d %.2f us\n", d, D.n, v, ms * 1000.f / 3);
+            if (solve_variant_twisted(v)) {
+                if (ms < best_tw) {
+                    best_tw = ms;
+                    best_twv = v;
+                }
+            } else if (ms < best) {
                 best = ms;
                 best_v = v;
             }
         }
+        // the two-ended sweep rounds differently from the LAPACK-order ones:
+        // take it only for a clear gain, so that the choice does not flip
+        // between runs on timing noise
+        if (best_tw < 0.9f * best) best_v = best_twv;
         D.solve_variant = best_v;
+        std::lock_guard<std::mutex> g(g_autotune_lock);
+        g_autotune_cache[key] = best_v;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
@@ -401,6 +661,8 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         D.fwd_fast = t.fwd_fast;
         D.bwd_fast = t.bwd_fast;
         for (int v : t.uext) c->uext_sum[d] += v;
+        twisted_tables tw;
+        const bool have_tw = make_twisted_tables(h.n, h.kl, h.ku, h.ldab, h.lu, h.ipiv, tw) == 0;
         const std::vector<double> m = row_band(h, 0);
         const std::vector<double> k = row_band(h, 1);
         const size_t nb = static_cast<size_t>(h.elements) * h.quad_order * 2 * (h.p + 1);
@@ -434,6 +696,13 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
             }
         int* erange = nullptr;
         if (e == cudaSuccess) e = A.upload(&erange, er.data(), er.size(), s);
+        double *tw_l = nullptr, *tw_u = nullptr, *tw_r = nullptr, *tw_g = nullptr;
+        if (have_tw) {
+            if (e == cudaSuccess) e = A.upload(&tw_l, tw.lmul.data(), tw.lmul.size(), s);
+            if (e == cudaSuccess) e = A.upload(&tw_u, tw.ucol.data(), tw.ucol.size(), s);
+            if (e == cudaSuccess) e = A.upload(&tw_r, tw.rdiag.data(), tw.rdiag.size(), s);
+            if (e == cudaSuccess) e = A.upload(&tw_g, tw.g.data(), tw.g.size(), s);
+        }
         if (h.xq) c->xq[d].assign(h.xq, h.xq + static_cast<size_t>(h.elements) * h.quad_order);
         // the host staging vectors above die at the end of this iteration
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -450,6 +719,16 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         D.jac = jac;
         D.first = first;
         D.erange = erange;
+        if (have_tw) {
+            D.tw_k = tw.k;
+            D.tw_n1 = tw.n1;
+            D.tw_n2 = tw.n2;
+            D.tw_rows = tw.rows;
+            D.tw_lmul = tw_l;
+            D.tw_ucol = tw_u;
+            D.tw_rdiag = tw_r;
+            D.tw_g = tw_g;
+        }
     }
     const int nscratch = ndim == 3 ? 4 : (ndim == 2 ? 2 : 0);
     for (int i = 0; i < nscratch; ++i)
@@ -467,6 +746,7 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
 int adsg_ctx_destroy(adsg_ctx* ctx) {
     if (!ctx) return 0;
     cudaStreamSynchronize(ctx->stream);
+    detach_adjoints(ctx);
     delete ctx;
     return 0;
 }
@@ -676,7 +956,7 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
 // default) and each segment is recomputed once during the backward sweep.
 // ---------------------------------------------------------------------------
 struct adsg_adjoint {
-    adsg_ctx* ctx = nullptr;
+    adsg_ctx* ctx = nullptr;  // null once the context is destroyed
     int nsteps = 0, every = 1, nck = 0;
     double dt = 0.0;
     bool forward_done = false;
@@ -688,6 +968,17 @@ struct adsg_adjoint {
     double* scalar = nullptr;
     dev_arena arena;
 };
+
+extern "C++" {
+namespace adsg {
+
+void detach_adjoints(adsg_ctx* c) {
+    for (adsg_adjoint* a : c->adjoints) a->ctx = nullptr;
+    c->adjoints.clear();
+}
+
+}  // namespace adsg
+}
 
 namespace {
 
@@ -734,13 +1025,19 @@ int adsg_adjoint_create(adsg_ctx* ctx, int nsteps, double dt, int checkpoint_eve
         delete a;
         return fail_cuda(e, "adjoint allocation");
     }
+    ctx->adjoints.push_back(a);
     *out = a;
     return 0;
 }
 
 int adsg_adjoint_destroy(adsg_adjoint* a) {
-    if (a && a->ctx) cudaStreamSynchronize(a->ctx->stream);
-    delete a;
+    if (!a) return 0;
+    if (a->ctx) {
+        cudaStreamSynchronize(a->ctx->stream);
+        auto& v = a->ctx->adjoints;
+        v.erase(std::remove(v.begin(), v.end(), a), v.end());
+    }
+    delete a;  // freeing device memory waits for the device
     return 0;
 }
 
@@ -756,6 +1053,7 @@ int adsg_adjoint_forward(adsg_adjoint* a, const double* u0_dev, const double* ka
     if (!u0_dev) return fail(-2, "u0 is NULL");
     if (!kappa_dev) return fail(-3, "kappa is NULL");
     if (!uT_dev) return fail(-4, "uT is NULL");
+    if (!a->ctx) return fail(-1, "the adjoint's context was destroyed");
     adsg_ctx* c = a->ctx;
     const size_t bytes = sizeof(double) * c->size;
     cudaStream_t s = c->stream;
@@ -785,6 +1083,7 @@ int adsg_adjoint_backward(adsg_adjoint* a, const double* dL_duT_dev, double* gra
     if (!grad_u0_dev) return fail(-3, "grad_u0 is NULL");
     if (!grad_kappa_dev) return fail(-4, "grad_kappa is NULL");
     if (!a->forward_done) return fail(-1, "adsg_adjoint_forward must run first");
+    if (!a->ctx) return fail(-1, "the adjoint's context was destroyed");
     adsg_ctx* c = a->ctx;
     const size_t n = static_cast<size_t>(c->size);
     const size_t bytes = sizeof(double) * n;

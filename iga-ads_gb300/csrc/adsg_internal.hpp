@@ -38,11 +38,26 @@ struct solve_tables {
     int fwd_fast = 0, bwd_fast = 0;
 };
 
+// Twisted (two-ended) factorisation of a band matrix with kl == ku == k:
+// rows [0, n1) are eliminated top-down, rows [n1, n) bottom-up, and the 2k
+// unknowns where the chains meet come from a dense 2k x 2k inverse.  Tables
+// are laid out as dim_dev's tw_* members (see make_twisted_tables).
+struct twisted_tables {
+    int k = 0, n1 = 0, n2 = 0, rows = 0;
+    std::vector<double> lmul, ucol, rdiag, g;
+};
+
 // Row-format band [n][2p+1] of sum_e sum_q B_a B_b w_q J_e (which: 0 values, 1 derivatives).
 std::vector<double> row_band(const adsg_dim_desc& d, int which);
 bool valid_desc(const adsg_dim_desc& d);
 // 0 on success, else the 1-based column of a zero diagonal.
 int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t);
+
+// Builds the twisted tables of the matrix whose dgbtrf factors (ab, ipiv) are
+// given.  Returns 0 when built; non-zero when the band is not symmetric in
+// shape, too short, or the unpivoted elimination is not accurate enough
+// (the LAPACK-order sweeps are used then).
+int make_twisted_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, twisted_tables& t);
 
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const char* msg);

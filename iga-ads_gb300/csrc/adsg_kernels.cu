@@ -598,6 +598,234 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
     sweep_global<KL, KU, UNR>(x, L.elem_stride, D);
 }
 
+// ---------------------------------------------------------------------------
+// Twisted line solve.  Each line is split at n1 = n/2: lanes 0-15 of a warp
+// sweep rows [0, n1) of 16 lines top-down, lanes 16-31 rows [n1, n) of the
+// same lines bottom-up, each with its own unpivoted factors (the same band,
+// eliminated from its end).  Where the chains meet, the k last forward
+// results of both (exchanged by one shuffle) give the 2k unknowns
+// x[n1-k .. n1+k) through a precomputed 2k x 2k inverse; each chain then
+// back-substitutes outward from there.  Same FP64 work per row as the
+// LAPACK-order sweep, twice the independent chains per line.
+// ---------------------------------------------------------------------------
+template <int K, int UNR>
+__device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long long es, const int nc,
+                                              const double* __restrict__ lmul, const double* __restrict__ ucol,
+                                              const double* __restrict__ rdiag, const double* __restrict__ G,
+                                              const unsigned mask) {
+    auto ld = [&](int r) -> double {
+        if (r < 0 || r >= nc) return 0.0;
+        return x[r * es];
+    };
+    // ---- forward (unit lower factor, no row exchanges) ----
+    double f[K + 1];
+#pragma unroll
+    for (int t = 0; t <= K; ++t) f[t] = ld(t);
+    int j = 0;
+    {
+        double pre[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) pre[u] = ld(K + 1 + u);
+        const double* lp = lmul;
+        double lnx[UNR * K];
+#pragma unroll
+        for (int q = 0; q < UNR * K; ++q) lnx[q] = __ldg(lp + q);
+        for (; j + UNR <= nc; j += UNR) {
+            double inc[UNR], lc[UNR * K];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) inc[u] = pre[u];
+#pragma unroll
+            for (int q = 0; q < UNR * K; ++q) lc[q] = lnx[q];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) pre[u] = ld(j + UNR + K + 1 + u);
+            lp += UNR * K;  // tables carry 16 rows of zero padding past the chain
+#pragma unroll
+            for (int q = 0; q < UNR * K; ++q) lnx[q] = __ldg(lp + q);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                x[(j + u) * es] = f[0];
+                const double ny = -f[0];
+#pragma unroll
+                for (int t = 1; t <= K; ++t) f[t] = fma(ny, lc[u * K + t - 1], f[t]);
+#pragma unroll
+                for (int t = 0; t < K; ++t) f[t] = f[t + 1];
+                f[K] = inc[u];
+            }
+        }
+    }
+    for (; j < nc; ++j) {
+        const double incoming = ld(j + K + 1);
+        x[j * es] = f[0];
+        const double ny = -f[0];
+#pragma unroll
+        for (int t = 1; t <= K; ++t) f[t] = fma(ny, __ldg(lmul + static_cast<long long>(j) * K + t - 1), f[t]);
+#pragma unroll
+        for (int t = 0; t < K; ++t) f[t] = f[t + 1];
+        f[K] = incoming;
+    }
+    // ---- meeting point ----
+    double own[K], oth[K], z[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) own[i] = x[(nc - K + i) * es];
+#pragma unroll
+    for (int i = 0; i < K; ++i) oth[i] = __shfl_xor_sync(mask, own[i], 16);
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        double acc = 0.0;
+#pragma unroll
+        for (int i = 0; i < K; ++i) acc = fma(__ldg(G + a * 2 * K + i), own[i], acc);
+#pragma unroll
+        for (int i = 0; i < K; ++i) acc = fma(__ldg(G + a * 2 * K + K + i), oth[i], acc);
+        z[a] = acc;
+    }
+    // ---- backward (upper factor, bandwidth K), columns nc-1 .. 0 ----
+    double b[K + 1];
+#pragma unroll
+    for (int d = 0; d <= K; ++d) b[d] = ld(nc - 1 - d);
+    int c = nc - 1;
+#pragma unroll
+    for (int a = K - 1; a >= 0; --a, --c) {  // the chain's K interface rows
+        const double v = z[a];
+        x[c * es] = v;
+        const double nv = -v;
+#pragma unroll
+        for (int d = 1; d <= K; ++d) b[d] = fma(nv, __ldg(ucol + static_cast<long long>(c) * K + d - 1), b[d]);
+#pragma unroll
+        for (int d = 0; d < K; ++d) b[d] = b[d + 1];
+        b[K] = ld(c - K - 1);
+    }
+    {
+        double pre[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) pre[u] = ld(c - K - 1 - u);
+        double rnx[UNR], unx[UNR * K];
+        auto load_block = [&](int jj, double* r, double* uu) {
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const int cc = max(jj - u, 0);
+                r[u] = __ldg(rdiag + cc);
+#pragma unroll
+                for (int d = 0; d < K; ++d) uu[u * K + d] = __ldg(ucol + static_cast<long long>(cc) * K + d);
+            }
+        };
+        load_block(c, rnx, unx);
+        for (; c - UNR + 1 >= 0; c -= UNR) {
+            double inc[UNR], rc[UNR], uc[UNR * K];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                inc[u] = pre[u];
+                rc[u] = rnx[u];
+            }
+#pragma unroll
+            for (int q = 0; q < UNR * K; ++q) uc[q] = unx[q];
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) pre[u] = ld(c - UNR - K - 1 - u);
+            load_block(c - UNR, rnx, unx);
+#pragma unroll
+            for (int u = 0; u < UNR; ++u) {
+                const double v = b[0] * rc[u];
+                x[(c - u) * es] = v;
+                const double nv = -v;
+#pragma unroll
+                for (int d = 1; d <= K; ++d) b[d] = fma(nv, uc[u * K + d - 1], b[d]);
+#pragma unroll
+                for (int d = 0; d < K; ++d) b[d] = b[d + 1];
+                b[K] = inc[u];
+            }
+        }
+    }
+    for (; c >= 0; --c) {
+        const double incoming = ld(c - K - 1);
+        const double v = b[0] * __ldg(rdiag + c);
+        x[c * es] = v;
+        const double nv = -v;
+#pragma unroll
+        for (int d = 1; d <= K; ++d) b[d] = fma(nv, __ldg(ucol + static_cast<long long>(c) * K + d - 1), b[d]);
+#pragma unroll
+        for (int d = 0; d < K; ++d) b[d] = b[d + 1];
+        b[K] = incoming;
+    }
+}
+
+template <int K, int UNR>
+__global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restrict__ data, dim_dev D, line_layout L) {
+    const int lane = threadIdx.x & 31, chain = lane >> 4;
+    const long long g = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 16 + (lane & 15);
+    const bool active = g < L.nlines;
+    const unsigned mask = __ballot_sync(0xffffffffu, active);  // lanes g and g^16 share a line
+    if (!active) return;
+    double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    const long long es = L.elem_stride;
+    const long long off = static_cast<long long>(chain) * D.tw_rows;
+    if (chain) x += static_cast<long long>(D.n - 1) * es;
+    twisted_chain<K, UNR>(x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
+                          D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
+}
+
+// The same sweep for contiguous lines (the x direction), where a lane walking
+// its own line would touch a different cache line per lane and row: each
+// warp first copies its 16 lines (16 n consecutive doubles) into a shared
+// tile with coalesced loads, sweeps there, and copies the tile back.  The
+// tile pitch is odd so that the 16 lines of one row fall in distinct banks.
+__host__ __device__ inline int twisted_pitch(int n) { return n | 1; }
+
+template <int K, int UNR>
+__global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* __restrict__ data, dim_dev D,
+                                                                        line_layout L) {
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4;
+    const int n = D.n, pitch = twisted_pitch(n);
+    const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
+    if (g0 >= L.nlines) return;  // whole warp
+    const int nv = static_cast<int>(min(16LL, L.nlines - g0));
+    double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
+    const double* src = data + g0 * n;
+    const int count = nv * n;
+    for (int e = lane; e < count; e += 32) {
+        const int line = e / n;
+        tile[line * pitch + (e - line * n)] = src[e];
+    }
+    __syncwarp();
+    const int line = lane & 15;
+    const bool active = line < nv;
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (active) {
+        double* x = tile + line * pitch + (chain ? n - 1 : 0);
+        const long long off = static_cast<long long>(chain) * D.tw_rows;
+        twisted_chain<K, UNR>(x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
+                              D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
+    }
+    __syncwarp();
+    double* dst = data + g0 * n;
+    for (int e = lane; e < count; e += 32) {
+        const int ln = e / n;
+        dst[e] = tile[ln * pitch + (e - ln * n)];
+    }
+}
+
+size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
+
+template <int K>
+static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, bool staged, cudaStream_t s) {
+    constexpr int UNR = K > 2 ? 4 : 8;
+    if (staged && L.contiguous) {
+        const size_t per_warp = twisted_staged_smem_per_warp(d.n);
+        const int wpb = per_warp * 4 <= 227 * 1024 ? 4 : (per_warp * 2 <= 227 * 1024 ? 2 : 1);
+        const size_t smem = per_warp * wpb;
+        if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+        if (smem > 48 * 1024) {
+            cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(line_solve_twisted_staged_kernel<K, UNR>), smem);
+            if (e != cudaSuccess) return e;
+        }
+        const long long per = 16LL * wpb;
+        line_solve_twisted_staged_kernel<K, UNR><<<(L.nlines + per - 1) / per, 32 * wpb, smem, s>>>(data, d, L);
+        return cudaGetLastError();
+    }
+    const long long per = 64;  // 4 warps x 16 lines
+    line_solve_twisted_kernel<K, UNR><<<(L.nlines + per - 1) / per, 128, 0, s>>>(data, d, L);
+    return cudaGetLastError();
+}
+
 template <int KL, int KU>
 static cudaError_t line_solve_t(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {
     const size_t smem = line_solve_smem_per_warp(d.n);
@@ -661,6 +889,9 @@ static cudaError_t line_solve_variant(int variant, double* data, const dim_dev& 
 }
 
 bool line_solve_variant_ok(int variant, const dim_dev& d) {
+    if (variant == SOLVE_TWISTED) return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr;
+    if (variant == SOLVE_TWISTED_STAGED)
+        return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr && twisted_staged_smem_per_warp(d.n) <= 227 * 1024;
     const int kl = d.kl, ku = d.ku_regular, w = d.w;
     const bool reg = (kl == 1 && ku <= 2 && w <= 3 && w >= 1) || (kl == 2 && ku <= 2 && w <= 4 && w >= 2) ||
                      (kl == 3 && ku <= 3 && w <= 6 && w >= 3) || (kl == 4 && ku <= 4 && w <= 8 && w >= 4);
@@ -677,7 +908,17 @@ cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout&
     // U extent (columns beyond it take the wide-column branch)
     const int kl = d.kl, ku = d.ku_regular, w = d.w;
     const int v = trans ? SOLVE_STAGED_1 : d.solve_variant;
-    if (!trans && v != SOLVE_STAGED_1 && line_solve_variant_ok(v, d)) {
+    if (!trans && (v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED) && line_solve_variant_ok(v, d)) {
+        const bool staged = v == SOLVE_TWISTED_STAGED;
+        switch (d.tw_k) {
+            case 1: return twisted_t<1>(data, d, L, staged, s);
+            case 2: return twisted_t<2>(data, d, L, staged, s);
+            case 3: return twisted_t<3>(data, d, L, staged, s);
+            default: return twisted_t<4>(data, d, L, staged, s);
+        }
+    }
+    if (!trans && v != SOLVE_STAGED_1 && v != SOLVE_TWISTED && v != SOLVE_TWISTED_STAGED &&
+        line_solve_variant_ok(v, d)) {
         if (kl == 1 && ku <= 1 && w <= 2) return line_solve_variant<1, 1>(v, data, d, L, s);
         if (kl == 1 && ku <= 2 && w <= 3) return line_solve_variant<1, 2>(v, data, d, L, s);
         if (kl == 2) return line_solve_variant<2, 2>(v, data, d, L, s);

@@ -9,7 +9,20 @@ namespace adsg {
 // Per-dimension device tables.  Band rows hold the 2p+1 coefficients of row r
 // for columns r-p .. r+p (zero outside the matrix).
 // Line-solve kernel variants chosen per direction by the context's autotuner.
-enum solve_variant_id { SOLVE_STAGED_1 = 0, SOLVE_STAGED_2 = 1, SOLVE_STAGED_4 = 2, SOLVE_GLOBAL_4 = 3, SOLVE_NVARIANTS = 4 };
+// SOLVE_TWISTED* sweep each line from both ends (a two-chain factorisation of
+// the same band; the staged form copies contiguous lines through shared
+// memory and equals the plain form on strided lines); the others follow
+// LAPACK dgbtrs's column order and give bitwise equal results.
+enum solve_variant_id {
+    SOLVE_STAGED_1 = 0,
+    SOLVE_STAGED_2 = 1,
+    SOLVE_STAGED_4 = 2,
+    SOLVE_GLOBAL_4 = 3,
+    SOLVE_TWISTED = 4,
+    SOLVE_TWISTED_STAGED = 5,
+    SOLVE_NVARIANTS = 6
+};
+inline bool solve_variant_twisted(int v) { return v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED; }
 
 struct dim_dev {
     int n = 0, p = 0, kl = 0, w = 0;  // w = kl + ku: widest upper extent of U
@@ -32,6 +45,13 @@ struct dim_dev {
     const double* jac = nullptr;    // [E]
     const int* first = nullptr;     // [E]
     const int* erange = nullptr;    // [n][2] first and last element supporting each dof
+    // Twisted factorisation (0 = not available): rows [0, tw_n1) form chain 0,
+    // rows [tw_n1, n) chain 1 in reverse order; tables per chain, stride tw_rows.
+    int tw_k = 0, tw_n1 = 0, tw_n2 = 0, tw_rows = 0;
+    const double* tw_lmul = nullptr;   // [2][tw_rows][k] multipliers of chain-local column j
+    const double* tw_ucol = nullptr;   // [2][tw_rows][k] U(j-d, j), d = 1..k
+    const double* tw_rdiag = nullptr;  // [2][tw_rows] 1 / U(j, j)
+    const double* tw_g = nullptr;      // [2][k][2k] interface rows: own tail, then the other chain's tail
 };
 
 // Where the grid lines of one direction sit in a tensor of extents n[0..2]

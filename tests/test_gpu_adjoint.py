@@ -117,3 +117,17 @@ def test_torch_autograd_bridge(cuda):
     assert abs(float(loss) - loss_ref) <= 1e-14 * abs(loss_ref)
     np.testing.assert_array_equal(u0.grad.cpu().numpy(), gu_ref)
     np.testing.assert_array_equal(kappa.grad.cpu().numpy(), gk_ref)
+
+
+def test_adjoint_outliving_its_context_fails_cleanly(cuda):
+    """Destroying the context first detaches its adjoints: their calls then
+    report an error and their destruction stays safe (as happens when a
+    garbage collector finalises both in arbitrary order)."""
+    import torch
+
+    ctx, adj, _, dev = _setup((2, 2), (6, 5), 4, 1e-3)
+    ctx.close()
+    uT = torch.empty_like(dev["u0"])
+    with pytest.raises(RuntimeError, match="context was destroyed"):
+        adj.forward(dev["u0"], dev["kappa"], uT)
+    adj.close()

@@ -31,13 +31,15 @@ def test_batch_against_oracle_and_loop(cuda):
     for i, (nd, p, e, dt) in enumerate(SMALL):
         ref = oracle.Problem([p] * nd, [e] * nd).heat_steps(u0[i], dt, 3)
         assert oracle.rel_l2(got[i], ref) <= 3 * step_tol([_cond(p, e)] * nd), (i, SMALL[i])
-    # the same three steps through the plain per-instance kernels
+    # the same three steps through the plain per-instance kernels (their
+    # autotuned solves may use the two-ended sweep, which rounds differently
+    # from the batched kernel's LAPACK-order sweep)
     for i, u in enumerate(u0):
         b.set_state(i, u)
     b.steps_looped(3)
     b.synchronize()
-    for i in range(len(SMALL)):
-        assert oracle.rel_l2(b.get_state(i), got[i]) <= 1e-14
+    for i, (nd, p, e, dt) in enumerate(SMALL):
+        assert oracle.rel_l2(b.get_state(i), got[i]) <= 3 * step_tol([_cond(p, e)] * nd), (i, SMALL[i])
 
 
 def test_batch_repeated_calls_and_parity(cuda):
@@ -71,8 +73,10 @@ def test_mixed_64_batch_matches_plain_kernels(cuda):
         b.set_state(i, u)
     b.steps_looped(2)
     b.synchronize()
-    for i in range(64):
-        assert oracle.rel_l2(b.get_state(i), got[i]) <= 1e-13, specs[i]
+    # the per-instance contexts may solve with the two-ended sweep, which
+    # rounds differently from the batched kernel's LAPACK-order sweep
+    for i, (nd, p, e, dt) in enumerate(specs):
+        assert oracle.rel_l2(b.get_state(i), got[i]) <= 2 * step_tol([_cond(p, e)] * nd), specs[i]
 
 
 def test_batch_rejects_bad_specs():

@@ -140,4 +140,5 @@ def test_generalised_random_against_oracle(special, cuda):
         lu, piv = std[d]
         for idx in np.ndindex(b.shape[:-1]):
             b[idx] = oracle.dgbtrs("N", n[d], kl, ku, 1, lu, ldab, piv, b[idx].copy(), n[d])
-    assert oracle.rel_l2(got, t.ravel()) <= 1e-13
+    # the shared directions may use the two-ended sweep (rounding differs from dgbtrs)
+    assert oracle.rel_l2(got, t.ravel()) <= 1e-12

@@ -279,7 +279,7 @@ def test_full_size_against_oracle_one_step_sampled(big):
     assert oracle.rel_l2(got, ref) <= step_tol(_conds(dims))
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("p,elements", [
     ((2, 2, 2), (30, 7, 9)),
     ((4, 4, 4), (12, 9, 6)),
@@ -289,7 +289,8 @@ def test_full_size_against_oracle_one_step_sampled(big):
 ])
 def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypatch):
     """The autotuner's candidates (staged 1/2/4 tiles per block, in-place
-    global sweep) each match the oracle's dgbtrs-based ADS solve."""
+    global sweep, two-ended twisted sweep in global memory or staged through
+    shared memory) each match the oracle's dgbtrs-based ADS solve."""
     monkeypatch.setenv("ADSG_SOLVE_VARIANT", str(variant))
     dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
     ctx = ads.Context(dims)
@@ -303,9 +304,12 @@ def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypa
     ctx.heat_steps_host(s, 1e-5, 2)
     assert oracle.rel_l2(s, pr.heat_steps(u, 1e-5, 2)) <= step_tol(_conds(dims)) * 2
     chosen = ctx.solve_variants()
-    assert all(0 <= v <= 3 for v in chosen)
+    assert all(0 <= v <= 5 for v in chosen)
     if variant in (0, 3):  # always applicable for p <= 4
         assert chosen == [variant] * len(p)
+    if variant in (4, 5):  # the twisted sweeps need n >= 4p + 2 along the direction
+        for d, v in zip(dims, chosen):
+            assert (v == variant) == (d.dofs() >= 4 * d.p + 2)
 
 
 def test_failure_detection_counts_nonfinite(cuda):
