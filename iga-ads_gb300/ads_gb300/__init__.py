@@ -94,6 +94,7 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_stage_times": (i, [vp, _c_double_p, ctypes.POINTER(ctypes.c_longlong)]),
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
+        "adsg_ctx_launch_pdl": (i, [vp]),
         "adsg_quad_size": (ll, [vp]),
         "adsg_count_nonfinite": (i, [vp, vp, ctypes.POINTER(ll)]),
         "adsg_load_vector": (i, [vp, vp, vp]),
@@ -291,6 +292,10 @@ class Context:
         v = np.zeros(3, np.int32)
         _check(library().adsg_ctx_solve_variants(self._h, _iptr(v)))
         return [int(x) for x in v[: len(self.dims)]]
+
+    def launch_pdl(self) -> bool:
+        """Whether the step's kernels use programmatic dependent launch."""
+        return library().adsg_ctx_launch_pdl(self._h) == 1
 
     def stage_work(self) -> dict:
         """{stage: (fp64_flops, hbm_bytes)} of one launch of each stage."""

@@ -370,6 +370,7 @@ struct adsg_ctx {
     long long stage_launches[ADSG_NSTAGES] = {};
     // adjoints created on this context (detached when the context goes first)
     std::vector<adsg_adjoint*> adjoints;
+    int pdl = 0;  // programmatic dependent launch for the step kernels (chosen at creation)
 
     cudaEvent_t take_event() {
         if (!spare.empty()) {
@@ -443,6 +444,7 @@ int ensure_dt_bands(adsg_ctx* c, double dt) {
 // rhs = (M(x)M(x)M - dt (K(x)M(x)M + M(x)K(x)M + M(x)M(x)K)) u_prev as a sequence of
 // band passes along z, y, x (3D), y, x (2D) or x (1D).
 int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) {
+    pdl_scope pdl(c->pdl);
     int st = ensure_dt_bands(c, dt);
     if (st) return st;
     const long long total = c->size;
@@ -488,6 +490,7 @@ int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) {
 }
 
 int enqueue_solve(adsg_ctx* c, double* x, int trans) {
+    pdl_scope pdl(c->pdl);
     for (int d = 0; d < c->ndim; ++d) {
         line_layout L = make_line_layout(c->n, c->ndim, d);
         stage_scope sc(c, ADSG_STAGE_SOLVE_X + d);
@@ -598,6 +601,55 @@ int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     int st = enqueue_rhs(c, prev, next, dt);
     if (st) return st;
     return enqueue_solve(c, next, 0);
+}
+
+// Launch-mode tuner: time a few explicit steps with and without programmatic
+// dependent launch and keep the faster (results are the same either way).
+// ADSG_PDL=0/1 forces the mode.
+int autotune_launch_mode(adsg_ctx* c) {
+    const char* force = std::getenv("ADSG_PDL");
+    if (force && (*force == '0' || *force == '1')) {
+        c->pdl = *force == '1';
+        return 0;
+    }
+    double* tmp = nullptr;
+    if (cudaMalloc(&tmp, sizeof(double) * c->size) != cudaSuccess) {  // no room: keep plain launches
+        cudaGetLastError();
+        c->pdl = 0;
+        return 0;
+    }
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    float best = 1e30f;
+    int best_mode = 0, rc = 0;
+    const int reps = 4;
+    for (int mode = 0; mode < 2 && e == cudaSuccess && rc == 0; ++mode) {
+        c->pdl = mode;
+        rc = enqueue_step(c, c->ping, tmp, 1e-6);  // warm-up (also builds the dt bands)
+        if (rc == 0) e = cudaEventRecord(a, c->stream);
+        for (int r = 0; r < reps && rc == 0 && e == cudaSuccess; ++r) {
+            rc = enqueue_step(c, c->ping, tmp, 1e-6);
+            if (rc == 0) rc = enqueue_step(c, tmp, c->ping, 1e-6);
+        }
+        if (rc == 0 && e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+        if (rc == 0 && e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (rc == 0 && e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        if (rc == 0 && e == cudaSuccess && ms < best) {
+            best = ms;
+            best_mode = mode;
+        }
+    }
+    c->pdl = best_mode;
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaFree(tmp);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail_cuda(e, "launch-mode tuner");
+    // the tuner ran on the context's own (zeroed) state buffer; leave it zero
+    ADSG_CUDA_TRY(cudaMemsetAsync(c->ping, 0, sizeof(double) * c->size, c->stream), "launch-mode tuner");
+    return 0;
 }
 
 }  // namespace
@@ -736,6 +788,10 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
     if ((e = c->arena.alloc(&c->ping, c->size)) != cudaSuccess) return bail(e, "state alloc");
     if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return bail(e, "set-up copies");
     if (int st = autotune_solves(c)) {
+        delete c;
+        return st;
+    }
+    if (int st = autotune_launch_mode(c)) {
         delete c;
         return st;
     }
@@ -886,6 +942,8 @@ int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants) {
     for (int d = 0; d < 3; ++d) variants[d] = d < ctx->ndim ? ctx->dims[d].solve_variant : -1;
     return 0;
 }
+
+int adsg_ctx_launch_pdl(const adsg_ctx* ctx) { return ctx ? ctx->pdl : -1; }
 
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
     if (!ctx) return fail(-1, "ctx is NULL");

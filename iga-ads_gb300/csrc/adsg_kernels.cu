@@ -10,12 +10,54 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
 #include "adsg_kernels.cuh"
 
 namespace adsg {
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch.  The step's kernels are launched with
+// programmatic stream serialisation: the next kernel on the stream may be
+// scheduled once every block of the current one has started, and waits in
+// griddepcontrol.wait (before its first global memory access) until the
+// current kernel has completed and its writes are visible.  This hides the
+// launch latency between the six kernels of a step behind the last wave of
+// the previous one.  Without the attribute both instructions are no-ops.
+// Whether the attribute is set is chosen per context (set_launch_pdl): it
+// pays on small, launch-bound grids, while on large ones the early-placed
+// blocks of a one-wave solve kernel can land unevenly across the SMs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait_and_release() {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+static thread_local int t_pdl_mode = 0;  // set per context around its launches
+
+void set_launch_pdl(int on) { t_pdl_mode = on ? 1 : 0; }
+int launch_pdl_mode() { return t_pdl_mode; }
+
+static bool pdl_enabled() { return t_pdl_mode == 1; }
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------
 // Band pass: one output per thread, 2p+1 neighbours along one axis.
@@ -35,6 +77,7 @@ __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict
     constexpr int BW = 2 * P + 1;
     long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (g >= total) return;
+    pdl_wait_and_release();
     const int r = static_cast<int>((g / stride) % n_axis);
     const double* a0 = A0 + static_cast<long long>(r) * BW;
     const double* a1 = IN1 ? A1 + static_cast<long long>(r) * BW : nullptr;
@@ -60,16 +103,18 @@ static cudaError_t band_pass_p(const double* in0, const double* in1, double* out
                                const double* A0, const double* A1, const double* B0, int n_axis,
                                long long stride, long long total, cudaStream_t s) {
     const int threads = 256;
-    const long long blocks = (total + threads - 1) / threads;
+    const dim3 grid(static_cast<unsigned>((total + threads - 1) / threads));
     if (in1 && out1)
-        band_pass_kernel<P, true, true><<<blocks, threads, 0, s>>>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total);
-    else if (in1)
-        band_pass_kernel<P, true, false><<<blocks, threads, 0, s>>>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total);
-    else if (out1)
-        band_pass_kernel<P, false, true><<<blocks, threads, 0, s>>>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total);
-    else
-        band_pass_kernel<P, false, false><<<blocks, threads, 0, s>>>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total);
-    return cudaGetLastError();
+        return launch_pdl(band_pass_kernel<P, true, true>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
+                          n_axis, stride, total);
+    if (in1)
+        return launch_pdl(band_pass_kernel<P, true, false>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
+                          n_axis, stride, total);
+    if (out1)
+        return launch_pdl(band_pass_kernel<P, false, true>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
+                          n_axis, stride, total);
+    return launch_pdl(band_pass_kernel<P, false, false>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
+                      n_axis, stride, total);
 }
 
 cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double* out0, double* out1,
@@ -419,6 +464,7 @@ __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ dat
     const int lane = threadIdx.x & 31;
     const long long line0 = static_cast<long long>(blockIdx.x) * 32;
     if (line0 >= L.nlines) return;
+    pdl_wait_and_release();
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
     double* s = smem + kPadLo * kPitch;
     for (int r = 0; r < kPadLo; ++r) smem[r * kPitch + lane] = 0.0;
@@ -594,6 +640,7 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
     const int lane = threadIdx.x & 31;
     const long long g = static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) * 32 + (threadIdx.x >> 5) * 32 + lane;
     if (g >= L.nlines) return;
+    pdl_wait_and_release();
     double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
     sweep_global<KL, KU, UNR>(x, L.elem_stride, D);
 }
@@ -754,6 +801,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restr
     const bool active = g < L.nlines;
     const unsigned mask = __ballot_sync(0xffffffffu, active);  // lanes g and g^16 share a line
     if (!active) return;
+    pdl_wait_and_release();
     double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
     const long long es = L.elem_stride;
     const long long off = static_cast<long long>(chain) * D.tw_rows;
@@ -777,6 +825,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
     const int n = D.n, pitch = twisted_pitch(n);
     const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
     if (g0 >= L.nlines) return;  // whole warp
+    pdl_wait_and_release();
     const int nv = static_cast<int>(min(16LL, L.nlines - g0));
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const double* src = data + g0 * n;
@@ -818,12 +867,12 @@ static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& 
             if (e != cudaSuccess) return e;
         }
         const long long per = 16LL * wpb;
-        line_solve_twisted_staged_kernel<K, UNR><<<(L.nlines + per - 1) / per, 32 * wpb, smem, s>>>(data, d, L);
-        return cudaGetLastError();
+        return launch_pdl(line_solve_twisted_staged_kernel<K, UNR>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
+                          dim3(32 * wpb), smem, s, data, d, L);
     }
     const long long per = 64;  // 4 warps x 16 lines
-    line_solve_twisted_kernel<K, UNR><<<(L.nlines + per - 1) / per, 128, 0, s>>>(data, d, L);
-    return cudaGetLastError();
+    return launch_pdl(line_solve_twisted_kernel<K, UNR>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
+                      dim3(128), 0, s, data, d, L);
 }
 
 template <int KL, int KU>
@@ -834,8 +883,8 @@ static cudaError_t line_solve_t(double* data, const dim_dev& d, const line_layou
         if (e != cudaSuccess) return e;
     }
     const long long blocks = (L.nlines + 31) / 32;
-    line_solve_kernel<KL, KU><<<blocks, 32, smem, s>>>(data, d, L, trans);
-    return cudaGetLastError();
+    return launch_pdl(line_solve_kernel<KL, KU>, dim3(static_cast<unsigned>(blocks)), dim3(32), smem, s, data, d, L,
+                      trans);
 }
 
 // staged kernel with several warps (one tile each) per block
@@ -845,6 +894,7 @@ __global__ void __launch_bounds__(32 * WPB) line_solve_staged_kernel(double* __r
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long line0 = (static_cast<long long>(blockIdx.x) * WPB + warp) * 32;
     if (line0 >= L.nlines) return;
+    pdl_wait_and_release();
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
     double* base = smem + static_cast<size_t>(warp) * (D.n + kPadLo + kPadHi) * kPitch;
     double* s = base + kPadLo * kPitch;
@@ -866,8 +916,8 @@ static cudaError_t staged_t(double* data, const dim_dev& d, const line_layout& L
         if (e != cudaSuccess) return e;
     }
     const long long per = 32LL * WPB;
-    line_solve_staged_kernel<KL, KU, WPB><<<(L.nlines + per - 1) / per, 32 * WPB, smem, s>>>(data, d, L);
-    return cudaGetLastError();
+    return launch_pdl(line_solve_staged_kernel<KL, KU, WPB>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
+                      dim3(32 * WPB), smem, s, data, d, L);
 }
 
 template <int KL, int KU>
@@ -882,8 +932,8 @@ static cudaError_t line_solve_variant(int variant, double* data, const dim_dev& 
         case SOLVE_GLOBAL_4:
         default: {
             const long long per = 128;
-            line_solve_global_kernel<KL, KU, (KL > 2 ? 4 : 8)><<<(L.nlines + per - 1) / per, 128, 0, s>>>(data, d, L);
-            return cudaGetLastError();
+            return launch_pdl(line_solve_global_kernel<KL, KU, (KL > 2 ? 4 : 8)>,
+                              dim3(static_cast<unsigned>((L.nlines + per - 1) / per)), dim3(128), 0, s, data, d, L);
         }
     }
 }

@@ -65,6 +65,16 @@ struct line_layout {
 
 line_layout make_line_layout(const int* n, int ndim, int d);
 
+// Programmatic dependent launch for the step kernels issued by the calling
+// thread (0 = off, 1 = on).
+void set_launch_pdl(int on);
+int launch_pdl_mode();
+struct pdl_scope {
+    int saved;
+    explicit pdl_scope(int on) : saved(launch_pdl_mode()) { set_launch_pdl(on); }
+    ~pdl_scope() { set_launch_pdl(saved); }
+};
+
 // Stacked solve tables of several factorised bands of one size (generalised ADS).
 struct line_tables {
     int n = 0, kl = 0, w = 0, nmat = 0;

@@ -152,9 +152,18 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
  * autotuner times each applicable variant on the context's own buffers):
  * 0 one 32-line tile per block staged in shared memory, 1 and 2 the same with
  * two / four tiles per block, 3 lines swept in place in global memory, four
- * warps per block.  variants has 3 entries (-1 for absent dimensions).  The
- * environment variable ADSG_SOLVE_VARIANT forces a variant where it applies. */
+ * warps per block (0-3 follow dgbtrs's operation order and agree bitwise);
+ * 4 the two-ended sweep (each line swept from both ends by two lanes, the
+ * meeting unknowns from a small dense inverse) in global memory, 5 the same
+ * with contiguous lines staged through shared memory.  variants has 3 entries
+ * (-1 for absent dimensions).  The environment variable ADSG_SOLVE_VARIANT
+ * forces a variant where it applies; ADSG_AUTOTUNE_LOG=1 prints the timings.
+ * Decisions are cached per shape for the process. */
 int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants);
+/* 1 when the step's kernels use programmatic dependent launch (chosen at
+ * creation by timing a few steps both ways; ADSG_PDL=0/1 forces it), 0 when
+ * not, -1 for a NULL context.  Results do not depend on it. */
+int adsg_ctx_launch_pdl(const adsg_ctx* ctx);
 
 /* ---- host-buffer entry points (the reference-facing boundary) ------------- */
 

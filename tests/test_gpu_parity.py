@@ -328,3 +328,22 @@ def test_failure_detection_counts_nonfinite(cuda):
     ctx.heat_steps(v, 1e-1, 400)  # far above the stability limit
     ctx.synchronize()
     assert ctx.count_nonfinite(v) > 0
+
+
+@pytest.mark.parametrize("p,elements", [((2, 2, 2), (20, 18, 16)), ((2, 2), (32, 32))])
+def test_launch_mode_does_not_change_results(p, elements, cuda, monkeypatch):
+    """Programmatic dependent launch only moves when the next kernel's blocks
+    are scheduled: the steps agree bitwise with and without it."""
+    out = []
+    for mode in ("0", "1"):
+        monkeypatch.setenv("ADSG_PDL", mode)
+        dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+        ctx = ads.Context(dims)
+        assert ctx.launch_pdl() == (mode == "1")
+        u = np.random.default_rng(3).uniform(-1, 1, ctx.size)
+        ctx.heat_steps_host(u, 1e-5, 5)
+        r = np.empty_like(u)
+        ctx.heat_rhs_host(u, r, 1e-5)
+        out.append((u, r))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
