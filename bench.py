@@ -296,8 +296,7 @@ def run_ours(args, cfg):
     ctx.set_stream(stream)  # the flush, the events and our kernels share one stream
 
     def step(prev, nxt):
-        ctx.heat_rhs(prev, nxt, dt)
-        ctx.ads_solve(nxt)
+        ctx.heat_step(prev, nxt, dt)  # heat_3d::step: compute_rhs, then ads_solve
 
     # warm-up
     bufs = [A, B]

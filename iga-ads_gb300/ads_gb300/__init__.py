@@ -86,6 +86,7 @@ def library() -> ctypes.CDLL:
         "adsg_heat_rhs_elem": (i, [vp, vp, vp, vp, d]),
         "adsg_ads_solve": (i, [vp, vp, vp]),
         "adsg_ads_solve_t": (i, [vp, vp]),
+        "adsg_heat_step": (i, [vp, vp, vp, d]),
         "adsg_heat_steps": (i, [vp, vp, d, i]),
         "adsg_heat_steps_host": (i, [vp, _c_double_p, d, i]),
         "adsg_ads_solve_host": (i, [vp, _c_double_p]),
@@ -316,6 +317,10 @@ class Context:
 
     def ads_solve_t(self, rhs) -> None:
         _check(library().adsg_ads_solve_t(self._h, _devptr(rhs)))
+
+    def heat_step(self, u_prev, u_next, dt: float) -> None:
+        """One explicit step u_next = M^-1 R u_prev (heat_3d::step)."""
+        _check(library().adsg_heat_step(self._h, _devptr(u_prev), _devptr(u_next), float(dt)))
 
     def heat_steps(self, u, dt: float, nsteps: int) -> None:
         _check(library().adsg_heat_steps(self._h, _devptr(u), float(dt), int(nsteps)))

@@ -142,6 +142,33 @@ void host_twisted_backward(const twisted_tables& t, int chain, double* x, long l
 
 }  // namespace
 
+void scale_twisted(const twisted_tables& t, int n, twisted_tables& o, std::vector<double>& scale) {
+    const int k = t.k, rows = t.rows;
+    o = t;
+    scale.assign(n, 1.0);
+    for (int chain = 0; chain < 2; ++chain) {
+        const int nc = chain ? t.n2 : t.n1;
+        const size_t off = static_cast<size_t>(chain) * rows;
+        const double* sc = t.rdiag.data() + off;  // 1 / U(i, i), chain-local row i
+        for (int i = 0; i < nc; ++i) scale[chain ? n - 1 - i : i] = sc[i];
+        for (int j = 0; j < nc; ++j)
+            for (int q = 1; q <= k; ++q) {
+                const size_t at = (off + j) * k + q - 1;
+                o.lmul[at] = j + q < nc ? sc[j + q] * t.lmul[at] / sc[j] : 0.0;
+                o.ucol[at] = j - q >= 0 ? t.ucol[at] * sc[j - q] : 0.0;
+            }
+        for (int i = 0; i < nc; ++i) o.rdiag[off + i] = 1.0;
+        const int no = chain ? t.n1 : t.n2;
+        const double* so = t.rdiag.data() + static_cast<size_t>(1 - chain) * rows;
+        double* g = o.g.data() + static_cast<size_t>(chain) * 2 * k * k;
+        for (int a = 0; a < k; ++a)
+            for (int i = 0; i < k; ++i) {
+                g[a * 2 * k + i] /= sc[nc - k + i];
+                g[a * 2 * k + k + i] /= so[no - k + i];
+            }
+    }
+}
+
 int make_twisted_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, twisted_tables& t) {
     const int k = kl;
     if (kl != ku || k < 1 || k > 4 || n < 4 * k + 2) return 1;
@@ -344,6 +371,15 @@ struct adsg_ctx {
     dim_dev dims[3];
     double* nrow[3] = {nullptr, nullptr, nullptr};
     double* kdt[3] = {nullptr, nullptr, nullptr};
+    // The explicit step's own view of each direction.  Where the direction is
+    // solved with a two-ended sweep, its band rows are pre-multiplied by
+    // 1 / U(r, r) of that sweep's factors and the solve tables are the unit-
+    // diagonal ones: the RHS passes deliver the row-scaled right-hand side at
+    // no extra cost and the backward sweeps drop their multiply.  Elsewhere
+    // sdims[d] equals dims[d].
+    dim_dev sdims[3];
+    double* snrow[3] = {nullptr, nullptr, nullptr};
+    double* skdt[3] = {nullptr, nullptr, nullptr};
     double band_dt = std::nan("");
     double* scratch[4] = {nullptr, nullptr, nullptr, nullptr};
     double* ping = nullptr;  // second state buffer of the step loop
@@ -436,6 +472,14 @@ int ensure_dt_bands(adsg_ctx* c, double dt) {
         ADSG_CUDA_TRY(launch_dt_bands(c->dims[d], dt, c->nrow[d], c->kdt[d], c->stream), "dt bands");
         c->dims[d].nrow = c->nrow[d];
         c->dims[d].kdt = c->kdt[d];
+        if (c->snrow[d]) {
+            ADSG_CUDA_TRY(launch_dt_bands(c->sdims[d], dt, c->snrow[d], c->skdt[d], c->stream), "dt bands");
+            c->sdims[d].nrow = c->snrow[d];
+            c->sdims[d].kdt = c->skdt[d];
+        } else {
+            c->sdims[d].nrow = c->nrow[d];
+            c->sdims[d].kdt = c->kdt[d];
+        }
     }
     c->band_dt = dt;
     return 0;
@@ -443,12 +487,11 @@ int ensure_dt_bands(adsg_ctx* c, double dt) {
 
 // rhs = (M(x)M(x)M - dt (K(x)M(x)M + M(x)K(x)M + M(x)M(x)K)) u_prev as a sequence of
 // band passes along z, y, x (3D), y, x (2D) or x (1D).
-int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) {
+int enqueue_rhs_with(adsg_ctx* c, const dim_dev* D, const double* u, double* rhs, double dt) {
     pdl_scope pdl(c->pdl);
     int st = ensure_dt_bands(c, dt);
     if (st) return st;
     const long long total = c->size;
-    const dim_dev* D = c->dims;
     cudaStream_t s = c->stream;
     double** T = c->scratch;
     if (c->ndim == 1) {
@@ -489,15 +532,19 @@ int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) {
     return 0;
 }
 
-int enqueue_solve(adsg_ctx* c, double* x, int trans) {
+int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) { return enqueue_rhs_with(c, c->dims, u, rhs, dt); }
+
+int enqueue_solve_with(adsg_ctx* c, const dim_dev* D, double* x, int trans) {
     pdl_scope pdl(c->pdl);
     for (int d = 0; d < c->ndim; ++d) {
         line_layout L = make_line_layout(c->n, c->ndim, d);
         stage_scope sc(c, ADSG_STAGE_SOLVE_X + d);
-        ADSG_CUDA_TRY(launch_line_solve(x, c->dims[d], L, trans, c->stream), "line solve");
+        ADSG_CUDA_TRY(launch_line_solve(x, D[d], L, trans, c->stream), "line solve");
     }
     return 0;
 }
+
+int enqueue_solve(adsg_ctx* c, double* x, int trans) { return enqueue_solve_with(c, c->dims, x, trans); }
 
 std::mutex g_autotune_lock;
 std::map<std::string, int> g_autotune_cache;
@@ -597,10 +644,53 @@ int autotune_solves(adsg_ctx* c) {
     return rc;
 }
 
+// One explicit step prev -> next through the step's own view (sdims): the
+// row-scaled right-hand side, then the solves.
 int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
-    int st = enqueue_rhs(c, prev, next, dt);
+    int st = ensure_dt_bands(c, dt);  // before the view is read
     if (st) return st;
-    return enqueue_solve(c, next, 0);
+    st = enqueue_rhs_with(c, c->sdims, prev, next, dt);
+    if (st) return st;
+    return enqueue_solve_with(c, c->sdims, next, 0);
+}
+
+// Builds the step's view of direction d once its solve variant is chosen.
+int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tables* tw) {
+    c->sdims[d] = c->dims[d];
+    if (!tw || !solve_variant_twisted(c->dims[d].solve_variant)) return 0;
+    twisted_tables u;
+    std::vector<double> scale;
+    scale_twisted(*tw, h.n, u, scale);
+    std::vector<double> m = row_band(h, 0), k = row_band(h, 1);
+    const int bw = 2 * h.p + 1;
+    for (int r = 0; r < h.n; ++r)
+        for (int t = 0; t < bw; ++t) {
+            m[static_cast<size_t>(r) * bw + t] *= scale[r];
+            k[static_cast<size_t>(r) * bw + t] *= scale[r];
+        }
+    double *sm = nullptr, *sk = nullptr, *l = nullptr, *uc = nullptr, *rd = nullptr, *g = nullptr;
+    dev_arena& A = c->arena;
+    cudaStream_t s = c->stream;
+    cudaError_t e = A.upload(&sm, m.data(), m.size(), s);
+    if (e == cudaSuccess) e = A.upload(&sk, k.data(), k.size(), s);
+    if (e == cudaSuccess) e = A.alloc(&c->snrow[d], m.size());
+    if (e == cudaSuccess) e = A.alloc(&c->skdt[d], m.size());
+    if (e == cudaSuccess) e = A.upload(&l, u.lmul.data(), u.lmul.size(), s);
+    if (e == cudaSuccess) e = A.upload(&uc, u.ucol.data(), u.ucol.size(), s);
+    if (e == cudaSuccess) e = A.upload(&rd, u.rdiag.data(), u.rdiag.size(), s);
+    if (e == cudaSuccess) e = A.upload(&g, u.g.data(), u.g.size(), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die here
+    if (e != cudaSuccess) return fail_cuda(e, "step tables");
+    dim_dev& S = c->sdims[d];
+    S.mrow = sm;
+    S.krow = sk;
+    S.tw_lmul = l;
+    S.tw_ucol = uc;
+    S.tw_rdiag = rd;
+    S.tw_g = g;
+    S.tw_unit = 1;
+    c->band_dt = std::nan("");  // the scaled dt bands are built on the next step
+    return 0;
 }
 
 // Launch-mode tuner: time a few explicit steps with and without programmatic
@@ -688,6 +778,8 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         delete c;
         return fail_cuda(e, "cudaStreamCreate");
     }
+    twisted_tables tw_keep[3];
+    bool tw_ok[3] = {false, false, false};
     c->own_stream = true;
 
     auto bail = [&](cudaError_t err, const char* where) {
@@ -713,8 +805,9 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         D.fwd_fast = t.fwd_fast;
         D.bwd_fast = t.bwd_fast;
         for (int v : t.uext) c->uext_sum[d] += v;
-        twisted_tables tw;
+        twisted_tables& tw = tw_keep[d];
         const bool have_tw = make_twisted_tables(h.n, h.kl, h.ku, h.ldab, h.lu, h.ipiv, tw) == 0;
+        tw_ok[d] = have_tw;
         const std::vector<double> m = row_band(h, 0);
         const std::vector<double> k = row_band(h, 1);
         const size_t nb = static_cast<size_t>(h.elements) * h.quad_order * 2 * (h.p + 1);
@@ -791,6 +884,11 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         delete c;
         return st;
     }
+    for (int d = 0; d < ndim; ++d)
+        if (int st = build_step_dim(c, d, dims[d], tw_ok[d] ? &tw_keep[d] : nullptr)) {
+            delete c;
+            return st;
+        }
     if (int st = autotune_launch_mode(c)) {
         delete c;
         return st;
@@ -870,6 +968,18 @@ int adsg_ads_solve_t(adsg_ctx* ctx, double* rhs_dev) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!rhs_dev) return fail(-2, "rhs is NULL");
     return enqueue_solve(ctx, rhs_dev, 1);
+}
+
+int adsg_heat_step(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, double dt) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_prev_dev) return fail(-2, "u_prev is NULL");
+    if (!u_next_dev) return fail(-3, "u_next is NULL");
+    if (!std::isfinite(dt)) return fail(-4, "dt must be finite");
+    const char* a = reinterpret_cast<const char*>(u_prev_dev);
+    const char* b = reinterpret_cast<const char*>(u_next_dev);
+    const size_t bytes = sizeof(double) * static_cast<size_t>(ctx->size);
+    if (a < b + bytes && b < a + bytes) return fail(-3, "u_prev and u_next overlap");
+    return enqueue_step(ctx, u_prev_dev, u_next_dev, dt);
 }
 
 int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps) {

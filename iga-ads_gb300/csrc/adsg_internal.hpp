@@ -47,6 +47,13 @@ struct twisted_tables {
     std::vector<double> lmul, ucol, rdiag, g;
 };
 
+// Row-scaled form of twisted tables for a right-hand side that arrives
+// multiplied by scale[r] = 1 / U(r, r) (r the global row along the line):
+// the upper factors get a unit diagonal (rdiag = 1, unused), the multipliers
+// and the meeting-point rows absorb the scaling.  Solving the scaled system
+// gives the same x.
+void scale_twisted(const twisted_tables& t, int n, twisted_tables& out, std::vector<double>& scale);
+
 // Row-format band [n][2p+1] of sum_e sum_q B_a B_b w_q J_e (which: 0 values, 1 derivatives).
 std::vector<double> row_band(const adsg_dim_desc& d, int which);
 bool valid_desc(const adsg_dim_desc& d);

@@ -655,7 +655,9 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
 // back-substitutes outward from there.  Same FP64 work per row as the
 // LAPACK-order sweep, twice the independent chains per line.
 // ---------------------------------------------------------------------------
-template <int K, int UNR>
+// UNIT: the right-hand side arrives row-scaled by 1 / U(r, r) and the tables
+// have a unit upper diagonal (no multiply in the backward sweep).
+template <int K, int UNR, bool UNIT>
 __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long long es, const int nc,
                                               const double* __restrict__ lmul, const double* __restrict__ ucol,
                                               const double* __restrict__ rdiag, const double* __restrict__ G,
@@ -750,7 +752,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 const int cc = max(jj - u, 0);
-                r[u] = __ldg(rdiag + cc);
+                r[u] = UNIT ? 1.0 : __ldg(rdiag + cc);
 #pragma unroll
                 for (int d = 0; d < K; ++d) uu[u * K + d] = __ldg(ucol + static_cast<long long>(cc) * K + d);
             }
@@ -770,7 +772,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
             load_block(c - UNR, rnx, unx);
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
-                const double v = b[0] * rc[u];
+                const double v = UNIT ? b[0] : b[0] * rc[u];
                 x[(c - u) * es] = v;
                 const double nv = -v;
 #pragma unroll
@@ -783,7 +785,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
     }
     for (; c >= 0; --c) {
         const double incoming = ld(c - K - 1);
-        const double v = b[0] * __ldg(rdiag + c);
+        const double v = UNIT ? b[0] : b[0] * __ldg(rdiag + c);
         x[c * es] = v;
         const double nv = -v;
 #pragma unroll
@@ -794,7 +796,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
     }
 }
 
-template <int K, int UNR>
+template <int K, int UNR, bool UNIT>
 __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restrict__ data, dim_dev D, line_layout L) {
     const int lane = threadIdx.x & 31, chain = lane >> 4;
     const long long g = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 16 + (lane & 15);
@@ -806,7 +808,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restr
     const long long es = L.elem_stride;
     const long long off = static_cast<long long>(chain) * D.tw_rows;
     if (chain) x += static_cast<long long>(D.n - 1) * es;
-    twisted_chain<K, UNR>(x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
+    twisted_chain<K, UNR, UNIT>(x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
                           D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
 }
 
@@ -817,7 +819,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restr
 // tile pitch is odd so that the 16 lines of one row fall in distinct banks.
 __host__ __device__ inline int twisted_pitch(int n) { return n | 1; }
 
-template <int K, int UNR>
+template <int K, int UNR, bool UNIT>
 __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* __restrict__ data, dim_dev D,
                                                                         line_layout L) {
     extern __shared__ double smem[];
@@ -841,7 +843,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
     if (active) {
         double* x = tile + line * pitch + (chain ? n - 1 : 0);
         const long long off = static_cast<long long>(chain) * D.tw_rows;
-        twisted_chain<K, UNR>(x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
+        twisted_chain<K, UNR, UNIT>(x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
                               D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
     }
     __syncwarp();
@@ -854,7 +856,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
 
 size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
 
-template <int K>
+template <int K, bool UNIT>
 static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, bool staged, cudaStream_t s) {
     constexpr int UNR = K > 2 ? 4 : 8;
     if (staged && L.contiguous) {
@@ -863,15 +865,16 @@ static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& 
         const size_t smem = per_warp * wpb;
         if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
         if (smem > 48 * 1024) {
-            cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(line_solve_twisted_staged_kernel<K, UNR>), smem);
+            cudaError_t e =
+                ensure_smem_attribute(reinterpret_cast<const void*>(line_solve_twisted_staged_kernel<K, UNR, UNIT>), smem);
             if (e != cudaSuccess) return e;
         }
         const long long per = 16LL * wpb;
-        return launch_pdl(line_solve_twisted_staged_kernel<K, UNR>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
+        return launch_pdl(line_solve_twisted_staged_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
                           dim3(32 * wpb), smem, s, data, d, L);
     }
     const long long per = 64;  // 4 warps x 16 lines
-    return launch_pdl(line_solve_twisted_kernel<K, UNR>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
+    return launch_pdl(line_solve_twisted_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
                       dim3(128), 0, s, data, d, L);
 }
 
@@ -960,11 +963,19 @@ cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout&
     const int v = trans ? SOLVE_STAGED_1 : d.solve_variant;
     if (!trans && (v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED) && line_solve_variant_ok(v, d)) {
         const bool staged = v == SOLVE_TWISTED_STAGED;
+        if (d.tw_unit) {
+            switch (d.tw_k) {
+                case 1: return twisted_t<1, true>(data, d, L, staged, s);
+                case 2: return twisted_t<2, true>(data, d, L, staged, s);
+                case 3: return twisted_t<3, true>(data, d, L, staged, s);
+                default: return twisted_t<4, true>(data, d, L, staged, s);
+            }
+        }
         switch (d.tw_k) {
-            case 1: return twisted_t<1>(data, d, L, staged, s);
-            case 2: return twisted_t<2>(data, d, L, staged, s);
-            case 3: return twisted_t<3>(data, d, L, staged, s);
-            default: return twisted_t<4>(data, d, L, staged, s);
+            case 1: return twisted_t<1, false>(data, d, L, staged, s);
+            case 2: return twisted_t<2, false>(data, d, L, staged, s);
+            case 3: return twisted_t<3, false>(data, d, L, staged, s);
+            default: return twisted_t<4, false>(data, d, L, staged, s);
         }
     }
     if (!trans && v != SOLVE_STAGED_1 && v != SOLVE_TWISTED && v != SOLVE_TWISTED_STAGED &&

@@ -48,6 +48,7 @@ struct dim_dev {
     // Twisted factorisation (0 = not available): rows [0, tw_n1) form chain 0,
     // rows [tw_n1, n) chain 1 in reverse order; tables per chain, stride tw_rows.
     int tw_k = 0, tw_n1 = 0, tw_n2 = 0, tw_rows = 0;
+    int tw_unit = 0;  // tables of the row-scaled system (unit upper diagonal)
     const double* tw_lmul = nullptr;   // [2][tw_rows][k] multipliers of chain-local column j
     const double* tw_ucol = nullptr;   // [2][tw_rows][k] U(j-d, j), d = 1..k
     const double* tw_rdiag = nullptr;  // [2][tw_rows] 1 / U(j, j)

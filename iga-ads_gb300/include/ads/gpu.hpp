@@ -126,6 +126,9 @@ public:
     // device buffers
     void compute_rhs_heat_dev(const double* u_prev, double* rhs, double dt) { check(adsg_heat_rhs(ctx_, u_prev, rhs, dt)); }
     void solve_dev(double* rhs) { check(adsg_ads_solve(ctx_, rhs, nullptr)); }
+    void heat_step_dev(const double* u_prev, double* u_next, double dt) {
+        check(adsg_heat_step(ctx_, u_prev, u_next, dt));
+    }
     void heat_steps_dev(double* u, double dt, int nsteps) { check(adsg_heat_steps(ctx_, u, dt, nsteps)); }
     void synchronize() { check(adsg_ctx_synchronize(ctx_)); }
 

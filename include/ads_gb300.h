@@ -123,9 +123,18 @@ int adsg_ads_solve(adsg_ctx* ctx, double* rhs_dev, double* buf_dev);
  * adsg_ads_solve. */
 int adsg_ads_solve_t(adsg_ctx* ctx, double* rhs_dev);
 
+/* One explicit step, heat_3d::step (heat_3d.hpp:39-47: compute_rhs then
+ * ads_solve): u_next = M^-1 R u_prev.  u_prev_dev and u_next_dev must not
+ * overlap.  Because the right-hand side stays internal, directions solved
+ * with the two-ended sweep receive it row-scaled by their factors' diagonal
+ * (folded into the band rows) and skip the backward sweep's multiply; the
+ * result equals adsg_heat_rhs + adsg_ads_solve up to rounding. */
+int adsg_heat_step(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, double dt);
+
 /* nsteps of simulation_base::run's loop with heat_3d's step
  * (simulation_base.cpp:11-20, heat_3d.hpp:39-47): swap, compute_rhs, solve.
- * u_dev holds the state in and out.  Steps are replayed from a CUDA graph. */
+ * u_dev holds the state in and out.  Steps are adsg_heat_step's, replayed
+ * from a CUDA graph. */
 int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps);
 
 /* ---- stage timers (observability) -----------------------------------------

@@ -242,19 +242,26 @@ def test_full_size_linearity_and_determinism(big):
 
 
 def test_full_size_graph_steps_equal_explicit_loop(big):
+    """adsg_heat_steps replays adsg_heat_step bitwise; both agree with
+    compute_rhs + ads_solve issued as two calls up to rounding (the step path
+    feeds the two-ended solves a row-scaled right-hand side)."""
     import torch
 
     dims, ctx, u = big
     a = u.clone()
     ctx.heat_steps(a, 1e-6, 3)
-    b = u.clone()
-    tmp = torch.empty_like(u)
+    b, tb = u.clone(), torch.empty_like(u)
     for _ in range(3):
-        ctx.heat_rhs(b, tmp, 1e-6)
-        ctx.ads_solve(tmp)
-        b, tmp = tmp, b
+        ctx.heat_step(b, tb, 1e-6)
+        b, tb = tb, b
+    c, tc = u.clone(), torch.empty_like(u)
+    for _ in range(3):
+        ctx.heat_rhs(c, tc, 1e-6)
+        ctx.ads_solve(tc)
+        c, tc = tc, c
     ctx.synchronize()
     assert torch.equal(a, b)
+    assert float(torch.linalg.norm(b - c) / torch.linalg.norm(c)) <= 1e-13
 
 
 def test_full_size_element_and_factored_rhs_agree(big):
@@ -347,3 +354,32 @@ def test_launch_mode_does_not_change_results(p, elements, cuda, monkeypatch):
         out.append((u, r))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("p,elements", [
+    ((2, 2, 2), (30, 7, 9)),
+    ((4, 4, 4), (12, 9, 6)),
+    ((3, 3), (50, 33)),
+    ((1, 2, 4), (5, 6, 7)),
+    ((2,), (200,)),
+    ((3, 2), (1, 40)),
+])
+def test_heat_step_against_oracle(p, elements, cuda):
+    """adsg_heat_step (heat_3d::step) on mixed grids: directions with and
+    without the two-ended solve (and so with and without the row-scaled
+    right-hand side) against the oracle's compute_rhs + dgbtrs solve."""
+    import torch
+
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    pr = oracle.Problem(list(p), list(elements))
+    u0 = np.random.default_rng(11).uniform(-1, 1, pr.size)
+    a = torch.from_numpy(u0).cuda()
+    b = torch.empty_like(a)
+    for _ in range(2):
+        ctx.heat_step(a, b, 1e-5)
+        a, b = b, a
+    ctx.synchronize()
+    assert oracle.rel_l2(a.cpu().numpy(), pr.heat_steps(u0, 1e-5, 2)) <= 2 * step_tol(_conds(dims))
+    with pytest.raises(RuntimeError, match="overlap"):
+        ctx.heat_step(a, a, 1e-5)
