@@ -96,6 +96,7 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
         "adsg_ctx_launch_pdl": (i, [vp]),
+        "adsg_ctx_fused_x": (i, [vp]),
         "adsg_quad_size": (ll, [vp]),
         "adsg_count_nonfinite": (i, [vp, vp, ctypes.POINTER(ll)]),
         "adsg_load_vector": (i, [vp, vp, vp]),
@@ -165,8 +166,8 @@ def _host(a: np.ndarray) -> np.ndarray:
     return a
 
 
-NSTAGES = 7
-STAGES = ("rhs_outer", "rhs_middle", "rhs_x", "solve_x", "solve_y", "solve_z", "rhs_elem")
+NSTAGES = 8
+STAGES = ("rhs_outer", "rhs_middle", "rhs_x", "solve_x", "solve_y", "solve_z", "rhs_elem", "rhs_solve_x")
 
 
 class Dimension:
@@ -297,6 +298,10 @@ class Context:
     def launch_pdl(self) -> bool:
         """Whether the step's kernels use programmatic dependent launch."""
         return library().adsg_ctx_launch_pdl(self._h) == 1
+
+    def fused_x(self) -> bool:
+        """Whether heat_step fuses the x band pass into the x solve."""
+        return library().adsg_ctx_fused_x(self._h) == 1
 
     def stage_work(self) -> dict:
         """{stage: (fp64_flops, hbm_bytes)} of one launch of each stage."""

@@ -406,7 +406,8 @@ struct adsg_ctx {
     long long stage_launches[ADSG_NSTAGES] = {};
     // adjoints created on this context (detached when the context goes first)
     std::vector<adsg_adjoint*> adjoints;
-    int pdl = 0;  // programmatic dependent launch for the step kernels (chosen at creation)
+    int pdl = 0;     // programmatic dependent launch for the step kernels (chosen at creation)
+    int fuse_x = 0;  // the step fuses the x band pass with the x solve (chosen at creation)
 
     cudaEvent_t take_event() {
         if (!spare.empty()) {
@@ -487,56 +488,69 @@ int ensure_dt_bands(adsg_ctx* c, double dt) {
 
 // rhs = (M(x)M(x)M - dt (K(x)M(x)M + M(x)K(x)M + M(x)M(x)K)) u_prev as a sequence of
 // band passes along z, y, x (3D), y, x (2D) or x (1D).
-int enqueue_rhs_with(adsg_ctx* c, const dim_dev* D, const double* u, double* rhs, double dt) {
+// fused_x: the x pass is issued fused with the x solve (rhs then holds the
+// x-solved right-hand side); the caller checks fusion_ok first.
+// outer_done: the first (outermost-axis) pass has already been issued into
+// scratch[0..1] (the host entry overlaps it with the upload).
+int enqueue_rhs_with(adsg_ctx* c, const dim_dev* D, const double* u, double* rhs, double dt, bool fused_x = false,
+                     bool outer_done = false) {
     pdl_scope pdl(c->pdl);
     int st = ensure_dt_bands(c, dt);
     if (st) return st;
     const long long total = c->size;
     cudaStream_t s = c->stream;
     double** T = c->scratch;
-    if (c->ndim == 1) {
+    const line_layout Lx = make_line_layout(c->n, c->ndim, 0);
+    // the last pass, along x: out = A0 (.) in0 [+ A1 (.) in1]
+    auto x_pass = [&](const double* in0, const double* in1, const double* A0, const double* A1) -> int {
+        if (fused_x) {
+            stage_scope sc(c, ADSG_STAGE_RHS_SOLVE_X);
+            ADSG_CUDA_TRY(launch_rhs_x_solve(in0, in1, rhs, A0, A1, D[0], Lx, s), "rhs pass x + x solve");
+            return 0;
+        }
         stage_scope sc(c, ADSG_STAGE_RHS_X);
-        ADSG_CUDA_TRY(launch_band_pass(D[0].p, u, nullptr, rhs, nullptr, D[0].nrow, nullptr, nullptr, D[0].n, 1,
-                                       total, s),
+        ADSG_CUDA_TRY(launch_band_pass(D[0].p, in0, in1, rhs, nullptr, A0, A1, nullptr, D[0].n, 1, total, s),
                       "rhs pass x");
+        return 0;
+    };
+    if (c->ndim == 1) {
+        if (int st2 = x_pass(u, nullptr, D[0].nrow, nullptr)) return st2;
     } else if (c->ndim == 2) {
         const long long sy = c->n[0];
         // A = My u, C = Ny u
-        stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
-        ADSG_CUDA_TRY(launch_band_pass(D[1].p, u, nullptr, T[0], T[1], D[1].mrow, nullptr, D[1].nrow, D[1].n, sy,
-                                       total, s),
-                      "rhs pass y");
+        if (!outer_done) {
+            stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
+            ADSG_CUDA_TRY(launch_band_pass(D[1].p, u, nullptr, T[0], T[1], D[1].mrow, nullptr, D[1].nrow, D[1].n, sy,
+                                           total, s),
+                          "rhs pass y");
+        }
         // rhs = (-dt Kx) A + Mx C
-        stage_scope s2(c, ADSG_STAGE_RHS_X);
-        ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[0], T[1], rhs, nullptr, D[0].kdt, D[0].mrow, nullptr, D[0].n, 1,
-                                       total, s),
-                      "rhs pass x");
+        if (int st2 = x_pass(T[0], T[1], D[0].kdt, D[0].mrow)) return st2;
     } else {
         const long long sy = c->n[0], sz = static_cast<long long>(c->n[0]) * c->n[1];
         // A = Mz u, C = Nz u
-        { stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
-        ADSG_CUDA_TRY(launch_band_pass(D[2].p, u, nullptr, T[0], T[1], D[2].mrow, nullptr, D[2].nrow, D[2].n, sz,
-                                       total, s),
-                      "rhs pass z"); }
+        if (!outer_done) {
+            stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
+            ADSG_CUDA_TRY(launch_band_pass(D[2].p, u, nullptr, T[0], T[1], D[2].mrow, nullptr, D[2].nrow, D[2].n, sz,
+                                           total, s),
+                          "rhs pass z");
+        }
         // F = (-dt Ky) A + My C,  G = My A
         { stage_scope s2(c, ADSG_STAGE_RHS_MIDDLE);
         ADSG_CUDA_TRY(launch_band_pass(D[1].p, T[0], T[1], T[2], T[3], D[1].kdt, D[1].mrow, D[1].mrow, D[1].n, sy,
                                        total, s),
                       "rhs pass y"); }
         // rhs = (-dt Kx) G + Mx F
-        stage_scope s3(c, ADSG_STAGE_RHS_X);
-        ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[3], T[2], rhs, nullptr, D[0].kdt, D[0].mrow, nullptr, D[0].n, 1,
-                                       total, s),
-                      "rhs pass x");
+        if (int st2 = x_pass(T[3], T[2], D[0].kdt, D[0].mrow)) return st2;
     }
     return 0;
 }
 
 int enqueue_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) { return enqueue_rhs_with(c, c->dims, u, rhs, dt); }
 
-int enqueue_solve_with(adsg_ctx* c, const dim_dev* D, double* x, int trans) {
+int enqueue_solve_with(adsg_ctx* c, const dim_dev* D, double* x, int trans, int first_dim = 0, int end_dim = 3) {
     pdl_scope pdl(c->pdl);
-    for (int d = 0; d < c->ndim; ++d) {
+    for (int d = first_dim; d < c->ndim && d < end_dim; ++d) {
         line_layout L = make_line_layout(c->n, c->ndim, d);
         stage_scope sc(c, ADSG_STAGE_SOLVE_X + d);
         ADSG_CUDA_TRY(launch_line_solve(x, D[d], L, trans, c->stream), "line solve");
@@ -646,12 +660,18 @@ int autotune_solves(adsg_ctx* c) {
 
 // One explicit step prev -> next through the step's own view (sdims): the
 // row-scaled right-hand side, then the solves.
+bool fusion_ok(const adsg_ctx* c) {
+    return c->sdims[0].solve_variant == SOLVE_TWISTED_STAGED &&
+           rhs_x_solve_ok(c->sdims[0], make_line_layout(c->n, c->ndim, 0));
+}
+
 int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     int st = ensure_dt_bands(c, dt);  // before the view is read
     if (st) return st;
-    st = enqueue_rhs_with(c, c->sdims, prev, next, dt);
+    const bool fused = c->fuse_x && fusion_ok(c);
+    st = enqueue_rhs_with(c, c->sdims, prev, next, dt, fused);
     if (st) return st;
-    return enqueue_solve_with(c, c->sdims, next, 0);
+    return enqueue_solve_with(c, c->sdims, next, 0, fused ? 1 : 0);
 }
 
 // Builds the step's view of direction d once its solve variant is chosen.
@@ -693,29 +713,49 @@ int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tab
     return 0;
 }
 
-// Launch-mode tuner: time a few explicit steps with and without programmatic
-// dependent launch and keep the faster (results are the same either way).
-// ADSG_PDL=0/1 forces the mode.
+// Step tuner: time a few explicit steps under each launch mode and keep the
+// fastest.  Two switches, neither of which changes any result bit:
+// programmatic dependent launch (ADSG_PDL=0/1 forces it) and, where the x
+// direction uses the staged two-ended solve, fusing the x band pass into that
+// solve (ADSG_FUSE_X=0/1 forces it).
 int autotune_launch_mode(adsg_ctx* c) {
-    const char* force = std::getenv("ADSG_PDL");
-    if (force && (*force == '0' || *force == '1')) {
-        c->pdl = *force == '1';
+    auto forced = [](const char* name) -> int {
+        const char* v = std::getenv(name);
+        return v && (*v == '0' || *v == '1') ? *v - '0' : -1;
+    };
+    const int f_pdl = forced("ADSG_PDL"), f_fuse = forced("ADSG_FUSE_X");
+    const bool can_fuse = fusion_ok(c);
+    std::vector<int> modes;  // bit 0: pdl, bit 1: fuse
+    for (int m = 0; m < 4; ++m) {
+        const int pdl = m & 1, fuse = (m >> 1) & 1;
+        if (fuse && !can_fuse) continue;
+        if (f_pdl >= 0 && pdl != f_pdl) continue;
+        if (f_fuse >= 0 && fuse != (f_fuse && can_fuse)) continue;
+        modes.push_back(m);
+    }
+    if (modes.empty()) modes.push_back(0);
+    auto apply = [&](int m) {
+        c->pdl = m & 1;
+        c->fuse_x = (m >> 1) & 1;
+    };
+    if (modes.size() == 1) {
+        apply(modes[0]);
         return 0;
     }
     double* tmp = nullptr;
     if (cudaMalloc(&tmp, sizeof(double) * c->size) != cudaSuccess) {  // no room: keep plain launches
         cudaGetLastError();
-        c->pdl = 0;
+        apply(modes[0]);
         return 0;
     }
     cudaEvent_t a = nullptr, b = nullptr;
     cudaError_t e = cudaEventCreate(&a);
     if (e == cudaSuccess) e = cudaEventCreate(&b);
     float best = 1e30f;
-    int best_mode = 0, rc = 0;
+    int best_mode = modes[0], rc = 0;
     const int reps = 4;
-    for (int mode = 0; mode < 2 && e == cudaSuccess && rc == 0; ++mode) {
-        c->pdl = mode;
+    for (size_t i = 0; i < modes.size() && e == cudaSuccess && rc == 0; ++i) {
+        apply(modes[i]);
         rc = enqueue_step(c, c->ping, tmp, 1e-6);  // warm-up (also builds the dt bands)
         if (rc == 0) e = cudaEventRecord(a, c->stream);
         for (int r = 0; r < reps && rc == 0 && e == cudaSuccess; ++r) {
@@ -728,10 +768,10 @@ int autotune_launch_mode(adsg_ctx* c) {
         if (rc == 0 && e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
         if (rc == 0 && e == cudaSuccess && ms < best) {
             best = ms;
-            best_mode = mode;
+            best_mode = modes[i];
         }
     }
-    c->pdl = best_mode;
+    apply(best_mode);
     if (a) cudaEventDestroy(a);
     if (b) cudaEventDestroy(b);
     cudaFree(tmp);
@@ -739,6 +779,53 @@ int autotune_launch_mode(adsg_ctx* c) {
     if (e != cudaSuccess) return fail_cuda(e, "launch-mode tuner");
     // the tuner ran on the context's own (zeroed) state buffer; leave it zero
     ADSG_CUDA_TRY(cudaMemsetAsync(c->ping, 0, sizeof(double) * c->size, c->stream), "launch-mode tuner");
+    return 0;
+}
+
+// Host-buffer steps (2D and 3D).  The host link moves ~200 GB/s either way,
+// so each step's state costs about as long to move as to compute.  When the
+// input is pinned host memory (mapped into the device's address space), the
+// first step's first band pass, the only reader of that input, reads it
+// there directly as column sweeps: the upload runs under the pass's
+// arithmetic instead of before it.  The result is copied back once after the
+// last step (stores to host memory from the solve kernels were measured
+// slower than one copy).
+int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, double dt, int nsteps) {
+    const int o = c->ndim - 1;  // outermost axis
+    const long long so = c->size / c->n[o];
+    int st = ensure_dt_bands(c, dt);
+    if (st) return st;
+    const dim_dev* D = c->sdims;
+    double* cur = c->host_io;
+    double* nxt = c->ping;
+    const double* in_dev = nullptr;
+    {
+        cudaPointerAttributes attr{};
+        if (cudaPointerGetAttributes(&attr, u_in) == cudaSuccess && attr.type == cudaMemoryTypeHost)
+            in_dev = static_cast<const double*>(attr.devicePointer);
+        cudaGetLastError();
+    }
+    // below ~2 MB the copy is a few microseconds and the column sweeps would
+    // run nearly serially
+    const bool direct_in = in_dev && outer_pass_columns_ok(D[o].p) && c->size >= (1LL << 18);
+    if (direct_in) {
+        pdl_scope pdl(c->pdl);
+        stage_scope sc(c, ADSG_STAGE_RHS_OUTER);
+        ADSG_CUDA_TRY(launch_outer_pass_columns(D[o].p, in_dev, c->scratch[0], c->scratch[1], D[o].mrow, D[o].nrow,
+                                                c->n[o], so, c->stream),
+                      "rhs pass (outer, from host)");
+    } else {
+        ADSG_CUDA_TRY(cudaMemcpyAsync(cur, u_in, sizeof(double) * c->size, cudaMemcpyHostToDevice, c->stream), "H2D");
+    }
+    for (int step = 0; step < nsteps; ++step) {
+        const bool fused = c->fuse_x && fusion_ok(c);
+        st = enqueue_rhs_with(c, D, cur, nxt, dt, fused, /*outer_done=*/step == 0 && direct_in);
+        if (st) return st;
+        st = enqueue_solve_with(c, D, nxt, 0, fused ? 1 : 0);
+        if (st) return st;
+        std::swap(cur, nxt);
+    }
+    ADSG_CUDA_TRY(cudaMemcpyAsync(u_out, cur, sizeof(double) * c->size, cudaMemcpyDeviceToHost, c->stream), "D2H");
     return 0;
 }
 
@@ -1055,6 +1142,8 @@ int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants) {
 
 int adsg_ctx_launch_pdl(const adsg_ctx* ctx) { return ctx ? ctx->pdl : -1; }
 
+int adsg_ctx_fused_x(const adsg_ctx* ctx) { return ctx ? ctx->fuse_x : -1; }
+
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!flops) return fail(-2, "flops is NULL");
@@ -1111,6 +1200,9 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
             bytes[ADSG_STAGE_RHS_ELEM] = 16.0 * total;
         }
     }
+    // fused x pass + x solve: both works, the pass's inputs and the solved output
+    flops[ADSG_STAGE_RHS_SOLVE_X] = flops[ADSG_STAGE_RHS_X] + flops[ADSG_STAGE_SOLVE_X];
+    bytes[ADSG_STAGE_RHS_SOLVE_X] = bytes[ADSG_STAGE_RHS_X];
     return 0;
 }
 
@@ -1622,8 +1714,17 @@ int adsg_ads_solve_general_host(adsg_ctx* ctx, int special_dim, const adsg_line_
 int adsg_heat_steps_host(adsg_ctx* ctx, double* u_host, double dt, int nsteps) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!u_host) return fail(-2, "u is NULL");
+    if (!std::isfinite(dt)) return fail(-3, "dt must be finite");
+    if (nsteps < 0) return fail(-4, "nsteps must be >= 0");
+    if (nsteps == 0) return 0;
     if (!ctx->host_io) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->host_io, ctx->size), "io alloc");
     const size_t bytes = sizeof(double) * ctx->size;
+    if (ctx->ndim >= 2) {
+        int st = heat_steps_host_direct(ctx, u_host, u_host, dt, nsteps);
+        if (st) return st;
+        ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+        return 0;
+    }
     ADSG_CUDA_TRY(cudaMemcpyAsync(ctx->host_io, u_host, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
     int st = adsg_heat_steps(ctx, ctx->host_io, dt, nsteps);
     if (st) return st;

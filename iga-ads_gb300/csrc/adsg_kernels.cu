@@ -134,6 +134,82 @@ cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double
     }
 }
 
+// ---------------------------------------------------------------------------
+// Outer-axis pass as column sweeps.  Thread (column, segment) walks the rows
+// of one segment of one column of the outermost axis with a window of the
+// 2P+1 neighbouring inputs, so every input value is read once (plus a 2P-row
+// halo per segment) instead of 2P+1 times.  That matters when the input sits
+// in pinned host memory, whose lines the GPU does not keep in L2: the pass
+// then streams its input over the host link once while it computes.  The
+// rows ahead are prefetched PRE deep to keep enough host reads in flight.
+// Per output the operations and their order are band_pass_kernel's
+// (out0 = A0 (.) in, out1 = B0 (.) in), so the results are bitwise equal.
+// ---------------------------------------------------------------------------
+template <int P>
+__global__ void __launch_bounds__(128) outer_columns_kernel(const double* __restrict__ in, double* __restrict__ out0,
+                                                            double* __restrict__ out1, const double* __restrict__ A0,
+                                                            const double* __restrict__ B0, int n, long long so,
+                                                            int seg) {
+    constexpr int BW = 2 * P + 1, PRE = 8;
+    const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const long long nseg = (n + seg - 1) / seg;
+    if (t >= so * nseg) return;
+    pdl_wait_and_release();
+    const long long col = t % so;
+    const int r0 = static_cast<int>(t / so) * seg, r1 = min(n, r0 + seg);
+    const double* src = in + col;
+    auto ld = [&](int r) -> double { return (r >= 0 && r < n) ? src[r * so] : 0.0; };
+    double w[BW];
+#pragma unroll
+    for (int q = 0; q < BW; ++q) w[q] = ld(r0 - P + q);
+    double pre[PRE];
+#pragma unroll
+    for (int q = 0; q < PRE; ++q) pre[q] = ld(r0 + P + 1 + q);
+    for (int r = r0; r < r1; ++r) {
+        const double* a0 = A0 + static_cast<long long>(r) * BW;
+        const double* b0 = B0 + static_cast<long long>(r) * BW;
+        double acc0 = 0.0, acc1 = 0.0;
+#pragma unroll
+        for (int q = 0; q < BW; ++q) {
+            const int c = r - P + q;
+            if (c >= 0 && c < n) {
+                acc0 = fma(__ldg(a0 + q), w[q], acc0);
+                acc1 = fma(__ldg(b0 + q), w[q], acc1);
+            }
+        }
+        out0[col + r * so] = acc0;
+        out1[col + r * so] = acc1;
+#pragma unroll
+        for (int q = 0; q < BW - 1; ++q) w[q] = w[q + 1];
+        w[BW - 1] = pre[0];
+#pragma unroll
+        for (int q = 0; q < PRE - 1; ++q) pre[q] = pre[q + 1];
+        pre[PRE - 1] = ld(r + P + 1 + PRE);
+    }
+}
+
+bool outer_pass_columns_ok(int p) { return p >= 1 && p <= 4; }
+
+cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, double* out1, const double* A0,
+                                      const double* B0, int n_axis, long long stride, cudaStream_t s) {
+    if (!outer_pass_columns_ok(p)) return cudaErrorInvalidValue;
+    // whole columns (each input read exactly once) unless there are too few
+    // columns to give every sub-partition a few warps; segments re-read a
+    // 2p-row halo each
+    const long long want = 16384;
+    int seg = n_axis;
+    if (stride < want) seg = static_cast<int>(std::max<long long>(32, (n_axis * stride + want - 1) / want));
+    const long long threads = stride * ((n_axis + seg - 1) / seg);
+    if (threads <= 0) return cudaSuccess;
+    const dim3 grid(static_cast<unsigned>((threads + 127) / 128)), block(128);
+    switch (p) {
+        case 1: return launch_pdl(outer_columns_kernel<1>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
+        case 2: return launch_pdl(outer_columns_kernel<2>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
+        case 3: return launch_pdl(outer_columns_kernel<3>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
+        default: return launch_pdl(outer_columns_kernel<4>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
+    }
+}
+
 __global__ void dt_bands_kernel(const double* __restrict__ mrow, const double* __restrict__ krow,
                                 double* __restrict__ nrow, double* __restrict__ kdt, double dt, int count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -657,11 +733,14 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
 // ---------------------------------------------------------------------------
 // UNIT: the right-hand side arrives row-scaled by 1 / U(r, r) and the tables
 // have a unit upper diagonal (no multiply in the backward sweep).
+// xo: where the backward sweep stores the solution (x itself, or another
+// buffer with the same layout, e.g. mapped host memory); the forward results
+// stay in x.
 template <int K, int UNR, bool UNIT>
-__device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long long es, const int nc,
-                                              const double* __restrict__ lmul, const double* __restrict__ ucol,
-                                              const double* __restrict__ rdiag, const double* __restrict__ G,
-                                              const unsigned mask) {
+__device__ __forceinline__ void twisted_chain(double* __restrict__ x, double* __restrict__ xo, const long long es,
+                                              const int nc, const double* __restrict__ lmul,
+                                              const double* __restrict__ ucol, const double* __restrict__ rdiag,
+                                              const double* __restrict__ G, const unsigned mask) {
     auto ld = [&](int r) -> double {
         if (r < 0 || r >= nc) return 0.0;
         return x[r * es];
@@ -735,7 +814,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
 #pragma unroll
     for (int a = K - 1; a >= 0; --a, --c) {  // the chain's K interface rows
         const double v = z[a];
-        x[c * es] = v;
+        xo[c * es] = v;
         const double nv = -v;
 #pragma unroll
         for (int d = 1; d <= K; ++d) b[d] = fma(nv, __ldg(ucol + static_cast<long long>(c) * K + d - 1), b[d]);
@@ -773,7 +852,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
 #pragma unroll
             for (int u = 0; u < UNR; ++u) {
                 const double v = UNIT ? b[0] : b[0] * rc[u];
-                x[(c - u) * es] = v;
+                xo[(c - u) * es] = v;
                 const double nv = -v;
 #pragma unroll
                 for (int d = 1; d <= K; ++d) b[d] = fma(nv, uc[u * K + d - 1], b[d]);
@@ -786,7 +865,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, const long
     for (; c >= 0; --c) {
         const double incoming = ld(c - K - 1);
         const double v = UNIT ? b[0] : b[0] * __ldg(rdiag + c);
-        x[c * es] = v;
+        xo[c * es] = v;
         const double nv = -v;
 #pragma unroll
         for (int d = 1; d <= K; ++d) b[d] = fma(nv, __ldg(ucol + static_cast<long long>(c) * K + d - 1), b[d]);
@@ -808,7 +887,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restr
     const long long es = L.elem_stride;
     const long long off = static_cast<long long>(chain) * D.tw_rows;
     if (chain) x += static_cast<long long>(D.n - 1) * es;
-    twisted_chain<K, UNR, UNIT>(x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
+    twisted_chain<K, UNR, UNIT>(x, x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
                           D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
 }
 
@@ -843,8 +922,8 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
     if (active) {
         double* x = tile + line * pitch + (chain ? n - 1 : 0);
         const long long off = static_cast<long long>(chain) * D.tw_rows;
-        twisted_chain<K, UNR, UNIT>(x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
-                              D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
+        twisted_chain<K, UNR, UNIT>(x, x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K,
+                                    D.tw_ucol + off * K, D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
     }
     __syncwarp();
     double* dst = data + g0 * n;
@@ -855,6 +934,109 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
 }
 
 size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
+
+// ---------------------------------------------------------------------------
+// The x band pass of the right-hand side fused with the x line solve.  Both
+// work on the same contiguous x-lines: each warp computes the band pass of its
+// 16 lines straight into its shared tile (out = A0 (.) in0 [+ A1 (.) in1],
+// the same operations in the same order as band_pass_kernel, so the tile
+// holds bitwise the values that kernel would store), sweeps the tile with the
+// two-ended solve and writes the solved lines once.
+// ---------------------------------------------------------------------------
+template <int K, int UNR, bool UNIT, bool IN1>
+__global__ void __launch_bounds__(128) rhs_x_solve_kernel(const double* __restrict__ in0,
+                                                          const double* __restrict__ in1,
+                                                          double* __restrict__ out, const double* __restrict__ A0,
+                                                          const double* __restrict__ A1, dim_dev D, line_layout L) {
+    extern __shared__ double smem[];
+    constexpr int BW = 2 * K + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4;
+    const int n = D.n, pitch = twisted_pitch(n);
+    const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
+    if (g0 >= L.nlines) return;  // whole warp
+    pdl_wait_and_release();
+    const int nv = static_cast<int>(min(16LL, L.nlines - g0));
+    double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
+    const long long base = g0 * n;
+    const int count = nv * n;
+    for (int e = lane; e < count; e += 32) {
+        const int line = e / n, r = e - line * n;
+        const double* a0 = A0 + static_cast<long long>(r) * BW;
+        const double* a1 = IN1 ? A1 + static_cast<long long>(r) * BW : nullptr;
+        const long long g = base + e;
+        double acc = 0.0;
+#pragma unroll
+        for (int t = 0; t < BW; ++t) {
+            const int c = r - K + t;
+            if (c >= 0 && c < n) {
+                const long long at = g + (t - K);
+                acc = fma(__ldg(a0 + t), __ldg(in0 + at), acc);
+                if (IN1) acc = fma(__ldg(a1 + t), __ldg(in1 + at), acc);
+            }
+        }
+        tile[line * pitch + r] = acc;
+    }
+    __syncwarp();
+    const int line = lane & 15;
+    const bool active = line < nv;
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (active) {
+        double* x = tile + line * pitch + (chain ? n - 1 : 0);
+        const long long off = static_cast<long long>(chain) * D.tw_rows;
+        twisted_chain<K, UNR, UNIT>(x, x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K,
+                                    D.tw_ucol + off * K, D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
+    }
+    __syncwarp();
+    for (int e = lane; e < count; e += 32) {
+        const int ln = e / n;
+        out[base + e] = tile[ln * pitch + (e - ln * n)];
+    }
+}
+
+template <int K, bool UNIT, bool IN1>
+static cudaError_t rhs_x_solve_t(const double* in0, const double* in1, double* out, const double* A0,
+                                 const double* A1, const dim_dev& d, const line_layout& L, cudaStream_t s) {
+    constexpr int UNR = K > 2 ? 4 : 8;
+    const size_t per_warp = twisted_staged_smem_per_warp(d.n);
+    const int wpb = per_warp * 4 <= 227 * 1024 ? 4 : (per_warp * 2 <= 227 * 1024 ? 2 : 1);
+    const size_t smem = per_warp * wpb;
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    auto kern = rhs_x_solve_kernel<K, UNR, UNIT, IN1>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(kern), smem);
+        if (e != cudaSuccess) return e;
+    }
+    const long long per = 16LL * wpb;
+    return launch_pdl(kern, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)), dim3(32 * wpb), smem, s, in0, in1,
+                      out, A0, A1, d, L);
+}
+
+template <int K>
+static cudaError_t rhs_x_solve_k(const double* in0, const double* in1, double* out, const double* A0,
+                                 const double* A1, const dim_dev& d, const line_layout& L, cudaStream_t s) {
+    if (d.tw_unit)
+        return in1 ? rhs_x_solve_t<K, true, true>(in0, in1, out, A0, A1, d, L, s)
+                   : rhs_x_solve_t<K, true, false>(in0, in1, out, A0, A1, d, L, s);
+    return in1 ? rhs_x_solve_t<K, false, true>(in0, in1, out, A0, A1, d, L, s)
+               : rhs_x_solve_t<K, false, false>(in0, in1, out, A0, A1, d, L, s);
+}
+
+bool rhs_x_solve_ok(const dim_dev& d, const line_layout& L) {
+    return L.contiguous && d.tw_k >= 1 && d.tw_k <= 4 && d.tw_k == d.p && d.tw_lmul != nullptr &&
+           twisted_staged_smem_per_warp(d.n) <= 227 * 1024;
+}
+
+cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out, const double* A0, const double* A1,
+                               const dim_dev& d, const line_layout& L, cudaStream_t s) {
+    if (!rhs_x_solve_ok(d, L)) return cudaErrorInvalidValue;
+    if (L.nlines <= 0) return cudaSuccess;
+    switch (d.tw_k) {
+        case 1: return rhs_x_solve_k<1>(in0, in1, out, A0, A1, d, L, s);
+        case 2: return rhs_x_solve_k<2>(in0, in1, out, A0, A1, d, L, s);
+        case 3: return rhs_x_solve_k<3>(in0, in1, out, A0, A1, d, L, s);
+        default: return rhs_x_solve_k<4>(in0, in1, out, A0, A1, d, L, s);
+    }
+}
 
 template <int K, bool UNIT>
 static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, bool staged, cudaStream_t s) {

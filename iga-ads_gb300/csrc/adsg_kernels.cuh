@@ -117,6 +117,13 @@ int batch_max_blocks_per_sm();
 cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double* out0, double* out1,
                              const double* A0, const double* A1, const double* B0, int n_axis,
                              long long stride, long long total, cudaStream_t s);
+// The first pass of a step (out0 = A0 (.) in, out1 = B0 (.) in along the
+// outermost axis) as column sweeps that read every input value once: for an
+// input in pinned host memory, read over the host link while the pass
+// computes.  Same operations in the same order as launch_band_pass; p <= 4.
+bool outer_pass_columns_ok(int p);
+cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, double* out1, const double* A0,
+                                      const double* B0, int n_axis, long long stride, cudaStream_t s);
 
 // nrow = mrow - dt*krow, kdt = -dt*krow for one dimension
 cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* kdt, cudaStream_t s);
@@ -127,6 +134,11 @@ cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout&
                               cudaStream_t s);
 size_t line_solve_smem_per_warp(int n);
 bool line_solve_variant_ok(int variant, const dim_dev& d);
+// x band pass (out = A0 (.) in0 [+ A1 (.) in1]) fused with the two-ended x
+// solve on contiguous lines; out holds the solved lines.
+bool rhs_x_solve_ok(const dim_dev& d, const line_layout& L);
+cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out, const double* A0, const double* A1,
+                               const dim_dev& d, const line_layout& L, cudaStream_t s);
 
 // element-wise sum-factorised quadrature (optional kappa field) -----------
 // g += mu^T (dR/dkappa) u  (gradient of the element operator w.r.t. kappa coefficients)

@@ -153,7 +153,8 @@ int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps);
 #define ADSG_STAGE_SOLVE_Y 4
 #define ADSG_STAGE_SOLVE_Z 5
 #define ADSG_STAGE_RHS_ELEM 6   /* element-wise sum-factorised quadrature */
-#define ADSG_NSTAGES 7
+#define ADSG_STAGE_RHS_SOLVE_X 7 /* x band pass fused with the x solve (adsg_heat_step) */
+#define ADSG_NSTAGES 8
 int adsg_ctx_enable_stage_timers(adsg_ctx* ctx, int enable);
 int adsg_ctx_stage_times(adsg_ctx* ctx, double* ms, long long* launches);
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
@@ -173,6 +174,10 @@ int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants);
  * creation by timing a few steps both ways; ADSG_PDL=0/1 forces it), 0 when
  * not, -1 for a NULL context.  Results do not depend on it. */
 int adsg_ctx_launch_pdl(const adsg_ctx* ctx);
+/* 1 when adsg_heat_step fuses the x band pass into the x solve (possible when
+ * x uses solve variant 5; chosen at creation by timing, ADSG_FUSE_X=0/1
+ * forces it), 0 when not, -1 for a NULL context.  Results do not depend on it. */
+int adsg_ctx_fused_x(const adsg_ctx* ctx);
 
 /* ---- host-buffer entry points (the reference-facing boundary) ------------- */
 

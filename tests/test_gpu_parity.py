@@ -337,23 +337,29 @@ def test_failure_detection_counts_nonfinite(cuda):
     assert ctx.count_nonfinite(v) > 0
 
 
-@pytest.mark.parametrize("p,elements", [((2, 2, 2), (20, 18, 16)), ((2, 2), (32, 32))])
+@pytest.mark.parametrize("p,elements", [((2, 2, 2), (20, 18, 16)), ((2, 2), (32, 32)), ((4, 3), (30, 20)),
+                                        ((3,), (64,))])
 def test_launch_mode_does_not_change_results(p, elements, cuda, monkeypatch):
     """Programmatic dependent launch only moves when the next kernel's blocks
-    are scheduled: the steps agree bitwise with and without it."""
+    are scheduled, and the fused x pass + x solve computes the band pass in
+    band_pass_kernel's order: the steps agree bitwise in every mode."""
     out = []
-    for mode in ("0", "1"):
-        monkeypatch.setenv("ADSG_PDL", mode)
+    for pdl, fuse in (("0", "0"), ("1", "0"), ("0", "1"), ("1", "1")):
+        monkeypatch.setenv("ADSG_PDL", pdl)
+        monkeypatch.setenv("ADSG_FUSE_X", fuse)
+        monkeypatch.setenv("ADSG_SOLVE_VARIANT", "5")
         dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
         ctx = ads.Context(dims)
-        assert ctx.launch_pdl() == (mode == "1")
+        assert ctx.launch_pdl() == (pdl == "1")
+        assert ctx.fused_x() == (fuse == "1")
         u = np.random.default_rng(3).uniform(-1, 1, ctx.size)
         ctx.heat_steps_host(u, 1e-5, 5)
         r = np.empty_like(u)
         ctx.heat_rhs_host(u, r, 1e-5)
         out.append((u, r))
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    np.testing.assert_array_equal(out[0][1], out[1][1])
+    for u, r in out[1:]:
+        np.testing.assert_array_equal(u, out[0][0])
+        np.testing.assert_array_equal(r, out[0][1])
 
 
 @pytest.mark.parametrize("p,elements", [
@@ -383,3 +389,37 @@ def test_heat_step_against_oracle(p, elements, cuda):
     assert oracle.rel_l2(a.cpu().numpy(), pr.heat_steps(u0, 1e-5, 2)) <= 2 * step_tol(_conds(dims))
     with pytest.raises(RuntimeError, match="overlap"):
         ctx.heat_step(a, a, 1e-5)
+
+
+@pytest.mark.parametrize("p,elements,variant", [
+    ((2, 2, 2), (30, 7, 9), None),
+    ((2, 2, 2), (62, 62, 62), None),
+    ((2, 2, 2), (300, 300, 1), None),     # 3 rows along the outermost axis (shorter than a column segment)
+    ((4, 4, 4), (60, 60, 60), "3"),
+    ((3, 4), (600, 45), None),
+    ((1, 1, 1), (40, 30, 50), None),
+])
+@pytest.mark.parametrize("nsteps", [1, 3])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_entry_reading_pinned_input_is_exact(p, elements, variant, nsteps, pinned, cuda, monkeypatch):
+    """adsg_heat_steps_host: from pinned buffers the first band pass reads the
+    input in host memory directly (column sweeps); from pageable ones the
+    input is copied first.  Either way the result equals the device-resident
+    steps bitwise."""
+    import torch
+
+    if variant:
+        monkeypatch.setenv("ADSG_SOLVE_VARIANT", variant)
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    u0 = np.random.default_rng(5).uniform(-1, 1, ctx.size)
+    if pinned:
+        ht = torch.from_numpy(u0.copy()).pin_memory()
+        h = ht.numpy()
+    else:
+        h = u0.copy()
+    ctx.heat_steps_host(h, 1e-5, nsteps)
+    d = torch.from_numpy(u0).cuda()
+    ctx.heat_steps(d, 1e-5, nsteps)
+    ctx.synchronize()
+    np.testing.assert_array_equal(h, d.cpu().numpy())
