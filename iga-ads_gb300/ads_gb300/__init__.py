@@ -56,6 +56,22 @@ class DimDesc(ctypes.Structure):
     ]
 
 
+class PointForm(ctypes.Structure):
+    """adsg_point_form (include/ads_gb300.h): constants plus optional
+    per-Gauss-point fields (device addresses) of A u v + B grad u.grad v + G v + D."""
+
+    _fields_ = [
+        ("alpha", ctypes.c_double),
+        ("beta", ctypes.c_double),
+        ("gamma", ctypes.c_double),
+        ("delta", ctypes.c_double),
+        ("alpha_q", ctypes.c_void_p),
+        ("beta_q", ctypes.c_void_p),
+        ("gamma_q", ctypes.c_void_p),
+        ("delta_q", ctypes.c_void_p),
+    ]
+
+
 _lib = None
 
 
@@ -87,6 +103,7 @@ def library() -> ctypes.CDLL:
         "adsg_ads_solve": (i, [vp, vp, vp]),
         "adsg_ads_solve_t": (i, [vp, vp]),
         "adsg_heat_step": (i, [vp, vp, vp, d]),
+        "adsg_form_rhs": (i, [vp, vp, ctypes.POINTER(PointForm), vp]),
         "adsg_heat_steps": (i, [vp, vp, d, i]),
         "adsg_heat_steps_host": (i, [vp, _c_double_p, d, i]),
         "adsg_ads_solve_host": (i, [vp, _c_double_p]),
@@ -322,6 +339,15 @@ class Context:
 
     def ads_solve_t(self, rhs) -> None:
         _check(library().adsg_ads_solve_t(self._h, _devptr(rhs)))
+
+    def form_rhs(self, u, rhs, alpha: float = 0.0, beta: float = 0.0, gamma: float = 0.0, delta: float = 0.0,
+                 alpha_q=None, beta_q=None, gamma_q=None, delta_q=None) -> None:
+        """rhs = sum_e sum_q w J [A u v + B grad u.grad v + G v + D] with each of
+        A, B, G, D a constant plus an optional Gauss-point field (device tensors
+        in the layout of eval_quad); D enters without a test function."""
+        f = PointForm(float(alpha), float(beta), float(gamma), float(delta), _devptr(alpha_q), _devptr(beta_q),
+                      _devptr(gamma_q), _devptr(delta_q))
+        _check(library().adsg_form_rhs(self._h, _devptr(u), ctypes.byref(f), _devptr(rhs)))
 
     def heat_step(self, u_prev, u_next, dt: float) -> None:
         """One explicit step u_next = M^-1 R u_prev (heat_3d::step)."""

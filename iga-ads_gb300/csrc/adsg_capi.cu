@@ -1057,6 +1057,32 @@ int adsg_ads_solve_t(adsg_ctx* ctx, double* rhs_dev) {
     return enqueue_solve(ctx, rhs_dev, 1);
 }
 
+int adsg_form_rhs(adsg_ctx* ctx, const double* u_dev, const adsg_point_form* form, double* rhs_dev) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!form) return fail(-3, "form is NULL");
+    if (!rhs_dev) return fail(-4, "rhs is NULL");
+    const bool needs_u = form->alpha != 0.0 || form->beta != 0.0 || form->alpha_q || form->beta_q;
+    if (needs_u && !u_dev) return fail(-2, "u is NULL but the form has u terms");
+    if (ctx->ndim < 2) return fail(ADSG_ERR_UNSUPPORTED, "forms need a 2D or 3D context");
+    for (int d = 0; d < ctx->ndim; ++d)
+        if (ctx->dims[d].p != ctx->dims[0].p || ctx->dims[d].q != ctx->dims[d].p + 1 || ctx->dims[d].p > 4)
+            return fail(ADSG_ERR_UNSUPPORTED, "forms need the same degree p <= 4 and p+1 Gauss points in every direction");
+    point_form F;
+    F.alpha = form->alpha;
+    F.beta = form->beta;
+    F.gamma = form->gamma;
+    F.delta = form->delta;
+    F.alpha_q = form->alpha_q;
+    F.beta_q = form->beta_q;
+    F.gamma_q = form->gamma_q;
+    F.delta_q = form->delta_q;
+    ADSG_CUDA_TRY(cudaMemsetAsync(rhs_dev, 0, sizeof(double) * ctx->size, ctx->stream), "memset");
+    stage_scope sc(ctx, ADSG_STAGE_RHS_ELEM);
+    ADSG_CUDA_TRY(launch_form_elem(ctx->ndim, ctx->dims, needs_u ? u_dev : nullptr, F, rhs_dev, ctx->stream),
+                  "form rhs");
+    return 0;
+}
+
 int adsg_heat_step(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, double dt) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!u_prev_dev) return fail(-2, "u_prev is NULL");

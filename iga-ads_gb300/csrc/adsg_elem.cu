@@ -35,10 +35,12 @@ constexpr int warps_for() {
     return sizeof(S) * 4 <= 48 * 1024 ? 4 : (sizeof(S) * 3 <= 48 * 1024 ? 3 : (sizeof(S) * 2 <= 48 * 1024 ? 2 : 1));
 }
 
-template <int P, int Q, int kWarpsPerBlock = warps_for<elem3_smem<P + 1, Q>>()>
+// FORM: the general pointwise form of point_form (kappa and dt unused).
+template <int P, int Q, bool FORM = false, int kWarpsPerBlock = warps_for<elem3_smem<P + 1, Q>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem3_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
-                 dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt) {
+                 dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt,
+                 point_form F) {
     constexpr int N = P + 1;
     __shared__ elem3_smem<N, Q> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
@@ -57,7 +59,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     for (int t = lane; t < N * N * N; t += 32) {
         const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
         const long long g = (f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az);
-        S.c[t] = u[g];
+        S.c[t] = u ? u[g] : 0.0;
         S.kc[t] = kappa ? kappa[g] : 0.0;
     }
     for (int t = lane; t < Q * N; t += 32) {
@@ -109,7 +111,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     }
     __syncwarp();
     // z + pointwise form: f = W u, g* = -dt kappa W d*u
+    // (FORM: f = W (alpha u + gamma), g* = W beta d*u, and W delta summed)
     const double J = X.jac[e[0]] * Y.jac[e[1]] * Z.jac[e[2]];
+    double dsum = 0.0;
     for (int t = lane; t < Q * Q * Q; t += 32) {
         const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
         double uv = 0.0, ux = 0.0, uy = 0.0, uz = 0.0, kv = 0.0;
@@ -124,11 +128,31 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             if (kappa) kv = fma(bz, S.K1[src], kv);
         }
         const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * J;
-        const double g = (kappa ? -dt * kv : -dt) * W;
-        S.f[t] = uv * W;
-        S.gx[t] = ux * g;
-        S.gy[t] = uy * g;
-        S.gz[t] = uz * g;
+        if (FORM) {
+            const long long Qx = static_cast<long long>(X.elements) * Q, Qy = static_cast<long long>(Y.elements) * Q;
+            const long long pq = (static_cast<long long>(e[0]) * Q + qx) +
+                                 Qx * ((static_cast<long long>(e[1]) * Q + qy) + Qy * (static_cast<long long>(e[2]) * Q + qz));
+            const double al = F.alpha + (F.alpha_q ? F.alpha_q[pq] : 0.0);
+            const double be = F.beta + (F.beta_q ? F.beta_q[pq] : 0.0);
+            const double ga = F.gamma + (F.gamma_q ? F.gamma_q[pq] : 0.0);
+            const double de = F.delta + (F.delta_q ? F.delta_q[pq] : 0.0);
+            const double g = be * W;
+            S.f[t] = fma(al, uv, ga) * W;
+            S.gx[t] = ux * g;
+            S.gy[t] = uy * g;
+            S.gz[t] = uz * g;
+            dsum = fma(de, W, dsum);
+        } else {
+            const double g = (kappa ? -dt * kv : -dt) * W;
+            S.f[t] = uv * W;
+            S.gx[t] = ux * g;
+            S.gy[t] = uy * g;
+            S.gz[t] = uz * g;
+        }
+    }
+    if (FORM) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
     }
     __syncwarp();
     // z back: V00 <- S0[az][qy][qx], V01 <- Sx, V10 <- Sy
@@ -176,7 +200,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             o = fma(S.dB[0][q * N + ax], S.T1[src], o);
         }
         const long long g = (f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az);
-        rhs[g] += o;
+        rhs[g] += FORM ? o + dsum : o;
     }
 }
 
@@ -188,10 +212,10 @@ struct elem2_smem {
     double f[Q * Q], gx[Q * Q], gy[Q * Q];
 };
 
-template <int P, int Q, int kWarpsPerBlock = warps_for<elem2_smem<P + 1, Q>>()>
+template <int P, int Q, bool FORM = false, int kWarpsPerBlock = warps_for<elem2_smem<P + 1, Q>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem2_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
-                 dim_dev X, dim_dev Y, int cx, int cy, int mx, int my, double dt) {
+                 dim_dev X, dim_dev Y, int cx, int cy, int mx, int my, double dt, point_form F) {
     constexpr int N = P + 1;
     __shared__ elem2_smem<N, Q> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
@@ -206,7 +230,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     const long long nx = X.n;
     for (int t = lane; t < N * N; t += 32) {
         const long long g = (f0 + t % N) + nx * (f1 + t / N);
-        S.c[t] = u[g];
+        S.c[t] = u ? u[g] : 0.0;
         S.kc[t] = kappa ? kappa[g] : 0.0;
     }
     for (int t = lane; t < Q * N; t += 32) {
@@ -234,6 +258,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     }
     __syncwarp();
     const double J = X.jac[e[0]] * Y.jac[e[1]];
+    double dsum = 0.0;
     for (int t = lane; t < Q * Q; t += 32) {
         const int qx = t % Q, qy = t / Q;
         double uv = 0.0, ux = 0.0, uy = 0.0, kv = 0.0;
@@ -246,10 +271,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             if (kappa) kv = fma(by, S.K0[b * Q + qx], kv);
         }
         const double W = X.wq[qx] * Y.wq[qy] * J;
-        const double g = (kappa ? -dt * kv : -dt) * W;
-        S.f[t] = uv * W;
-        S.gx[t] = ux * g;
-        S.gy[t] = uy * g;
+        if (FORM) {
+            const long long Qx = static_cast<long long>(X.elements) * Q;
+            const long long pq = (static_cast<long long>(e[0]) * Q + qx) + Qx * (static_cast<long long>(e[1]) * Q + qy);
+            const double al = F.alpha + (F.alpha_q ? F.alpha_q[pq] : 0.0);
+            const double be = F.beta + (F.beta_q ? F.beta_q[pq] : 0.0);
+            const double ga = F.gamma + (F.gamma_q ? F.gamma_q[pq] : 0.0);
+            const double de = F.delta + (F.delta_q ? F.delta_q[pq] : 0.0);
+            const double g = be * W;
+            S.f[t] = fma(al, uv, ga) * W;
+            S.gx[t] = ux * g;
+            S.gy[t] = uy * g;
+            dsum = fma(de, W, dsum);
+        } else {
+            const double g = (kappa ? -dt * kv : -dt) * W;
+            S.f[t] = uv * W;
+            S.gx[t] = ux * g;
+            S.gy[t] = uy * g;
+        }
+    }
+    if (FORM) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
     }
     __syncwarp();
     // y back: T0 <- S0[ay][qx], T1 <- Sx
@@ -275,7 +318,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             o = fma(S.B[0][q * N + ax], S.T0[ay * Q + q], o);
             o = fma(S.dB[0][q * N + ax], S.T1[ay * Q + q], o);
         }
-        rhs[(f0 + ax) + nx * (f1 + ay)] += o;
+        rhs[(f0 + ax) + nx * (f1 + ay)] += FORM ? o + dsum : o;
     }
 }
 
@@ -471,6 +514,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     }
     __syncwarp();
     const double J = X.jac[e[0]] * Y.jac[e[1]];
+    double dsum = 0.0;
     for (int t = lane; t < Q * Q; t += 32) {
         const int qx = t % Q, qy = t / Q;
         double ux = 0.0, uy = 0.0, mx_ = 0.0, my_ = 0.0;
@@ -505,9 +549,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 
 int colour_count(int E, int c, int N) { return E > c ? (E - c + N - 1) / N : 0; }
 
-template <int P>
+template <int P, bool FORM>
 cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* kappa, double* rhs, double dt,
-                   cudaStream_t s) {
+                   const point_form& F, cudaStream_t s) {
     constexpr int N = P + 1, Q = P + 1;
     constexpr int W3 = warps_for<elem3_smem<N, Q>>();
     constexpr int W2 = warps_for<elem2_smem<N, Q>>();
@@ -520,8 +564,8 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                     const long long work = static_cast<long long>(mx) * my * mz;
                     if (!work) continue;
                     const long long blocks = (work + W3 - 1) / W3;
-                    elem3_kernel<P, Q><<<blocks, 32 * W3, 0, s>>>(u, kappa, rhs, d[0], d[1], d[2], cx, cy,
-                                                                             cz, mx, my, mz, dt);
+                    elem3_kernel<P, Q, FORM><<<blocks, 32 * W3, 0, s>>>(u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz,
+                                                                         mx, my, mz, dt, F);
                 }
     } else {
         for (int cx = 0; cx < N; ++cx)
@@ -530,7 +574,7 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                 const long long work = static_cast<long long>(mx) * my;
                 if (!work) continue;
                 const long long blocks = (work + W2 - 1) / W2;
-                elem2_kernel<P, Q><<<blocks, 32 * W2, 0, s>>>(u, kappa, rhs, d[0], d[1], cx, cy, mx, my, dt);
+                elem2_kernel<P, Q, FORM><<<blocks, 32 * W2, 0, s>>>(u, kappa, rhs, d[0], d[1], cx, cy, mx, my, dt, F);
             }
     }
     return cudaGetLastError();
@@ -588,11 +632,27 @@ cudaError_t launch_rhs_elem(int ndim, const dim_dev* dims, const double* u_prev,
     const int p = dims[0].p;
     for (int d = 0; d < ndim; ++d)
         if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    const point_form none;
     switch (p) {
-        case 1: return elem_p<1>(ndim, dims, u_prev, kappa, rhs, dt, s);
-        case 2: return elem_p<2>(ndim, dims, u_prev, kappa, rhs, dt, s);
-        case 3: return elem_p<3>(ndim, dims, u_prev, kappa, rhs, dt, s);
-        case 4: return elem_p<4>(ndim, dims, u_prev, kappa, rhs, dt, s);
+        case 1: return elem_p<1, false>(ndim, dims, u_prev, kappa, rhs, dt, none, s);
+        case 2: return elem_p<2, false>(ndim, dims, u_prev, kappa, rhs, dt, none, s);
+        case 3: return elem_p<3, false>(ndim, dims, u_prev, kappa, rhs, dt, none, s);
+        case 4: return elem_p<4, false>(ndim, dims, u_prev, kappa, rhs, dt, none, s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+cudaError_t launch_form_elem(int ndim, const dim_dev* dims, const double* u, const point_form& F, double* rhs,
+                             cudaStream_t s) {
+    if (ndim < 2) return cudaErrorNotSupported;
+    const int p = dims[0].p;
+    for (int d = 0; d < ndim; ++d)
+        if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    switch (p) {
+        case 1: return elem_p<1, true>(ndim, dims, u, nullptr, rhs, 0.0, F, s);
+        case 2: return elem_p<2, true>(ndim, dims, u, nullptr, rhs, 0.0, F, s);
+        case 3: return elem_p<3, true>(ndim, dims, u, nullptr, rhs, 0.0, F, s);
+        case 4: return elem_p<4, true>(ndim, dims, u, nullptr, rhs, 0.0, F, s);
         default: return cudaErrorNotSupported;
     }
 }

@@ -140,6 +140,22 @@ bool rhs_x_solve_ok(const dim_dev& d, const line_layout& L);
 cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out, const double* A0, const double* A1,
                                const dim_dev& d, const line_layout& L, cudaStream_t s);
 
+// General pointwise form of the element quadrature: per Gauss point, a
+// constant plus an optional field (Gauss-grid layout, x-fastest over
+// e_d * q + k_d) for each coefficient of
+//     rhs_a = sum_e sum_q w J [alpha u v_a + beta grad u . grad v_a + gamma v_a + delta]
+// where delta is added to every dof of the element (no test function).
+struct point_form {
+    double alpha = 0.0, beta = 0.0, gamma = 0.0, delta = 0.0;
+    const double* alpha_q = nullptr;
+    const double* beta_q = nullptr;
+    const double* gamma_q = nullptr;
+    const double* delta_q = nullptr;
+};
+// rhs += the form applied to u (u may be NULL when alpha = beta = 0)
+cudaError_t launch_form_elem(int ndim, const dim_dev* dims, const double* u, const point_form& F, double* rhs,
+                             cudaStream_t s);
+
 // element-wise sum-factorised quadrature (optional kappa field) -----------
 // g += mu^T (dR/dkappa) u  (gradient of the element operator w.r.t. kappa coefficients)
 cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,

@@ -201,6 +201,28 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
                  const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
                  int* info);
 
+/* ---- general pointwise forms (the other problems' compute_rhs) -------------
+ * rhs_a = sum_e sum_q w_q J_e [ A u v_a + B grad u . grad v_a + G v_a + D ]
+ * where each of A, B, G, D is a constant plus an optional per-point field
+ * (device, the Gauss-point layout of adsg_eval_quad; NULL = none) and D is
+ * added to every dof of the element without a test function.  Covers:
+ *  - heat_3d::compute_rhs (heat_3d.hpp:49-67): A = 1, B = -dt;
+ *  - scalability_3d::compute_rhs (scalability/test3d.hpp:66-95): A = 1,
+ *    B = -dt, D_q = dt f(x_q) (the reference adds its forcing this way);
+ *  - flow::compute_rhs (flow/flow.hpp:77-98): A = 1,
+ *    B_q = -dt k(x_q) exp(mi u(x_q)), G_q = dt h(x_q, t), with u(x_q) from
+ *    adsg_eval_quad and x_q from adsg_quad_points.
+ * u_dev may be NULL when A and B are zero (a pure load).  2D and 3D, the
+ * same degree and q = p + 1 in every direction.  rhs_dev is overwritten. */
+typedef struct adsg_point_form {
+    double alpha, beta, gamma, delta;
+    const double* alpha_q;
+    const double* beta_q;
+    const double* gamma_q;
+    const double* delta_q;
+} adsg_point_form;
+int adsg_form_rhs(adsg_ctx* ctx, const double* u_dev, const adsg_point_form* form, double* rhs_dev);
+
 /* ---- Gauss-point utilities: projection, norms, errors -----------------------
  * Point tensors are x-fastest over the Gauss points of all elements of every
  * direction: point (rx, ry, rz) with rd = e_d * q_d + k_d.

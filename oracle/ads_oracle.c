@@ -578,6 +578,73 @@ int orc_heat_rhs_kappa(const orc_problem* pr, const double* u_prev, const double
     return heat_rhs_seq(pr, u_prev, kappa, rhs, dt);
 }
 
+/* ------------------------------------------------------------------------ */
+/* General pointwise form of the element loop, the pattern the reference's  */
+/* other problems share: scalability_3d::compute_rhs (examples/scalability/ */
+/* test3d.hpp:66-95: val = u v - dt (grad u . grad v - f(x)), the forcing   */
+/* added without a test function) and flow::compute_rhs (examples/flow/     */
+/* flow.hpp:77-98: (u v + dt (-k e^{mi u} grad u . grad v + h v)) w J).     */
+/* Per Gauss point: val = A u v + B grad u . grad v + G v + D, each of A, B, */
+/* G, D a constant plus an optional point field (Gauss grid, x fastest over  */
+/* e_d q + k_d).  2D and 3D; loops in the reference's order.                */
+/* ------------------------------------------------------------------------ */
+static double pf(double c, const double* f, long pq) { return f ? c + f[pq] : c; }
+
+int orc_form_rhs(const orc_problem* pr, const double* u, const double* cst, const double* aq, const double* bq,
+                 const double* gq, const double* dq, double* rhs) {
+    if (pr->ndim < 2) return -1;
+    memset(rhs, 0, sizeof(double) * pr->size);
+    const orc_dim* X = &pr->d[0];
+    const orc_dim* Y = &pr->d[1];
+    const orc_dim* Z = pr->ndim == 3 ? &pr->d[2] : NULL;
+    const long nx = X->n, ny = Y->n;
+    const long Qx = (long)X->elements * X->q, Qy = (long)Y->elements * Y->q;
+    const int ez_n = Z ? Z->elements : 1, qz_n = Z ? Z->q : 1, pz = Z ? Z->p : 0;
+    for (int ex = 0; ex < X->elements; ++ex)
+        for (int ey = 0; ey < Y->elements; ++ey)
+            for (int ez = 0; ez < ez_n; ++ez) {
+                const int fx = X->first_dofs[ex], fy = Y->first_dofs[ey], fz = Z ? Z->first_dofs[ez] : 0;
+                const double J = X->J[ex] * Y->J[ey] * (Z ? Z->J[ez] : 1.0);
+                for (int qx = 0; qx < X->q; ++qx)
+                    for (int qy = 0; qy < Y->q; ++qy)
+                        for (int qz = 0; qz < qz_n; ++qz) {
+                            const double w = X->w[qx] * Y->w[qy] * (Z ? Z->w[qz] : 1.0);
+                            const long pq = ((long)ex * X->q + qx) +
+                                            Qx * (((long)ey * Y->q + qy) + Qy * ((long)ez * qz_n + qz));
+                            const double A = pf(cst[0], aq, pq), B = pf(cst[1], bq, pq), G = pf(cst[2], gq, pq),
+                                         D = pf(cst[3], dq, pq);
+                            double uv = 0, ux = 0, uy = 0, uz = 0;
+                            if (u)
+                                for (int bx = 0; bx <= X->p; ++bx)
+                                    for (int by = 0; by <= Y->p; ++by)
+                                        for (int bz = 0; bz <= pz; ++bz) {
+                                            const long g = (fx + bx) + nx * ((fy + by) + ny * (long)(fz + bz));
+                                            const double B1 = BT(X, ex, qx, 0, bx), B2 = BT(Y, ey, qy, 0, by);
+                                            const double dB1 = BT(X, ex, qx, 1, bx), dB2 = BT(Y, ey, qy, 1, by);
+                                            const double B3 = Z ? BT(Z, ez, qz, 0, bz) : 1.0;
+                                            const double dB3 = Z ? BT(Z, ez, qz, 1, bz) : 0.0;
+                                            uv += u[g] * (B1 * B2 * B3);
+                                            ux += u[g] * (dB1 * B2 * B3);
+                                            uy += u[g] * (B1 * dB2 * B3);
+                                            uz += u[g] * (B1 * B2 * dB3);
+                                        }
+                            for (int ax = 0; ax <= X->p; ++ax)
+                                for (int ay = 0; ay <= Y->p; ++ay)
+                                    for (int az = 0; az <= pz; ++az) {
+                                        const double B1 = BT(X, ex, qx, 0, ax), B2 = BT(Y, ey, qy, 0, ay);
+                                        const double dB1 = BT(X, ex, qx, 1, ax), dB2 = BT(Y, ey, qy, 1, ay);
+                                        const double B3 = Z ? BT(Z, ez, qz, 0, az) : 1.0;
+                                        const double dB3 = Z ? BT(Z, ez, qz, 1, az) : 0.0;
+                                        const double v = B1 * B2 * B3;
+                                        const double gp = ux * (dB1 * B2 * B3) + uy * (B1 * dB2 * B3) + uz * (B1 * B2 * dB3);
+                                        const double val = A * uv * v + B * gp + G * v + D;
+                                        rhs[(fx + ax) + nx * ((fy + ay) + ny * (long)(fz + az))] += val * w * J;
+                                    }
+                        }
+            }
+    return 0;
+}
+
 /* ---- executor stand-in: for_each over elements + synchronized scatter ---- */
 typedef struct {
     const orc_problem* pr;

@@ -84,6 +84,12 @@ int orc_heat_rhs_mt(const orc_problem* pr, const double* u_prev, double* rhs, do
  * Reduces to orc_heat_rhs for kappa == 1. */
 int orc_heat_rhs_kappa(const orc_problem* pr, const double* u_prev, const double* kappa,
                        double* rhs, double dt);
+/* General pointwise form (scalability test3d.hpp:66-95, flow.hpp:77-98):
+ * rhs_a = sum_e sum_q w J [A u v_a + B grad u . grad v_a + G v_a + D], with
+ * cst = {A, B, G, D} constants and aq..dq optional Gauss-point fields added
+ * to them (NULL = none).  u may be NULL (then the u terms vanish).  2D/3D. */
+int orc_form_rhs(const orc_problem* pr, const double* u, const double* cst, const double* aq, const double* bq,
+                 const double* gq, const double* dq, double* rhs);
 
 /* Adjoint support (no reference counterpart): g += mu^T (dR/dkappa) u, i.e.
  * g_c += -dt sum_e sum_q w J B_c(x_q) grad u . grad mu at the quadrature points. */

@@ -48,6 +48,7 @@ def lib() -> ctypes.CDLL:
         L.orc_heat_steps.argtypes = [vp, _dp, d, i, i]
         L.orc_projection_sin.argtypes = [vp, _dp]
         L.orc_kappa_grad.argtypes = [vp, _dp, _dp, _dp, d]
+        L.orc_form_rhs.argtypes = [vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_gauss.argtypes = [i, _dp, _dp]
         L.orc_dgbtrf.argtypes = [i, i, i, _dp, i, _ip]
         L.orc_dgbtrs.argtypes = [ctypes.c_char, i, i, i, i, _dp, i, _ip, _dp, i]
@@ -128,6 +129,17 @@ class Problem:
         lib().orc_kappa_grad(self._h, dp(np.ascontiguousarray(u, np.float64)), dp(np.ascontiguousarray(mu, np.float64)),
                              dp(g), dt)
         return g
+
+    def form_rhs(self, u, alpha=0.0, beta=0.0, gamma=0.0, delta=0.0, alpha_q=None, beta_q=None, gamma_q=None,
+                 delta_q=None):
+        """General pointwise form of the element loop (orc_form_rhs)."""
+        fields = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (alpha_q, beta_q, gamma_q, delta_q)]
+        uu = None if u is None else np.ascontiguousarray(u, np.float64)
+        cst = np.array([alpha, beta, gamma, delta], np.float64)
+        rhs = np.zeros(self.size)
+        lib().orc_form_rhs(self._h, None if uu is None else dp(uu), dp(cst),
+                           *[None if f is None else dp(f) for f in fields], dp(rhs))
+        return rhs
 
     def kappa_step(self, u, kappa, dt):
         """One step of the kappa-weighted scheme: M^{-1} R(kappa) u."""

@@ -24,6 +24,12 @@
 #include "heat/heat_3d.hpp"
 #undef private
 
+// The reference's flow environment (random channel paths, mt19937-seeded) is
+// header-only; its flow.hpp include is skipped (the flow class needs Galois).
+#define FLOW_FLOW_HPP
+#include "flow/environment.hpp"
+#undef FLOW_FLOW_HPP
+
 namespace {
 
 // 3D heat step in the executor form of heat_2d.hpp:166-192 /
@@ -110,6 +116,87 @@ public:
         std::swap(u, u_prev);
         compute_rhs();
         solve(u);
+    }
+};
+
+// scalability_3d::compute_rhs (examples/scalability/test3d.hpp:66-95) and
+// flow::compute_rhs (examples/flow/flow.hpp:77-98), loop for loop, on the
+// reference's own simulation_3d helpers with its sequential_executor in place
+// of galois_executor; forcing terms as test3d.hpp:56-63 and flow.hpp:128-132.
+class forms3_driver : public ads::simulation_3d {
+public:
+    vector_type u, u_prev;
+    ads::sequential_executor executor;
+    ads::problems::environment env{1};
+
+    explicit forms3_driver(const ads::config_3d& c)
+    : simulation_3d{c}
+    , u{shape()}
+    , u_prev{shape()} { }
+
+    double scal_forcing(double x, double y, double z) const {
+        double dx = x - 0.5, dy = y - 0.5, dz = z - 0.5;
+        double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+        return std::exp(-r) + 1 + std::cos(M_PI * x) * std::cos(M_PI * y) * std::cos(M_PI * z);
+    }
+
+    void scalability_rhs() {
+        auto& rhs = u;
+        zero(rhs);
+        executor.for_each(elements(), [&](index_type e) {
+            auto U = element_rhs();
+            double J = jacobian(e);
+            for (auto q : quad_points()) {
+                double w = weight(q);
+                auto x = point(e, q);
+                value_type uu = eval_fun(u_prev, e, q);
+                for (auto a : dofs_on_element(e)) {
+                    auto aa = dof_global_to_local(e, a);
+                    value_type v = eval_basis(e, q, a);
+                    double gradient_prod = grad_dot(uu, v);
+                    double val = uu.val * v.val - steps.dt * (gradient_prod - scal_forcing(x[0], x[1], x[2]));
+                    U(aa[0], aa[1], aa[2]) += val * w * J;
+                }
+            }
+            executor.synchronized([&]() { update_global_rhs(rhs, U, e); });
+        });
+    }
+
+    double flow_forcing(point_type x) const {
+        double pi2 = 2 * M_PI;
+        return 1 + std::sin(pi2 * x[0]) * std::sin(pi2 * x[1]) * std::sin(pi2 * x[2]);
+    }
+
+    // also returns k and u at every Gauss point (x-fastest over e_d q + k_d)
+    void flow_rhs(double* kq, double* uq) {
+        const long Qx = static_cast<long>(x.basis.elements) * x.basis.quad_order;
+        const long Qy = static_cast<long>(y.basis.elements) * y.basis.quad_order;
+        auto& rhs = u;
+        zero(rhs);
+        executor.for_each(elements(), [&](index_type e) {
+            auto U = element_rhs();
+            double J = jacobian(e);
+            for (auto q : quad_points()) {
+                double w = weight(q);
+                auto x = point(e, q);
+                double mi = 10;
+                double k = env.permeability(x[0], x[1], x[2]);
+                value_type uu = eval_fun(u_prev, e, q);
+                double h = flow_forcing(x);
+                const long pq = (static_cast<long>(e[0]) * this->x.basis.quad_order + q[0]) +
+                                Qx * ((static_cast<long>(e[1]) * this->y.basis.quad_order + q[1]) +
+                                      Qy * (static_cast<long>(e[2]) * this->z.basis.quad_order + q[2]));
+                kq[pq] = k;
+                uq[pq] = uu.val;
+                for (auto a : dofs_on_element(e)) {
+                    auto aa = dof_global_to_local(e, a);
+                    value_type v = eval_basis(e, q, a);
+                    double val = -k * std::exp(mi * uu.val) * grad_dot(uu, v) + h * v.val;
+                    U(aa[0], aa[1], aa[2]) += (uu.val * v.val + steps.dt * val) * w * J;
+                }
+            }
+            executor.synchronized([&] { update_global_rhs(rhs, U, e); });
+        });
     }
 };
 
@@ -254,6 +341,22 @@ int ref_heat_rhs(int ndim, int p, int elements, double dt, const double* u_prev,
     } else {
         return -1;
     }
+    return 0;
+}
+
+// scalability_3d's RHS (which = 0) or flow's RHS (which = 1, also filling
+// kq and uq, each of the Gauss-point count) from u_prev.
+int ref_form_rhs(int which, int p, int elements, double dt, const double* u_prev, double* rhs, double* kq,
+                 double* uq) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{1, dt};
+    forms3_driver s{ads::config_3d{dim, dim, dim, steps, 1}};
+    load(s.u_prev, u_prev);
+    if (which == 0)
+        s.scalability_rhs();
+    else
+        s.flow_rhs(kq, uq);
+    store(s.u, rhs);
     return 0;
 }
 

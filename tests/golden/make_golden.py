@@ -11,6 +11,11 @@ ads_solve, lin::factorize/solve_with_factorized).  Initial fields are the
 reference's projection of prod sin(pi x_d) solved by its ads_solve, plus
 SplitMix64 noise (the same generator as ads_gb300.inputs.splitmix_uniform).
 
+The form_* fixtures come from the reference's scalability_3d::compute_rhs
+(examples/scalability/test3d.hpp:66-95) and flow::compute_rhs
+(examples/flow/flow.hpp:77-98, permeability from its own environment class),
+reproduced loop for loop on simulation_3d by oracle/ref_driver.cpp.
+
 The small systems in solver_known_answers are those of the reference tests
 tests/ads/solver_test.cpp:63-255 and tests/ads/lin/band_solve_test.cpp:15-46,
 with the answers those tests expect.
@@ -62,6 +67,7 @@ def load_ref():
     L.ref_heat_steps.argtypes = [i, i, i, d, i, _dp, i]
     L.ref_heat_rhs.argtypes = [i, i, i, d, _dp, _dp]
     L.ref_projection_sin.argtypes = [i, i, i, _dp]
+    L.ref_form_rhs.argtypes = [i, i, i, d, _dp, _dp, _dp, _dp]
     return L
 
 
@@ -201,8 +207,36 @@ CASES = [
 ]
 
 
+def form_case(L, which, p, E, dt, seed):
+    """scalability_3d (which 0) or flow (which 1) compute_rhs from a seeded
+    u_prev; flow also records k and u at every Gauss point."""
+    n = E + p
+    size = n ** 3
+    u0 = (2.0 * splitmix_uniform(seed, size) - 1.0) * (0.05 if which else 1.0)
+    npts = (E * (p + 1)) ** 3
+    rhs, kq, uq = np.zeros(size), np.zeros(npts), np.zeros(npts)
+    L.ref_form_rhs(which, p, E, dt, dp(u0), dp(rhs), dp(kq), dp(uq))
+    xq = tables(L, p, E)["xq"]
+    out = dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), seed=np.int64(seed), u0=u0, rhs=rhs, xq=xq)
+    if which:
+        out.update(kq=kq, uq=uq)
+    return out
+
+
+FORM_CASES = [
+    # (name, which, p, elements, dt, seed)
+    ("form_scalability_p2_e5", 0, 2, 5, 1e-4, 11),
+    ("form_scalability_p3_e4", 0, 3, 4, 1e-4, 12),
+    ("form_flow_p2_e6", 1, 2, 6, 1e-3, 13),
+    ("form_flow_p4_e3", 1, 4, 3, 1e-3, 14),
+]
+
+
 def main():
     L = load_ref()
+    for name, which, p, E, dt, seed in FORM_CASES:
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **form_case(L, which, p, E, dt, seed))
+        print("wrote", name)
     for p, E in [(2, 8), (3, 7), (4, 12), (2, 32), (4, 36)]:
         np.savez_compressed(os.path.join(HERE, f"tables_p{p}_e{E}.npz"), **tables(L, p, E))
     np.savez_compressed(os.path.join(HERE, "solver_known_answers.npz"), **known_answers(L))

@@ -114,7 +114,7 @@ def test_torch_autograd_bridge(cuda):
     kappa = dev["kappa"].clone().requires_grad_(True)
     loss = MassNorm.apply(rollout(u0, kappa), dev["target"], ctx)
     loss.backward()
-    assert abs(float(loss) - loss_ref) <= 1e-14 * abs(loss_ref)
+    assert abs(float(loss.detach()) - loss_ref) <= 1e-14 * abs(loss_ref)
     np.testing.assert_array_equal(u0.grad.cpu().numpy(), gu_ref)
     np.testing.assert_array_equal(kappa.grad.cpu().numpy(), gk_ref)
 

@@ -164,3 +164,35 @@ def test_oracle_adjoint_matches_finite_differences():
         assert abs(fd_u - gu @ d) <= 1e-7 * max(abs(fd_u), 1e-30)
         fd_k = (loss(u0, kappa + h * d) - loss(u0, kappa - h * d)) / (2 * h)
         assert abs(fd_k - gk @ d) <= 1e-6 * max(abs(fd_k), 1e-30)
+
+
+def _grid(xq, E, q):
+    """Gauss-point coordinates of a cube, x-fastest over (rx, ry, rz)."""
+    axis = np.asarray(xq).reshape(E * q)
+    z, y, x = np.meshgrid(axis, axis, axis, indexing="ij")
+    return x.ravel(), y.ravel(), z.ravel()
+
+
+def form_fields(g):
+    """Point fields of a form fixture: scalability (test3d.hpp:56-63, the
+    forcing added without a test function) or flow (flow.hpp:77-98, with the
+    recorded permeability and u at the Gauss points, forcing flow.hpp:128-132)."""
+    p, E, dt = int(g["p"]), int(g["elements"]), float(g["dt"])
+    x, y, z = _grid(g["xq"], E, p + 1)
+    if "kq" not in g:
+        r = np.sqrt((x - 0.5) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2)
+        f = np.exp(-r) + 1 + np.cos(np.pi * x) * np.cos(np.pi * y) * np.cos(np.pi * z)
+        return dict(alpha=1.0, beta=-dt, delta_q=dt * f)
+    h = 1 + np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y) * np.sin(2 * np.pi * z)
+    return dict(alpha=1.0, beta_q=-dt * g["kq"] * np.exp(10.0 * g["uq"]), gamma_q=dt * h)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "form_*.npz"))), ids=os.path.basename)
+def test_form_rhs_matches_reference(path):
+    """The oracle's general pointwise form against the reference's
+    scalability_3d / flow compute_rhs loops."""
+    g = dict(np.load(path))
+    p, E = int(g["p"]), int(g["elements"])
+    pr = oracle.Problem([p] * 3, [E] * 3)
+    got = pr.form_rhs(g["u0"], **form_fields(g))
+    assert oracle.rel_l2(got, g["rhs"]) <= 1e-13
