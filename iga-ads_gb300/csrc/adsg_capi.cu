@@ -46,6 +46,30 @@ std::vector<double> row_band(const adsg_dim_desc& d, int which) {
     return rows;
 }
 
+// The widest range [lo, hi) of rows that are symmetric in both row-format
+// bands (coefficients of columns r-t and r+t equal to 1e-13 of the row's
+// size), grown from the middle row: with uniform open knots every row 2p-1 or
+// more away from the ends is a translate of one symmetric row.  lo = hi when
+// the middle row itself is not symmetric.
+void symmetric_row_range(const std::vector<double>& m, const std::vector<double>& k, int n, int p, int& lo, int& hi) {
+    const int bw = 2 * p + 1;
+    auto sym = [&](int r) {
+        for (const std::vector<double>* rows : {&m, &k}) {
+            const double* row = rows->data() + static_cast<size_t>(r) * bw;
+            double mx = 0.0;
+            for (int t = 0; t < bw; ++t) mx = std::max(mx, std::fabs(row[t]));
+            for (int t = 1; t <= p; ++t)
+                if (!(std::fabs(row[p - t] - row[p + t]) <= 1e-13 * mx)) return false;
+        }
+        return true;
+    };
+    lo = hi = n / 2;
+    if (n < 2 * p + 1 || !sym(n / 2)) return;
+    while (lo > p && sym(lo - 1)) --lo;
+    hi = n / 2 + 1;
+    while (hi < n - p && sym(hi)) ++hi;
+}
+
 bool valid_desc(const adsg_dim_desc& d) {
     if (d.p < 1 || d.p > ADSG_MAX_DEGREE || d.elements < 1 || d.quad_order < 1 || d.n < 1) return false;
     if (!d.btab || !d.w || !d.J || !d.first_dofs || !d.lu || !d.ipiv) return false;
@@ -521,7 +545,7 @@ int enqueue_rhs_with(adsg_ctx* c, const dim_dev* D, const double* u, double* rhs
         if (!outer_done) {
             stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
             ADSG_CUDA_TRY(launch_band_pass(D[1].p, u, nullptr, T[0], T[1], D[1].mrow, nullptr, D[1].nrow, D[1].n, sy,
-                                           total, s),
+                                           total, s, D[1].sym_lo, D[1].sym_hi),
                           "rhs pass y");
         }
         // rhs = (-dt Kx) A + Mx C
@@ -532,13 +556,13 @@ int enqueue_rhs_with(adsg_ctx* c, const dim_dev* D, const double* u, double* rhs
         if (!outer_done) {
             stage_scope s1(c, ADSG_STAGE_RHS_OUTER);
             ADSG_CUDA_TRY(launch_band_pass(D[2].p, u, nullptr, T[0], T[1], D[2].mrow, nullptr, D[2].nrow, D[2].n, sz,
-                                           total, s),
+                                           total, s, D[2].sym_lo, D[2].sym_hi),
                           "rhs pass z");
         }
         // F = (-dt Ky) A + My C,  G = My A
         { stage_scope s2(c, ADSG_STAGE_RHS_MIDDLE);
         ADSG_CUDA_TRY(launch_band_pass(D[1].p, T[0], T[1], T[2], T[3], D[1].kdt, D[1].mrow, D[1].mrow, D[1].n, sy,
-                                       total, s),
+                                       total, s, D[1].sym_lo, D[1].sym_hi),
                       "rhs pass y"); }
         // rhs = (-dt Kx) G + Mx F
         if (int st2 = x_pass(T[3], T[2], D[0].kdt, D[0].mrow)) return st2;
@@ -812,7 +836,7 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
         pdl_scope pdl(c->pdl);
         stage_scope sc(c, ADSG_STAGE_RHS_OUTER);
         ADSG_CUDA_TRY(launch_outer_pass_columns(D[o].p, in_dev, c->scratch[0], c->scratch[1], D[o].mrow, D[o].nrow,
-                                                c->n[o], so, c->stream),
+                                                c->n[o], so, c->stream, D[o].sym_lo, D[o].sym_hi),
                       "rhs pass (outer, from host)");
     } else {
         ADSG_CUDA_TRY(cudaMemcpyAsync(cur, u_in, sizeof(double) * c->size, cudaMemcpyHostToDevice, c->stream), "H2D");
@@ -897,6 +921,7 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         tw_ok[d] = have_tw;
         const std::vector<double> m = row_band(h, 0);
         const std::vector<double> k = row_band(h, 1);
+        symmetric_row_range(m, k, h.n, h.p, D.sym_lo, D.sym_hi);
         const size_t nb = static_cast<size_t>(h.elements) * h.quad_order * 2 * (h.p + 1);
         double *mrow = nullptr, *krow = nullptr, *lmul = nullptr, *ucol = nullptr, *rdiag = nullptr;
         double *btab = nullptr, *wq = nullptr, *jac = nullptr;

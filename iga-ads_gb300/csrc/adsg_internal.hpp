@@ -57,6 +57,7 @@ void scale_twisted(const twisted_tables& t, int n, twisted_tables& out, std::vec
 // Row-format band [n][2p+1] of sum_e sum_q B_a B_b w_q J_e (which: 0 values, 1 derivatives).
 std::vector<double> row_band(const adsg_dim_desc& d, int which);
 bool valid_desc(const adsg_dim_desc& d);
+void symmetric_row_range(const std::vector<double>& m, const std::vector<double>& k, int n, int p, int& lo, int& hi);
 // 0 on success, else the 1-based column of a zero diagonal.
 int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, solve_tables& t);
 

@@ -65,7 +65,14 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 // Threads of a warp take consecutive x, so every neighbour load is coalesced;
 // along y/z the band row is the same for the whole warp (broadcast loads).
 // ---------------------------------------------------------------------------
-template <int P, bool IN1, bool OUT1>
+// SYM (used where a pass has two outputs, OUT1): rows sym_lo .. sym_hi-1 are
+// symmetric (the host finds the range; uniform open knots make every row
+// 2p-1 or more away from the ends a translate of one symmetric row, up to
+// rounding), so the pair sums in(r-t) + in(r+t) are formed once and shared by
+// both outputs, with the left coefficient of each pair: 3p+2 FP64 operations
+// instead of 2(2p+1) for out0/out1 = A0/B0 (.) in0, and 5p+3 instead of
+// 3(2p+1) with a second input.  Other rows take the full band.
+template <int P, bool IN1, bool OUT1, bool SYM = false>
 __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict__ in0,
                                                          const double* __restrict__ in1,
                                                          double* __restrict__ out0,
@@ -73,7 +80,7 @@ __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict
                                                          const double* __restrict__ A0,
                                                          const double* __restrict__ A1,
                                                          const double* __restrict__ B0, int n_axis,
-                                                         long long stride, long long total) {
+                                                         long long stride, long long total, int sym_lo, int sym_hi) {
     constexpr int BW = 2 * P + 1;
     long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (g >= total) return;
@@ -83,6 +90,23 @@ __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict
     const double* a1 = IN1 ? A1 + static_cast<long long>(r) * BW : nullptr;
     const double* b0 = OUT1 ? B0 + static_cast<long long>(r) * BW : nullptr;
     double acc0 = 0.0, acc1 = 0.0;
+    if (SYM && r >= sym_lo && r < sym_hi) {
+        const double c0 = __ldg(in0 + g);
+        acc0 = __ldg(a0 + P) * c0;
+        if (OUT1) acc1 = __ldg(b0 + P) * c0;
+        if (IN1) acc0 = fma(__ldg(a1 + P), __ldg(in1 + g), acc0);
+#pragma unroll
+        for (int t = 1; t <= P; ++t) {
+            const long long off = static_cast<long long>(t) * stride;
+            const double s0 = __ldg(in0 + g - off) + __ldg(in0 + g + off);
+            acc0 = fma(__ldg(a0 + P - t), s0, acc0);
+            if (OUT1) acc1 = fma(__ldg(b0 + P - t), s0, acc1);
+            if (IN1) acc0 = fma(__ldg(a1 + P - t), __ldg(in1 + g - off) + __ldg(in1 + g + off), acc0);
+        }
+        out0[g] = acc0;
+        if (OUT1) out1[g] = acc1;
+        return;
+    }
 #pragma unroll
     for (int t = 0; t < BW; ++t) {
         const int c = r - P + t;
@@ -101,35 +125,49 @@ __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict
 template <int P>
 static cudaError_t band_pass_p(const double* in0, const double* in1, double* out0, double* out1,
                                const double* A0, const double* A1, const double* B0, int n_axis,
-                               long long stride, long long total, cudaStream_t s) {
+                               long long stride, long long total, cudaStream_t s, int lo, int hi) {
     const int threads = 256;
+    const bool sym = hi > lo;
     const dim3 grid(static_cast<unsigned>((total + threads - 1) / threads));
-    if (in1 && out1)
+    if (in1 && out1) {
+        if (sym)
+            return launch_pdl(band_pass_kernel<P, true, true, true>, grid, dim3(threads), 0, s, in0, in1, out0, out1,
+                              A0, A1, B0, n_axis, stride, total, lo, hi);
         return launch_pdl(band_pass_kernel<P, true, true>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
-                          n_axis, stride, total);
+                          n_axis, stride, total, lo, hi);
+    }
     if (in1)
         return launch_pdl(band_pass_kernel<P, true, false>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
-                          n_axis, stride, total);
-    if (out1)
+                          n_axis, stride, total, lo, hi);
+    if (out1) {
+        if (sym)
+            return launch_pdl(band_pass_kernel<P, false, true, true>, grid, dim3(threads), 0, s, in0, in1, out0, out1,
+                              A0, A1, B0, n_axis, stride, total, lo, hi);
         return launch_pdl(band_pass_kernel<P, false, true>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
-                          n_axis, stride, total);
+                          n_axis, stride, total, lo, hi);
+    }
     return launch_pdl(band_pass_kernel<P, false, false>, grid, dim3(threads), 0, s, in0, in1, out0, out1, A0, A1, B0,
-                      n_axis, stride, total);
+                      n_axis, stride, total, lo, hi);
 }
 
 cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double* out0, double* out1,
                              const double* A0, const double* A1, const double* B0, int n_axis,
-                             long long stride, long long total, cudaStream_t s) {
+                             long long stride, long long total, cudaStream_t s, int sym_lo, int sym_hi) {
     if (total <= 0) return cudaSuccess;
+    // a single output gains nothing from pair sums; the range must keep the
+    // pair's rows inside the axis
+    const int lo = std::max(sym_lo, p), hi = std::min(sym_hi, n_axis - p);
+    const bool sym = out1 != nullptr && hi > lo;
+    const int L = sym ? lo : 0, H = sym ? hi : 0;
     switch (p) {
-        case 1: return band_pass_p<1>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 2: return band_pass_p<2>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 3: return band_pass_p<3>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 4: return band_pass_p<4>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 5: return band_pass_p<5>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 6: return band_pass_p<6>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 7: return band_pass_p<7>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
-        case 8: return band_pass_p<8>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s);
+        case 1: return band_pass_p<1>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 2: return band_pass_p<2>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 3: return band_pass_p<3>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 4: return band_pass_p<4>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 5: return band_pass_p<5>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 6: return band_pass_p<6>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 7: return band_pass_p<7>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
+        case 8: return band_pass_p<8>(in0, in1, out0, out1, A0, A1, B0, n_axis, stride, total, s, L, H);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -145,11 +183,11 @@ cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double
 // Per output the operations and their order are band_pass_kernel's
 // (out0 = A0 (.) in, out1 = B0 (.) in), so the results are bitwise equal.
 // ---------------------------------------------------------------------------
-template <int P>
+template <int P, bool SYM>
 __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __restrict__ in, double* __restrict__ out0,
                                                             double* __restrict__ out1, const double* __restrict__ A0,
                                                             const double* __restrict__ B0, int n, long long so,
-                                                            int seg) {
+                                                            int seg, int sym_lo, int sym_hi) {
     constexpr int BW = 2 * P + 1, PRE = 8;
     const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     const long long nseg = (n + seg - 1) / seg;
@@ -169,12 +207,23 @@ __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __rest
         const double* a0 = A0 + static_cast<long long>(r) * BW;
         const double* b0 = B0 + static_cast<long long>(r) * BW;
         double acc0 = 0.0, acc1 = 0.0;
+        if (SYM && r >= sym_lo && r < sym_hi) {  // band_pass_kernel's SYM order
+            acc0 = __ldg(a0 + P) * w[P];
+            acc1 = __ldg(b0 + P) * w[P];
 #pragma unroll
-        for (int q = 0; q < BW; ++q) {
-            const int c = r - P + q;
-            if (c >= 0 && c < n) {
-                acc0 = fma(__ldg(a0 + q), w[q], acc0);
-                acc1 = fma(__ldg(b0 + q), w[q], acc1);
+            for (int t = 1; t <= P; ++t) {
+                const double s0 = w[P - t] + w[P + t];
+                acc0 = fma(__ldg(a0 + P - t), s0, acc0);
+                acc1 = fma(__ldg(b0 + P - t), s0, acc1);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < BW; ++q) {
+                const int c = r - P + q;
+                if (c >= 0 && c < n) {
+                    acc0 = fma(__ldg(a0 + q), w[q], acc0);
+                    acc1 = fma(__ldg(b0 + q), w[q], acc1);
+                }
             }
         }
         out0[col + r * so] = acc0;
@@ -191,7 +240,8 @@ __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __rest
 bool outer_pass_columns_ok(int p) { return p >= 1 && p <= 4; }
 
 cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, double* out1, const double* A0,
-                                      const double* B0, int n_axis, long long stride, cudaStream_t s) {
+                                      const double* B0, int n_axis, long long stride, cudaStream_t s, int sym_lo,
+                                      int sym_hi) {
     if (!outer_pass_columns_ok(p)) return cudaErrorInvalidValue;
     // whole columns (each input read exactly once) unless there are too few
     // columns to give every sub-partition a few warps; segments re-read a
@@ -202,12 +252,20 @@ cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, dou
     const long long threads = stride * ((n_axis + seg - 1) / seg);
     if (threads <= 0) return cudaSuccess;
     const dim3 grid(static_cast<unsigned>((threads + 127) / 128)), block(128);
+    const int lo = std::max(sym_lo, p), hi = std::min(sym_hi, n_axis - p);
+    const bool sym = hi > lo;
+#define ADSG_COLS(P_)                                                                                          \
+    (sym ? launch_pdl(outer_columns_kernel<P_, true>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg, \
+                      lo, hi)                                                                                   \
+         : launch_pdl(outer_columns_kernel<P_, false>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg, \
+                      0, 0))
     switch (p) {
-        case 1: return launch_pdl(outer_columns_kernel<1>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
-        case 2: return launch_pdl(outer_columns_kernel<2>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
-        case 3: return launch_pdl(outer_columns_kernel<3>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
-        default: return launch_pdl(outer_columns_kernel<4>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg);
+        case 1: return ADSG_COLS(1);
+        case 2: return ADSG_COLS(2);
+        case 3: return ADSG_COLS(3);
+        default: return ADSG_COLS(4);
     }
+#undef ADSG_COLS
 }
 
 __global__ void dt_bands_kernel(const double* __restrict__ mrow, const double* __restrict__ krow,

@@ -49,6 +49,7 @@ struct dim_dev {
     // rows [tw_n1, n) chain 1 in reverse order; tables per chain, stride tw_rows.
     int tw_k = 0, tw_n1 = 0, tw_n2 = 0, tw_rows = 0;
     int tw_unit = 0;  // tables of the row-scaled system (unit upper diagonal)
+    int sym_lo = 0, sym_hi = 0;  // rows [sym_lo, sym_hi) of the M and K bands are symmetric (pair sums allowed)
     const double* tw_lmul = nullptr;   // [2][tw_rows][k] multipliers of chain-local column j
     const double* tw_ucol = nullptr;   // [2][tw_rows][k] U(j-d, j), d = 1..k
     const double* tw_rdiag = nullptr;  // [2][tw_rows] 1 / U(j, j)
@@ -113,17 +114,20 @@ int batch_max_blocks_per_sm();
 
 // rhs passes -------------------------------------------------------------
 // out0 = A0 (.) in0 [+ A1 (.) in1],  out1 = B0 (.) in0  along one axis, where
-// (.) applies a band with rows of 2p+1 coefficients.
+// (.) applies a band with rows of 2p+1 coefficients.  Rows sym_lo .. sym_hi-1
+// of every band are symmetric (dim_dev::sym_lo/hi; an empty range for none),
+// so a two-output pass may share pair sums between its outputs there.
 cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double* out0, double* out1,
                              const double* A0, const double* A1, const double* B0, int n_axis,
-                             long long stride, long long total, cudaStream_t s);
+                             long long stride, long long total, cudaStream_t s, int sym_lo = 0, int sym_hi = 0);
 // The first pass of a step (out0 = A0 (.) in, out1 = B0 (.) in along the
 // outermost axis) as column sweeps that read every input value once: for an
 // input in pinned host memory, read over the host link while the pass
 // computes.  Same operations in the same order as launch_band_pass; p <= 4.
 bool outer_pass_columns_ok(int p);
 cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, double* out1, const double* A0,
-                                      const double* B0, int n_axis, long long stride, cudaStream_t s);
+                                      const double* B0, int n_axis, long long stride, cudaStream_t s, int sym_lo,
+                                      int sym_hi);
 
 // nrow = mrow - dt*krow, kdt = -dt*krow for one dimension
 cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* kdt, cudaStream_t s);
