@@ -392,6 +392,9 @@ def run_ours(args, cfg):
             "traffic": profiled_traffic(dom, size),
             "peak_source": "cuBLAS DGEMM 4096^3 measured live in bench.py (GB300 FP64 is not in "
                            "MEASURED_PEAKS.json)",
+            "flop_convention": "FP64 operations of the implemented algorithm (pair sums on symmetric band rows, "
+                               "unit-diagonal two-ended sweeps), 2 flops per FMA, multiply or add: each takes "
+                               "one DFMA issue slot, so frac reads as FP64 pipe utilisation against DGEMM",
             "algorithmic_bytes_per_launch": work[dom][1], "hbm_gbs": d["gbs"],
             "hbm_frac_of_measured": d["gbs"] / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None}
     step_flops = sum(work[k][0] * per_stage[k]["launches"] for k in per_stage) / args.steps

@@ -1201,36 +1201,63 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
     if (!bytes) return fail(-3, "bytes is NULL");
     for (int i = 0; i < ADSG_NSTAGES; ++i) flops[i] = bytes[i] = 0.0;
     const double total = static_cast<double>(ctx->size);
-    // in-band terms of one matvec along dimension d, per output, on average
-    auto terms = [&](int d) {
-        const double n = ctx->dims[d].n, p = ctx->dims[d].p;
-        const double inband = n * (2 * p + 1) - p * (p + 1);
-        return inband / n;
+    // FP64 operations of the algorithm each step kernel implements (the
+    // step's view, sdims), each counted as 2 flops: an add or a multiply
+    // takes a DFMA issue slot like an FMA, so the rate compares with the
+    // DGEMM roof as pipe utilisation.
+    const dim_dev* S = ctx->sdims;
+    // one band pass along direction d with `outs` outputs and `ins` inputs:
+    // full band rows take ins*outs... FMAs per in-band term; symmetric rows
+    // (two outputs) take the pair-sum form
+    auto pass_ops = [&](int d, int products, bool pair_form) {
+        const int n = S[d].n, p = S[d].p;
+        const int lo = std::max(S[d].sym_lo, p), hi = std::min(S[d].sym_hi, n - p);
+        double ops = 0.0;
+        for (int r = 0; r < n; ++r) {
+            const int inband = std::min(n - 1, r + p) - std::max(0, r - p) + 1;
+            if (pair_form && r >= lo && r < hi)
+                ops += products == 2 ? 3.0 * p + 2 : 5.0 * p + 3;  // p (2p) adds, 2 (3) centre terms, 2p (3p) FMAs
+            else
+                ops += static_cast<double>(products) * inband;
+        }
+        return ops / n * total;  // rows are equally populated
     };
     if (ctx->ndim == 3) {
-        flops[ADSG_STAGE_RHS_OUTER] = 2.0 * total * 2 * terms(2);  // Mz, Nz
+        flops[ADSG_STAGE_RHS_OUTER] = 2.0 * pass_ops(2, 2, true);  // Mz, Nz
         bytes[ADSG_STAGE_RHS_OUTER] = 8.0 * total * 3;
-        flops[ADSG_STAGE_RHS_MIDDLE] = 2.0 * total * 3 * terms(1);  // -dtKy, My (F); My (G)
+        flops[ADSG_STAGE_RHS_MIDDLE] = 2.0 * pass_ops(1, 3, true);  // -dtKy, My (F); My (G)
         bytes[ADSG_STAGE_RHS_MIDDLE] = 8.0 * total * 4;
-        flops[ADSG_STAGE_RHS_X] = 2.0 * total * 2 * terms(0);
+        flops[ADSG_STAGE_RHS_X] = 2.0 * pass_ops(0, 2, false);
         bytes[ADSG_STAGE_RHS_X] = 8.0 * total * 3;
     } else if (ctx->ndim == 2) {
-        flops[ADSG_STAGE_RHS_OUTER] = 2.0 * total * 2 * terms(1);
+        flops[ADSG_STAGE_RHS_OUTER] = 2.0 * pass_ops(1, 2, true);
         bytes[ADSG_STAGE_RHS_OUTER] = 8.0 * total * 3;
-        flops[ADSG_STAGE_RHS_X] = 2.0 * total * 2 * terms(0);
+        flops[ADSG_STAGE_RHS_X] = 2.0 * pass_ops(0, 2, false);
         bytes[ADSG_STAGE_RHS_X] = 8.0 * total * 3;
     } else {
-        flops[ADSG_STAGE_RHS_X] = 2.0 * total * terms(0);
+        flops[ADSG_STAGE_RHS_X] = 2.0 * pass_ops(0, 1, false);
         bytes[ADSG_STAGE_RHS_X] = 8.0 * total * 2;
     }
     for (int d = 0; d < ctx->ndim; ++d) {
-        // per line: forward sum_j min(kl, n-1-j) FMAs, backward sum_j (uext_j FMAs + 1 multiply)
-        const int n = ctx->dims[d].n;
+        const dim_dev& D = S[d];
+        const int n = D.n;
         const double lines = total / n;
-        double fma = 0.0;
-        for (int j = 0; j + 1 < n; ++j) fma += std::min(ctx->dims[d].kl, n - 1 - j);
-        fma += ctx->uext_sum[d];
-        flops[ADSG_STAGE_SOLVE_X + d] = lines * (2.0 * fma + n);
+        double ops = 0.0;
+        if (solve_variant_twisted(D.solve_variant) && D.tw_k > 0) {
+            // two chains: forward min(k, nc-1-j) FMAs, backward min(k, j) FMAs
+            // (+1 multiply unless unit-diagonal), 2k^2 FMAs each at the meeting
+            const int k = D.tw_k;
+            for (int nc : {D.tw_n1, D.tw_n2}) {
+                for (int j = 0; j < nc; ++j) ops += std::min(k, nc - 1 - j) + std::min(k, j) + (D.tw_unit ? 0 : 1);
+                ops += 2.0 * k * k;
+            }
+        } else {
+            // LAPACK order: forward sum_j min(kl, n-1-j) FMAs, backward sum_j
+            // (uext_j FMAs + 1 multiply)
+            for (int j = 0; j + 1 < n; ++j) ops += std::min(D.kl, n - 1 - j);
+            ops += ctx->uext_sum[d] + n;
+        }
+        flops[ADSG_STAGE_SOLVE_X + d] = 2.0 * lines * ops;
         bytes[ADSG_STAGE_SOLVE_X + d] = 16.0 * total;
     }
     {

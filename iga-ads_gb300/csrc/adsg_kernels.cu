@@ -203,11 +203,14 @@ __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __rest
     double pre[PRE];
 #pragma unroll
     for (int q = 0; q < PRE; ++q) pre[q] = ld(r0 + P + 1 + q);
-    for (int r = r0; r < r1; ++r) {
+    // one row: the host read PRE rows ahead is issued first, so that the
+    // link keeps PRE reads per thread in flight while the row computes
+    auto row = [&](int r, bool sym) {
+        const double incoming = ld(r + P + 1 + PRE);
         const double* a0 = A0 + static_cast<long long>(r) * BW;
         const double* b0 = B0 + static_cast<long long>(r) * BW;
         double acc0 = 0.0, acc1 = 0.0;
-        if (SYM && r >= sym_lo && r < sym_hi) {  // band_pass_kernel's SYM order
+        if (sym) {  // band_pass_kernel's SYM order
             acc0 = __ldg(a0 + P) * w[P];
             acc1 = __ldg(b0 + P) * w[P];
 #pragma unroll
@@ -233,8 +236,13 @@ __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __rest
         w[BW - 1] = pre[0];
 #pragma unroll
         for (int q = 0; q < PRE - 1; ++q) pre[q] = pre[q + 1];
-        pre[PRE - 1] = ld(r + P + 1 + PRE);
-    }
+        pre[PRE - 1] = incoming;
+    };
+    const int lo = SYM ? max(r0, min(r1, sym_lo)) : r1, hi = SYM ? max(lo, min(r1, sym_hi)) : r1;
+    int r = r0;
+    for (; r < lo; ++r) row(r, false);
+    for (; r < hi; ++r) row(r, true);
+    for (; r < r1; ++r) row(r, false);
 }
 
 bool outer_pass_columns_ok(int p) { return p >= 1 && p <= 4; }

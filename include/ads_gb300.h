@@ -143,9 +143,12 @@ int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps);
  * while a CUDA graph replays).  adsg_ctx_stage_times synchronises, adds the
  * elapsed times to ms[stage] and launch counts to launches[stage] (arrays of
  * ADSG_NSTAGES entries, accumulated since the last call) and resets them.
- * adsg_ctx_stage_work gives each stage's algorithmic work per launch: FP64
- * flops (FMA = 2, multiply = 1) and compulsory HBM bytes (each input read and
- * each output written once). */
+ * adsg_ctx_stage_work gives each stage's algorithmic work per launch: the FP64
+ * operations of the algorithm the stage's kernel implements in the step path
+ * (pair sums on symmetric band rows, two-ended unit-diagonal sweeps where the
+ * context chose them), each FMA, multiply or add counted as 2 flops since
+ * each takes one DFMA issue slot (the element stage: FMA = 2, others = 1), and
+ * compulsory HBM bytes (each input read and each output written once). */
 #define ADSG_STAGE_RHS_OUTER 0  /* band pass along z (3D) or y (2D) */
 #define ADSG_STAGE_RHS_MIDDLE 1 /* band pass along y (3D) */
 #define ADSG_STAGE_RHS_X 2      /* band pass along x, writes the RHS */
