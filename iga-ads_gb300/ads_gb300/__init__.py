@@ -137,6 +137,7 @@ def library() -> ctypes.CDLL:
         "adsg_batch_steps_looped": (i, [vp, i]),
         "adsg_batch_synchronize": (i, [vp]),
         "adsg_batch_tuning": (i, [vp, _c_int_p, _c_int_p]),
+        "adsg_batch_engine": (i, [vp]),
         "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
     }
@@ -505,7 +506,9 @@ class Batch:
         b = ctypes.c_int()
         g = ctypes.c_int()
         _check(library().adsg_batch_tuning(self._h, ctypes.byref(b), ctypes.byref(g)))
-        return {"blocks_per_sm": b.value, "graph": bool(g.value)}
+        engine = library().adsg_batch_engine(self._h)
+        return {"blocks_per_sm": b.value, "graph": bool(g.value),
+                "engine": "concurrent" if engine == 1 else "persistent"}
 
 
 def batch_specs(seed: int = 0, n2d: int = 32, n3d: int = 32, dt: float = 1e-6):

@@ -1,14 +1,21 @@
 // Batched engine: many independent heat simulations of uneven sizes and
-// degrees advanced together.  Each run of steps is ONE persistent cooperative
-// launch (all stages of all instances, grid barriers between stages),
-// replayed from a CUDA graph; its grid size is chosen by an autotuner that
-// times every feasible blocks-per-SM count on the batch itself.  The
-// reference has no batched form: its unit of work is one simulation object
-// driven by simulation_base::run (src/ads/simulation/simulation_base.cpp:11-20).
+// degrees advanced together, by one of two engines chosen at creation by
+// timing both on the batch itself:
+//  - persistent: ONE cooperative launch per run of steps (all stages of all
+//    instances, grid barriers between stages), replayed from a CUDA graph,
+//    its grid size autotuned;
+//  - concurrent: every instance has a plain context (its own tuned kernels:
+//    two-ended sweeps, pair sums, row-scaled step) on its own stream, and one
+//    step of all instances is a CUDA graph of independent per-instance
+//    chains forked from and joined to the batch stream, so the hardware runs
+//    the instances side by side.
+// The reference has no batched form: its unit of work is one simulation
+// object driven by simulation_base::run (src/ads/simulation/simulation_base.cpp:11-20).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <new>
 #include <vector>
 
@@ -59,15 +66,27 @@ struct adsg_batch {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = -1, graph_par = -1;
     bool graph_ok = true;
-    std::vector<adsg_ctx*> ctxs;  // plain contexts for the per-instance loop (created on demand)
+    int engine = 0;                    // 0 persistent kernel, 1 concurrent per-instance graph
+    std::vector<adsg_ctx*> ctxs;       // plain per-instance contexts (own streams)
+    std::vector<cudaEvent_t> events;   // fork/join and chaining events, one per instance + 1
+    cudaGraphExec_t step_graph[2] = {nullptr, nullptr};  // one concurrent step from parity 0 / 1
 
     ~adsg_batch() {
         if (stream) cudaStreamSynchronize(stream);
         for (auto* c : ctxs) adsg_ctx_destroy(c);
+        for (auto g : step_graph)
+            if (g) cudaGraphExecDestroy(g);
+        for (auto e : events) cudaEventDestroy(e);
         if (graph) cudaGraphExecDestroy(graph);
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+#define ADSG_BATCH_TRY(expr, where)                         \
+    do {                                                    \
+        cudaError_t e_ = (expr);                            \
+        if (e_ != cudaSuccess) return fail_cuda(e_, where); \
+    } while (0)
 
 namespace {
 
@@ -89,6 +108,85 @@ int check_error_word(adsg_batch* b) {
         cudaMemsetAsync(b->B.bar_count, 0, sizeof(unsigned), b->stream);
         cudaStreamSynchronize(b->stream);
         return fail(ADSG_ERR_DEVICE, "a grid barrier of the batched kernel timed out");
+    }
+    return 0;
+}
+
+// Per-instance contexts on their own streams, and the events that fork,
+// join or chain their work.
+int ensure_contexts(adsg_batch* b) {
+    if (!b->ctxs.empty()) return 0;
+    b->ctxs.assign(b->count, nullptr);
+    for (int i = 0; i < b->count; ++i) {
+        const dim_host& h = b->dims[i];
+        adsg_dim_desc d{};
+        d.p = h.p;
+        d.elements = h.elements;
+        d.quad_order = h.q;
+        d.n = h.n;
+        d.btab = h.btab.data();
+        d.w = h.w.data();
+        d.J = h.J.data();
+        d.first_dofs = h.first_dofs.data();
+        d.kl = h.kl;
+        d.ku = h.ku;
+        d.ldab = h.ldab;
+        d.lu = h.lu.data();
+        d.ipiv = h.ipiv.data();
+        const adsg_dim_desc descs[3] = {d, d, d};
+        if (int st = adsg_ctx_create(b->inst[i].ndim, descs, &b->ctxs[i])) {
+            b->ctxs[i] = nullptr;
+            return st;
+        }
+    }
+    while (b->events.size() < static_cast<size_t>(b->count) + 1) {
+        cudaEvent_t e = nullptr;
+        ADSG_BATCH_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+        b->events.push_back(e);
+    }
+    return 0;
+}
+
+// One step of every instance from parity par on its own context's stream:
+// fork from the batch stream, join back into it.
+int enqueue_concurrent_step(adsg_batch* b, int par) {
+    cudaEvent_t fork = b->events[b->count];
+    ADSG_BATCH_TRY(cudaEventRecord(fork, b->stream), "event");
+    for (int i = 0; i < b->count; ++i) {
+        cudaStream_t s = ctx_stream(b->ctxs[i]);
+        ADSG_BATCH_TRY(cudaStreamWaitEvent(s, fork, 0), "fork");
+        if (int st = adsg_heat_step(b->ctxs[i], b->inst[i].buf[par], b->inst[i].buf[par ^ 1], b->dt[i])) return st;
+        ADSG_BATCH_TRY(cudaEventRecord(b->events[i], s), "event");
+        ADSG_BATCH_TRY(cudaStreamWaitEvent(b->stream, b->events[i], 0), "join");
+    }
+    return 0;
+}
+
+int concurrent_steps(adsg_batch* b, int nsteps) {
+    for (int s = 0; s < nsteps; ++s) {
+        const int par = b->par;
+        if (!b->step_graph[par]) {
+            // prime each context's dt bands outside the capture
+            for (int i = 0; i < b->count; ++i)
+                if (int st = ctx_prepare_dt(b->ctxs[i], b->dt[i])) return st;
+            cudaGraph_t g = nullptr;
+            ADSG_BATCH_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+            const int st = enqueue_concurrent_step(b, par);
+            const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+            if (st) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (ec != cudaSuccess) return fail_cuda(ec, "end capture");
+            const cudaError_t ei = cudaGraphInstantiate(&b->step_graph[par], g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                b->step_graph[par] = nullptr;
+                return fail_cuda(ei, "graph instantiate");
+            }
+        }
+        ADSG_BATCH_TRY(cudaGraphLaunch(b->step_graph[par], b->stream), "graph launch");
+        b->par ^= 1;
     }
     return 0;
 }
@@ -263,6 +361,44 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
     }
     b->par = 0;
     if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
+    // engine: the persistent kernel (best grid above) against the concurrent
+    // per-instance graph, two steps each on the zero state
+    {
+        const char* force = std::getenv("ADSG_BATCH_ENGINE");
+        if (force && (*force == '0' || *force == '1')) {
+            b->engine = *force - '0';
+        } else if (ensure_contexts(b) == 0) {
+            cudaEventCreate(&t0);
+            cudaEventCreate(&t1);
+            float tp = 1e30f, tc = 1e30f;
+            if (launch_steps(b, 2, b->blocks_per_sm) == 0) {  // warm-up
+                cudaEventRecord(t0, b->stream);
+                if (launch_steps(b, 2, b->blocks_per_sm) == 0) {
+                    cudaEventRecord(t1, b->stream);
+                    if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&tp, t0, t1);
+                }
+            }
+            if (concurrent_steps(b, 2) == 0) {  // warm-up, builds both graphs
+                cudaEventRecord(t0, b->stream);
+                if (concurrent_steps(b, 2) == 0) {
+                    cudaEventRecord(t1, b->stream);
+                    if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&tc, t0, t1);
+                }
+            }
+            cudaEventDestroy(t0);
+            cudaEventDestroy(t1);
+            cudaGetLastError();
+            b->engine = tc < tp ? 1 : 0;
+            if (int st = check_error_word(b)) return bail(st);
+            for (int i = 0; i < count; ++i) {
+                cudaMemsetAsync(b->inst[i].buf[0], 0, sizeof(double) * b->inst[i].size, b->stream);
+                cudaMemsetAsync(b->inst[i].buf[1], 0, sizeof(double) * b->inst[i].size, b->stream);
+            }
+            b->par = 0;
+            if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
+        }
+        cudaGetLastError();
+    }
     *out = b;
     return 0;
 }
@@ -301,6 +437,10 @@ int adsg_batch_steps(adsg_batch* b, int nsteps) {
     if (!b) return fail(-1, "batch is NULL");
     if (nsteps < 0) return fail(-2, "nsteps must be >= 0");
     if (nsteps == 0) return 0;
+    if (b->engine == 1) {
+        if (int st = ensure_contexts(b)) return st;
+        return concurrent_steps(b, nsteps);
+    }
     if (b->graph_ok && !(b->graph && b->graph_steps == nsteps && b->graph_par == b->par)) {
         if (b->graph) {
             cudaGraphExecDestroy(b->graph);
@@ -336,36 +476,22 @@ int adsg_batch_steps(adsg_batch* b, int nsteps) {
 int adsg_batch_steps_looped(adsg_batch* b, int nsteps) {
     if (!b) return fail(-1, "batch is NULL");
     if (nsteps < 0) return fail(-2, "nsteps must be >= 0");
-    if (b->ctxs.empty()) {
-        b->ctxs.assign(b->count, nullptr);
-        for (int i = 0; i < b->count; ++i) {
-            const dim_host& h = b->dims[i];
-            adsg_dim_desc d{};
-            d.p = h.p;
-            d.elements = h.elements;
-            d.quad_order = h.q;
-            d.n = h.n;
-            d.btab = h.btab.data();
-            d.w = h.w.data();
-            d.J = h.J.data();
-            d.first_dofs = h.first_dofs.data();
-            d.kl = h.kl;
-            d.ku = h.ku;
-            d.ldab = h.ldab;
-            d.lu = h.lu.data();
-            d.ipiv = h.ipiv.data();
-            const adsg_dim_desc descs[3] = {d, d, d};
-            if (int st = adsg_ctx_create(b->inst[i].ndim, descs, &b->ctxs[i])) return st;
-            if (int st = adsg_ctx_set_stream(b->ctxs[i], b->stream)) return st;
-        }
-    }
+    if (int st = ensure_contexts(b)) return st;
+    // one instance after the other: each context's stream waits for the
+    // previous instance (or the batch stream), the batch stream for the last
     for (int s = 0; s < nsteps; ++s) {
+        cudaEvent_t prev = b->events[b->count];
+        ADSG_BATCH_TRY(cudaEventRecord(prev, b->stream), "event");
         for (int i = 0; i < b->count; ++i) {
+            cudaStream_t st_i = ctx_stream(b->ctxs[i]);
+            ADSG_BATCH_TRY(cudaStreamWaitEvent(st_i, prev, 0), "chain");
             double* cur = b->inst[i].buf[b->par];
             double* nxt = b->inst[i].buf[b->par ^ 1];
-            if (int st = adsg_heat_rhs(b->ctxs[i], cur, nxt, b->dt[i])) return st;
-            if (int st = adsg_ads_solve(b->ctxs[i], nxt, nullptr)) return st;
+            if (int st = adsg_heat_step(b->ctxs[i], cur, nxt, b->dt[i])) return st;
+            ADSG_BATCH_TRY(cudaEventRecord(b->events[i], st_i), "event");
+            prev = b->events[i];
         }
+        ADSG_BATCH_TRY(cudaStreamWaitEvent(b->stream, prev, 0), "chain");
         b->par ^= 1;
     }
     return 0;
@@ -379,8 +505,10 @@ int adsg_batch_synchronize(adsg_batch* b) {
 int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captured) {
     if (!b) return fail(-1, "batch is NULL");
     if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
-    if (graph_captured) *graph_captured = b->graph ? 1 : 0;
+    if (graph_captured) *graph_captured = b->graph || b->step_graph[0] || b->step_graph[1] ? 1 : 0;
     return 0;
 }
+
+int adsg_batch_engine(const adsg_batch* b) { return b ? b->engine : -1; }
 
 }  // extern "C"

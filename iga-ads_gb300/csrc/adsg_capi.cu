@@ -855,6 +855,11 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
 
 }  // namespace
 
+namespace adsg {
+cudaStream_t ctx_stream(adsg_ctx* c) { return c->stream; }
+int ctx_prepare_dt(adsg_ctx* c, double dt) { return ensure_dt_bands(c, dt); }
+}  // namespace adsg
+
 extern "C" {
 
 const char* adsg_last_error(void) { return g_last_error.c_str(); }

@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/ads_gb300.h"
 
 namespace adsg {
@@ -66,6 +68,11 @@ int make_solve_tables(int n, int kl, int ku, int ldab, const double* ab, const i
 // shape, too short, or the unpivoted elimination is not accurate enough
 // (the LAPACK-order sweeps are used then).
 int make_twisted_tables(int n, int kl, int ku, int ldab, const double* ab, const int* ipiv, twisted_tables& t);
+
+// A context's stream, and its dt-dependent bands built ahead of a stream
+// capture (used by the batched engine).
+cudaStream_t ctx_stream(adsg_ctx* c);
+int ctx_prepare_dt(adsg_ctx* c, double dt);
 
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const char* msg);

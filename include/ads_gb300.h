@@ -325,6 +325,12 @@ int adsg_batch_steps_looped(adsg_batch* b, int nsteps);
 int adsg_batch_synchronize(adsg_batch* b);
 /* Autotuned blocks per SM and whether the launch is replayed from a graph. */
 int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captured);
+/* The engine the batch chose at creation by timing both on itself: 0 the
+ * persistent cooperative kernel (grid barriers between stages), 1 a CUDA
+ * graph of independent per-instance chains (each instance's own tuned step
+ * kernels, run side by side); -1 for a NULL batch.  ADSG_BATCH_ENGINE=0/1
+ * forces it. */
+int adsg_batch_engine(const adsg_batch* b);
 
 /* ---- the heat RHS without any allocation --------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

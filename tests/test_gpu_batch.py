@@ -42,7 +42,11 @@ def test_batch_against_oracle_and_loop(cuda):
         assert oracle.rel_l2(b.get_state(i), got[i]) <= 3 * step_tol([_cond(p, e)] * nd), (i, SMALL[i])
 
 
-def test_batch_repeated_calls_and_parity(cuda):
+@pytest.mark.parametrize("engine", ["0", "1"])
+def test_batch_repeated_calls_and_parity(engine, cuda, monkeypatch):
+    """Both engines (persistent kernel, concurrent per-instance graph) over
+    repeated calls with odd and even step counts."""
+    monkeypatch.setenv("ADSG_BATCH_ENGINE", engine)
     b = ads.Batch(SMALL[:4])
     rng = np.random.default_rng(8)
     u0 = [rng.uniform(-1, 1, n) for n in b.sizes]
@@ -56,6 +60,7 @@ def test_batch_repeated_calls_and_parity(cuda):
         assert oracle.rel_l2(b.get_state(i), ref) <= 7 * step_tol([_cond(p, e)] * nd)
     t = b.tuning()
     assert t["blocks_per_sm"] >= 1
+    assert t["engine"] == ("concurrent" if engine == "1" else "persistent")
 
 
 def test_mixed_64_batch_matches_plain_kernels(cuda):
