@@ -114,6 +114,7 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
         "adsg_ctx_launch_pdl": (i, [vp]),
         "adsg_ctx_fused_x": (i, [vp]),
+        "adsg_ctx_step_1block": (i, [vp]),
         "adsg_quad_size": (ll, [vp]),
         "adsg_count_nonfinite": (i, [vp, vp, ctypes.POINTER(ll)]),
         "adsg_load_vector": (i, [vp, vp, vp]),
@@ -184,8 +185,8 @@ def _host(a: np.ndarray) -> np.ndarray:
     return a
 
 
-NSTAGES = 8
-STAGES = ("rhs_outer", "rhs_middle", "rhs_x", "solve_x", "solve_y", "solve_z", "rhs_elem", "rhs_solve_x")
+NSTAGES = 9
+STAGES = ("rhs_outer", "rhs_middle", "rhs_x", "solve_x", "solve_y", "solve_z", "rhs_elem", "rhs_solve_x", "step_1block")
 
 
 class Dimension:
@@ -320,6 +321,10 @@ class Context:
     def fused_x(self) -> bool:
         """Whether heat_step fuses the x band pass into the x solve."""
         return library().adsg_ctx_fused_x(self._h) == 1
+
+    def step_1block(self) -> bool:
+        """Whether heat_step runs a whole (small 2D) step in one block."""
+        return library().adsg_ctx_step_1block(self._h) == 1
 
     def stage_work(self) -> dict:
         """{stage: (fp64_flops, hbm_bytes)} of one launch of each stage."""

@@ -432,6 +432,7 @@ struct adsg_ctx {
     std::vector<adsg_adjoint*> adjoints;
     int pdl = 0;     // programmatic dependent launch for the step kernels (chosen at creation)
     int fuse_x = 0;  // the step fuses the x band pass with the x solve (chosen at creation)
+    int step_1block = 0;  // small 2D grids: the whole step in one block (chosen at creation)
 
     cudaEvent_t take_event() {
         if (!spare.empty()) {
@@ -689,9 +690,17 @@ bool fusion_ok(const adsg_ctx* c) {
            rhs_x_solve_ok(c->sdims[0], make_line_layout(c->n, c->ndim, 0));
 }
 
+bool step_1block_ok(const adsg_ctx* c) { return c->ndim == 2 && small2d_step_ok(c->sdims[0], c->sdims[1]); }
+
 int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     int st = ensure_dt_bands(c, dt);  // before the view is read
     if (st) return st;
+    if (c->step_1block && step_1block_ok(c)) {
+        pdl_scope pdl(c->pdl);
+        stage_scope sc(c, ADSG_STAGE_STEP_1BLOCK);
+        ADSG_CUDA_TRY(launch_small2d_step(prev, next, c->sdims[0], c->sdims[1], c->stream), "one-block step");
+        return 0;
+    }
     const bool fused = c->fuse_x && fusion_ok(c);
     st = enqueue_rhs_with(c, c->sdims, prev, next, dt, fused);
     if (st) return st;
@@ -747,20 +756,24 @@ int autotune_launch_mode(adsg_ctx* c) {
         const char* v = std::getenv(name);
         return v && (*v == '0' || *v == '1') ? *v - '0' : -1;
     };
-    const int f_pdl = forced("ADSG_PDL"), f_fuse = forced("ADSG_FUSE_X");
-    const bool can_fuse = fusion_ok(c);
-    std::vector<int> modes;  // bit 0: pdl, bit 1: fuse
-    for (int m = 0; m < 4; ++m) {
-        const int pdl = m & 1, fuse = (m >> 1) & 1;
+    const int f_pdl = forced("ADSG_PDL"), f_fuse = forced("ADSG_FUSE_X"), f_one = forced("ADSG_STEP_1BLOCK");
+    const bool can_fuse = fusion_ok(c), can_one = step_1block_ok(c);
+    std::vector<int> modes;  // bit 0: pdl, bit 1: fuse, bit 2: one-block step
+    for (int m = 0; m < 8; ++m) {
+        const int pdl = m & 1, fuse = (m >> 1) & 1, one = (m >> 2) & 1;
         if (fuse && !can_fuse) continue;
+        if (one && !can_one) continue;
+        if (one && fuse) continue;  // the one-block step has no separate x pass
         if (f_pdl >= 0 && pdl != f_pdl) continue;
         if (f_fuse >= 0 && fuse != (f_fuse && can_fuse)) continue;
+        if (f_one >= 0 && one != (f_one && can_one)) continue;
         modes.push_back(m);
     }
     if (modes.empty()) modes.push_back(0);
     auto apply = [&](int m) {
         c->pdl = m & 1;
         c->fuse_x = (m >> 1) & 1;
+        c->step_1block = (m >> 2) & 1;
     };
     if (modes.size() == 1) {
         apply(modes[0]);
@@ -1200,6 +1213,8 @@ int adsg_ctx_launch_pdl(const adsg_ctx* ctx) { return ctx ? ctx->pdl : -1; }
 
 int adsg_ctx_fused_x(const adsg_ctx* ctx) { return ctx ? ctx->fuse_x : -1; }
 
+int adsg_ctx_step_1block(const adsg_ctx* ctx) { return ctx ? ctx->step_1block : -1; }
+
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!flops) return fail(-2, "flops is NULL");
@@ -1286,6 +1301,11 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
     // fused x pass + x solve: both works, the pass's inputs and the solved output
     flops[ADSG_STAGE_RHS_SOLVE_X] = flops[ADSG_STAGE_RHS_X] + flops[ADSG_STAGE_SOLVE_X];
     bytes[ADSG_STAGE_RHS_SOLVE_X] = bytes[ADSG_STAGE_RHS_X];
+    // one-block step: the whole step's work, the state read and written once
+    flops[ADSG_STAGE_STEP_1BLOCK] = flops[ADSG_STAGE_RHS_OUTER] + flops[ADSG_STAGE_RHS_MIDDLE] +
+                                    flops[ADSG_STAGE_RHS_X] + flops[ADSG_STAGE_SOLVE_X] + flops[ADSG_STAGE_SOLVE_Y] +
+                                    flops[ADSG_STAGE_SOLVE_Z];
+    bytes[ADSG_STAGE_STEP_1BLOCK] = 16.0 * total;
     return 0;
 }
 

@@ -72,36 +72,39 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 // both outputs, with the left coefficient of each pair: 3p+2 FP64 operations
 // instead of 2(2p+1) for out0/out1 = A0/B0 (.) in0, and 5p+3 instead of
 // 3(2p+1) with a second input.  Other rows take the full band.
-template <int P, bool IN1, bool OUT1, bool SYM = false>
-__global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict__ in0,
-                                                         const double* __restrict__ in1,
-                                                         double* __restrict__ out0,
-                                                         double* __restrict__ out1,
-                                                         const double* __restrict__ A0,
-                                                         const double* __restrict__ A1,
-                                                         const double* __restrict__ B0, int n_axis,
-                                                         long long stride, long long total, int sym_lo, int sym_hi) {
+// One output of a band pass (the body of band_pass_kernel, shared with the
+// one-block small-grid step so that both perform the same operations in the
+// same order).  GIN: the inputs are in global memory (read through the
+// read-only path); otherwise in shared memory.
+template <bool GIN>
+__device__ __forceinline__ double ldin(const double* p) {
+    if (GIN) return __ldg(p);
+    return *p;
+}
+
+template <int P, bool IN1, bool OUT1, bool SYM, bool GIN>
+__device__ __forceinline__ void band_out(long long g, const double* in0, const double* in1, double* out0,
+                                         double* out1, const double* __restrict__ A0,
+                                         const double* __restrict__ A1, const double* __restrict__ B0, int n_axis,
+                                         long long stride, int sym_lo, int sym_hi) {
     constexpr int BW = 2 * P + 1;
-    long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (g >= total) return;
-    pdl_wait_and_release();
     const int r = static_cast<int>((g / stride) % n_axis);
     const double* a0 = A0 + static_cast<long long>(r) * BW;
     const double* a1 = IN1 ? A1 + static_cast<long long>(r) * BW : nullptr;
     const double* b0 = OUT1 ? B0 + static_cast<long long>(r) * BW : nullptr;
     double acc0 = 0.0, acc1 = 0.0;
     if (SYM && r >= sym_lo && r < sym_hi) {
-        const double c0 = __ldg(in0 + g);
+        const double c0 = ldin<GIN>(in0 + g);
         acc0 = __ldg(a0 + P) * c0;
         if (OUT1) acc1 = __ldg(b0 + P) * c0;
-        if (IN1) acc0 = fma(__ldg(a1 + P), __ldg(in1 + g), acc0);
+        if (IN1) acc0 = fma(__ldg(a1 + P), ldin<GIN>(in1 + g), acc0);
 #pragma unroll
         for (int t = 1; t <= P; ++t) {
             const long long off = static_cast<long long>(t) * stride;
-            const double s0 = __ldg(in0 + g - off) + __ldg(in0 + g + off);
+            const double s0 = ldin<GIN>(in0 + g - off) + ldin<GIN>(in0 + g + off);
             acc0 = fma(__ldg(a0 + P - t), s0, acc0);
             if (OUT1) acc1 = fma(__ldg(b0 + P - t), s0, acc1);
-            if (IN1) acc0 = fma(__ldg(a1 + P - t), __ldg(in1 + g - off) + __ldg(in1 + g + off), acc0);
+            if (IN1) acc0 = fma(__ldg(a1 + P - t), ldin<GIN>(in1 + g - off) + ldin<GIN>(in1 + g + off), acc0);
         }
         out0[g] = acc0;
         if (OUT1) out1[g] = acc1;
@@ -112,14 +115,29 @@ __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict
         const int c = r - P + t;
         if (c >= 0 && c < n_axis) {
             const long long at = g + static_cast<long long>(t - P) * stride;
-            const double v0 = __ldg(in0 + at);
+            const double v0 = ldin<GIN>(in0 + at);
             acc0 = fma(__ldg(a0 + t), v0, acc0);
             if (OUT1) acc1 = fma(__ldg(b0 + t), v0, acc1);
-            if (IN1) acc0 = fma(__ldg(a1 + t), __ldg(in1 + at), acc0);
+            if (IN1) acc0 = fma(__ldg(a1 + t), ldin<GIN>(in1 + at), acc0);
         }
     }
     out0[g] = acc0;
     if (OUT1) out1[g] = acc1;
+}
+
+template <int P, bool IN1, bool OUT1, bool SYM = false>
+__global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict__ in0,
+                                                         const double* __restrict__ in1,
+                                                         double* __restrict__ out0,
+                                                         double* __restrict__ out1,
+                                                         const double* __restrict__ A0,
+                                                         const double* __restrict__ A1,
+                                                         const double* __restrict__ B0, int n_axis,
+                                                         long long stride, long long total, int sym_lo, int sym_hi) {
+    long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    pdl_wait_and_release();
+    band_out<P, IN1, OUT1, SYM, true>(g, in0, in1, out0, out1, A0, A1, B0, n_axis, stride, sym_lo, sym_hi);
 }
 
 template <int P>
@@ -1075,6 +1093,92 @@ static cudaError_t rhs_x_solve_t(const double* in0, const double* in1, double* o
     const long long per = 16LL * wpb;
     return launch_pdl(kern, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)), dim3(32 * wpb), smem, s, in0, in1,
                       out, A0, A1, d, L);
+}
+
+// ---------------------------------------------------------------------------
+// One-block step for small 2D grids: adsg_heat_step's y pass, x pass, x sweep
+// and y sweep in one launch, separated by block barriers, on a grid whose
+// four working tensors fit in shared memory.  Launch latency, not work,
+// bounds such grids (four dependent launches of a few microseconds each).
+// The passes are band_out and the sweeps twisted_chain, so the operations and
+// their order are those of the separate kernels.
+// ---------------------------------------------------------------------------
+template <int K, int UNR>
+__device__ __forceinline__ void small_sweeps(double* R, const dim_dev& D, int nlines, long long line_stride,
+                                             long long es) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5, chain = lane >> 4;
+    for (int grp = warp; grp * 16 < nlines; grp += nwarps) {
+        const int line = grp * 16 + (lane & 15);
+        const bool active = line < nlines;
+        const unsigned mask = __ballot_sync(0xffffffffu, active);
+        if (active) {
+            double* x = R + line * line_stride + (chain ? static_cast<long long>(D.n - 1) * es : 0);
+            const long long off = static_cast<long long>(chain) * D.tw_rows;
+            twisted_chain<K, UNR, true>(x, x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K,
+                                        D.tw_ucol + off * K, D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
+        }
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restrict__ u, double* __restrict__ out,
+                                                           dim_dev X, dim_dev Y) {
+    extern __shared__ double sm[];
+    constexpr int UNR = K > 2 ? 4 : 8;
+    const int nx = X.n, ny = Y.n, N = nx * ny;
+    double* U = sm;
+    double* A = sm + N;
+    double* C = sm + 2 * N;
+    double* R = sm + 3 * N;
+    pdl_wait_and_release();
+    for (int g = threadIdx.x; g < N; g += blockDim.x) U[g] = u[g];
+    __syncthreads();
+    // y pass: A = My u, C = Ny u (pair sums on the symmetric rows, as launch_band_pass)
+    const int ylo = max(Y.sym_lo, K), yhi = min(Y.sym_hi, ny - K);
+    for (int g = threadIdx.x; g < N; g += blockDim.x) {
+        if (yhi > ylo)
+            band_out<K, false, true, true, false>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, ylo, yhi);
+        else
+            band_out<K, false, true, false, false>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, 0, 0);
+    }
+    __syncthreads();
+    // x pass: R = (-dt Kx) A + Mx C
+    for (int g = threadIdx.x; g < N; g += blockDim.x)
+        band_out<K, true, false, false, false>(g, A, C, R, nullptr, X.kdt, X.mrow, nullptr, nx, 1, 0, 0);
+    __syncthreads();
+    small_sweeps<K, UNR>(R, X, ny, nx, 1);  // x-lines: rows of R
+    __syncthreads();
+    small_sweeps<K, UNR>(R, Y, nx, 1, nx);  // y-lines: columns of R
+    __syncthreads();
+    for (int g = threadIdx.x; g < N; g += blockDim.x) out[g] = R[g];
+}
+
+size_t small2d_smem(const dim_dev& x, const dim_dev& y) { return sizeof(double) * 4 * static_cast<size_t>(x.n) * y.n; }
+
+bool small2d_step_ok(const dim_dev& x, const dim_dev& y) {
+    auto tw = [](const dim_dev& d) {
+        return solve_variant_twisted(d.solve_variant) && d.tw_unit && d.tw_k == d.p && d.tw_k >= 1 && d.tw_k <= 4 &&
+               d.tw_lmul != nullptr;
+    };
+    return tw(x) && tw(y) && x.p == y.p && small2d_smem(x, y) <= 200 * 1024;
+}
+
+cudaError_t launch_small2d_step(const double* u, double* out, const dim_dev& x, const dim_dev& y, cudaStream_t s) {
+    if (!small2d_step_ok(x, y)) return cudaErrorInvalidValue;
+    const size_t smem = small2d_smem(x, y);
+    auto go = [&](auto kern) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(kern), smem);
+            if (e != cudaSuccess) return e;
+        }
+        return launch_pdl(kern, dim3(1), dim3(512), smem, s, u, out, x, y);
+    };
+    switch (x.p) {
+        case 1: return go(small2d_step_kernel<1>);
+        case 2: return go(small2d_step_kernel<2>);
+        case 3: return go(small2d_step_kernel<3>);
+        default: return go(small2d_step_kernel<4>);
+    }
 }
 
 template <int K>

@@ -141,6 +141,10 @@ bool line_solve_variant_ok(int variant, const dim_dev& d);
 // x band pass (out = A0 (.) in0 [+ A1 (.) in1]) fused with the two-ended x
 // solve on contiguous lines; out holds the solved lines.
 bool rhs_x_solve_ok(const dim_dev& d, const line_layout& L);
+// A whole 2D step (the step view's passes and two-ended unit-diagonal sweeps)
+// in one block, for grids whose four working tensors fit in shared memory.
+bool small2d_step_ok(const dim_dev& x, const dim_dev& y);
+cudaError_t launch_small2d_step(const double* u, double* out, const dim_dev& x, const dim_dev& y, cudaStream_t s);
 cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out, const double* A0, const double* A1,
                                const dim_dev& d, const line_layout& L, cudaStream_t s);
 

@@ -157,7 +157,8 @@ int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps);
 #define ADSG_STAGE_SOLVE_Z 5
 #define ADSG_STAGE_RHS_ELEM 6   /* element-wise sum-factorised quadrature */
 #define ADSG_STAGE_RHS_SOLVE_X 7 /* x band pass fused with the x solve (adsg_heat_step) */
-#define ADSG_NSTAGES 8
+#define ADSG_STAGE_STEP_1BLOCK 8 /* a whole small 2D step in one block (adsg_heat_step) */
+#define ADSG_NSTAGES 9
 int adsg_ctx_enable_stage_timers(adsg_ctx* ctx, int enable);
 int adsg_ctx_stage_times(adsg_ctx* ctx, double* ms, long long* launches);
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
@@ -181,6 +182,11 @@ int adsg_ctx_launch_pdl(const adsg_ctx* ctx);
  * x uses solve variant 5; chosen at creation by timing, ADSG_FUSE_X=0/1
  * forces it), 0 when not, -1 for a NULL context.  Results do not depend on it. */
 int adsg_ctx_fused_x(const adsg_ctx* ctx);
+/* 1 when adsg_heat_step runs a whole 2D step in one block (grids whose four
+ * working tensors fit in 200 KB of shared memory, both directions on the
+ * two-ended sweep; chosen at creation by timing, ADSG_STEP_1BLOCK=0/1 forces
+ * it), 0 when not, -1 for a NULL context.  Results do not depend on it. */
+int adsg_ctx_step_1block(const adsg_ctx* ctx);
 
 /* ---- host-buffer entry points (the reference-facing boundary) ------------- */
 
