@@ -1020,6 +1020,177 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
 size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
 
 // ---------------------------------------------------------------------------
+// The two-ended sweep for contiguous lines, streamed in chunks.  A warp owns
+// 16 consecutive lines (lanes 0-15 chain 0, lanes 16-31 chain 1, as above)
+// and a shared buffer of 2 chains x 16 lines x kChunk rows.  Before each
+// chunk of a sweep, the whole warp copies the rows the chunk will read
+// (kChunk consecutive rows of one line and chain per warp-wide load: 256
+// coalesced bytes); the chunk then runs in registers, leaving its results in
+// the same slots, which the warp writes back the same way.  The forward
+// results make one round trip through memory (L2 at these sizes) for the
+// backward sweep.  Unlike the tile of variant 5 the buffer does not grow
+// with the line, so long lines keep many warps per SM.  Same operations in
+// the same order as twisted_chain.
+// ---------------------------------------------------------------------------
+constexpr int kChunk = 32, kChunkPitch = kChunk + 1;
+
+struct chunk_lines {
+    double* data;    // first line of the warp
+    int n, n1, n2;   // line length and the chains' lengths
+    int nv;          // valid lines of the warp (<= 16)
+};
+
+// chain-local row r of chain c lies at offset c ? n-1-r : r of its line
+__device__ __forceinline__ long long chunk_offset(const chunk_lines& W, int line, int c, int r) {
+    return static_cast<long long>(line) * W.n + (c ? W.n - 1 - r : r);
+}
+
+// buf[c][l][t] <- chain-local row (first[c] + dir * t) of line l, chain c
+// (0 outside the chain); dir = +1 (forward) or -1 (backward)
+__device__ __forceinline__ void chunk_stage(double* buf, const chunk_lines& W, const int first[2], int dir) {
+    const int lane = threadIdx.x & 31;
+    for (int idx = lane; idx < 2 * 16 * kChunk; idx += 32) {
+        const int c = idx / (16 * kChunk), l = (idx / kChunk) % 16, t = idx % kChunk;
+        const int r = first[c] + dir * t, nc = c ? W.n2 : W.n1;
+        double v = 0.0;
+        if (l < W.nv && r >= 0 && r < nc) v = W.data[chunk_offset(W, l, c, r)];
+        buf[(c * 16 + l) * kChunkPitch + t] = v;
+    }
+}
+
+__device__ __forceinline__ void chunk_flush(const double* buf, const chunk_lines& W, const int first[2], int dir) {
+    const int lane = threadIdx.x & 31;
+    for (int idx = lane; idx < 2 * 16 * kChunk; idx += 32) {
+        const int c = idx / (16 * kChunk), l = (idx / kChunk) % 16, t = idx % kChunk;
+        const int r = first[c] + dir * t, nc = c ? W.n2 : W.n1;
+        if (l < W.nv && r >= 0 && r < nc) W.data[chunk_offset(W, l, c, r)] = buf[(c * 16 + l) * kChunkPitch + t];
+    }
+}
+
+template <int K, bool UNIT>
+__global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double* __restrict__ data, dim_dev D,
+                                                                         line_layout L) {
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4, line = lane & 15;
+    const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
+    if (g0 >= L.nlines) return;  // whole warp
+    pdl_wait_and_release();
+    chunk_lines W;
+    W.data = data + g0 * D.n;
+    W.n = D.n;
+    W.n1 = D.tw_n1;
+    W.n2 = D.tw_n2;
+    W.nv = static_cast<int>(min(16LL, L.nlines - g0));
+    double* buf = smem + static_cast<size_t>(warp) * 2 * 16 * kChunkPitch;
+    double* mine = buf + (chain * 16 + line) * kChunkPitch;  // this lane's slots
+    const bool active = line < W.nv;  // every lane stays to the end: the staging is warp-wide
+    const int nc = chain ? W.n2 : W.n1, nmax = max(W.n1, W.n2);
+    const long long off = static_cast<long long>(chain) * D.tw_rows;
+    const double* lmul = D.tw_lmul + off * K;
+    const double* ucol = D.tw_ucol + off * K;
+    const double* rdiag = D.tw_rdiag + off;
+    const double* G = D.tw_g + chain * 2 * K * K;
+    auto ld = [&](int r) -> double { return (active && r >= 0 && r < nc) ? W.data[chunk_offset(W, line, chain, r)] : 0.0; };
+
+    // ---- forward: rows j0 .. j0+kChunk-1 read rows j+K+1 from the chunk ----
+    double f[K + 1];
+#pragma unroll
+    for (int t = 0; t <= K; ++t) f[t] = ld(t);
+    double own[K], pre_tail = 0.0;  // y rows nc-K .. nc-1 and nc-K-1
+#pragma unroll
+    for (int i = 0; i < K; ++i) own[i] = 0.0;
+    for (int j0 = 0; j0 < nmax; j0 += kChunk) {
+        const int first[2] = {j0 + K + 1, j0 + K + 1};
+        __syncwarp();
+        chunk_stage(buf, W, first, +1);
+        __syncwarp();
+        if (active) {
+            const int tend = min(kChunk, nc - j0);
+            for (int t = 0; t < tend; ++t) {
+                const int j = j0 + t;
+                const double incoming = mine[t];
+                const double yv = f[0];
+                mine[t] = yv;
+                if (j == nc - K - 1) pre_tail = yv;
+#pragma unroll
+                for (int i = 0; i < K; ++i)
+                    if (j == nc - K + i) own[i] = yv;
+                const double ny = -yv;
+#pragma unroll
+                for (int q = 1; q <= K; ++q) f[q] = fma(ny, __ldg(lmul + static_cast<long long>(j) * K + q - 1), f[q]);
+#pragma unroll
+                for (int q = 0; q < K; ++q) f[q] = f[q + 1];
+                f[K] = incoming;
+            }
+        }
+        __syncwarp();
+        const int out_first[2] = {j0, j0};
+        chunk_flush(buf, W, out_first, +1);
+    }
+    __syncwarp();  // the flushed forward results are visible to the whole warp
+    // ---- meeting point ----
+    double oth[K], z[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) oth[i] = __shfl_xor_sync(0xffffffffu, own[i], 16);
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        double acc = 0.0;
+#pragma unroll
+        for (int i = 0; i < K; ++i) acc = fma(__ldg(G + a * 2 * K + i), own[i], acc);
+#pragma unroll
+        for (int i = 0; i < K; ++i) acc = fma(__ldg(G + a * 2 * K + K + i), oth[i], acc);
+        z[a] = acc;
+    }
+    // ---- backward: columns nc-1 .. 0 ----
+    double b[K + 1];
+#pragma unroll
+    for (int d = 0; d < K; ++d) b[d] = own[K - 1 - d];
+    b[K] = pre_tail;
+    int c = nc - 1;
+#pragma unroll
+    for (int a = K - 1; a >= 0; --a, --c) {  // the chain's K interface rows
+        const double v = z[a];
+        if (active) W.data[chunk_offset(W, line, chain, c)] = v;
+        const double nv = -v;
+#pragma unroll
+        for (int d = 1; d <= K; ++d) b[d] = fma(nv, __ldg(ucol + static_cast<long long>(c) * K + d - 1), b[d]);
+#pragma unroll
+        for (int d = 0; d < K; ++d) b[d] = b[d + 1];
+        b[K] = ld(c - K - 1);
+    }
+    // chunks of columns c_hi, c_hi-1, ..., c_hi-kChunk+1, reading rows c-K-1
+    const int chi0[2] = {W.n1 - K - 1, W.n2 - K - 1};
+    const int steps = (max(chi0[0], chi0[1]) + kChunk) / kChunk;
+    for (int s = 0; s < steps; ++s) {
+        const int in_first[2] = {chi0[0] - s * kChunk - K - 1, chi0[1] - s * kChunk - K - 1};
+        __syncwarp();
+        chunk_stage(buf, W, in_first, -1);
+        __syncwarp();
+        if (active) {
+            const int chi = chi0[chain] - s * kChunk;
+            for (int t = 0; t < kChunk; ++t) {
+                const int cc = chi - t;
+                if (cc < 0) break;
+                const double incoming = mine[t];
+                const double v = UNIT ? b[0] : b[0] * __ldg(rdiag + cc);
+                mine[t] = v;
+                const double nv = -v;
+#pragma unroll
+                for (int d = 1; d <= K; ++d) b[d] = fma(nv, __ldg(ucol + static_cast<long long>(cc) * K + d - 1), b[d]);
+#pragma unroll
+                for (int d = 0; d < K; ++d) b[d] = b[d + 1];
+                b[K] = incoming;
+            }
+        }
+        __syncwarp();
+        const int out_first[2] = {chi0[0] - s * kChunk, chi0[1] - s * kChunk};
+        chunk_flush(buf, W, out_first, -1);
+    }
+}
+
+size_t twisted_chunked_smem_per_warp() { return sizeof(double) * 2 * 16 * kChunkPitch; }
+
+// ---------------------------------------------------------------------------
 // The x band pass of the right-hand side fused with the x line solve.  Both
 // work on the same contiguous x-lines: each warp computes the band pass of its
 // 16 lines straight into its shared tile (out = A0 (.) in0 [+ A1 (.) in1],
@@ -1209,8 +1380,15 @@ cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out
 }
 
 template <int K, bool UNIT>
-static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, bool staged, cudaStream_t s) {
+static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, int variant, cudaStream_t s) {
     constexpr int UNR = K > 2 ? 4 : 8;
+    if (variant == SOLVE_TWISTED_CHUNKED && L.contiguous) {
+        const long long per = 64;  // 4 warps x 16 lines
+        return launch_pdl(line_solve_twisted_chunked_kernel<K, UNIT>,
+                          dim3(static_cast<unsigned>((L.nlines + per - 1) / per)), dim3(128),
+                          4 * twisted_chunked_smem_per_warp(), s, data, d, L);
+    }
+    const bool staged = variant == SOLVE_TWISTED_STAGED;
     if (staged && L.contiguous) {
         const size_t per_warp = twisted_staged_smem_per_warp(d.n);
         const int wpb = per_warp * 4 <= 227 * 1024 ? 4 : (per_warp * 2 <= 227 * 1024 ? 2 : 1);
@@ -1294,7 +1472,8 @@ static cudaError_t line_solve_variant(int variant, double* data, const dim_dev& 
 }
 
 bool line_solve_variant_ok(int variant, const dim_dev& d) {
-    if (variant == SOLVE_TWISTED) return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr;
+    if (variant == SOLVE_TWISTED || variant == SOLVE_TWISTED_CHUNKED)
+        return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr;
     if (variant == SOLVE_TWISTED_STAGED)
         return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr && twisted_staged_smem_per_warp(d.n) <= 227 * 1024;
     const int kl = d.kl, ku = d.ku_regular, w = d.w;
@@ -1313,25 +1492,23 @@ cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout&
     // U extent (columns beyond it take the wide-column branch)
     const int kl = d.kl, ku = d.ku_regular, w = d.w;
     const int v = trans ? SOLVE_STAGED_1 : d.solve_variant;
-    if (!trans && (v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED) && line_solve_variant_ok(v, d)) {
-        const bool staged = v == SOLVE_TWISTED_STAGED;
+    if (!trans && solve_variant_twisted(v) && line_solve_variant_ok(v, d)) {
         if (d.tw_unit) {
             switch (d.tw_k) {
-                case 1: return twisted_t<1, true>(data, d, L, staged, s);
-                case 2: return twisted_t<2, true>(data, d, L, staged, s);
-                case 3: return twisted_t<3, true>(data, d, L, staged, s);
-                default: return twisted_t<4, true>(data, d, L, staged, s);
+                case 1: return twisted_t<1, true>(data, d, L, v, s);
+                case 2: return twisted_t<2, true>(data, d, L, v, s);
+                case 3: return twisted_t<3, true>(data, d, L, v, s);
+                default: return twisted_t<4, true>(data, d, L, v, s);
             }
         }
         switch (d.tw_k) {
-            case 1: return twisted_t<1, false>(data, d, L, staged, s);
-            case 2: return twisted_t<2, false>(data, d, L, staged, s);
-            case 3: return twisted_t<3, false>(data, d, L, staged, s);
-            default: return twisted_t<4, false>(data, d, L, staged, s);
+            case 1: return twisted_t<1, false>(data, d, L, v, s);
+            case 2: return twisted_t<2, false>(data, d, L, v, s);
+            case 3: return twisted_t<3, false>(data, d, L, v, s);
+            default: return twisted_t<4, false>(data, d, L, v, s);
         }
     }
-    if (!trans && v != SOLVE_STAGED_1 && v != SOLVE_TWISTED && v != SOLVE_TWISTED_STAGED &&
-        line_solve_variant_ok(v, d)) {
+    if (!trans && v != SOLVE_STAGED_1 && !solve_variant_twisted(v) && line_solve_variant_ok(v, d)) {
         if (kl == 1 && ku <= 1 && w <= 2) return line_solve_variant<1, 1>(v, data, d, L, s);
         if (kl == 1 && ku <= 2 && w <= 3) return line_solve_variant<1, 2>(v, data, d, L, s);
         if (kl == 2) return line_solve_variant<2, 2>(v, data, d, L, s);

@@ -10,9 +10,11 @@ namespace adsg {
 // for columns r-p .. r+p (zero outside the matrix).
 // Line-solve kernel variants chosen per direction by the context's autotuner.
 // SOLVE_TWISTED* sweep each line from both ends (a two-chain factorisation of
-// the same band; the staged form copies contiguous lines through shared
-// memory and equals the plain form on strided lines); the others follow
-// LAPACK dgbtrs's column order and give bitwise equal results.
+// the same band; on contiguous lines the staged form copies whole lines
+// through shared memory and the chunked form streams 32-row chunks; both
+// equal the plain form on strided lines, and all three give bitwise equal
+// results); the others follow LAPACK dgbtrs's column order and give bitwise
+// equal results.
 enum solve_variant_id {
     SOLVE_STAGED_1 = 0,
     SOLVE_STAGED_2 = 1,
@@ -20,9 +22,12 @@ enum solve_variant_id {
     SOLVE_GLOBAL_4 = 3,
     SOLVE_TWISTED = 4,
     SOLVE_TWISTED_STAGED = 5,
-    SOLVE_NVARIANTS = 6
+    SOLVE_TWISTED_CHUNKED = 6,
+    SOLVE_NVARIANTS = 7
 };
-inline bool solve_variant_twisted(int v) { return v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED; }
+inline bool solve_variant_twisted(int v) {
+    return v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED || v == SOLVE_TWISTED_CHUNKED;
+}
 
 struct dim_dev {
     int n = 0, p = 0, kl = 0, w = 0;  // w = kl + ku: widest upper extent of U

@@ -286,7 +286,7 @@ def test_full_size_against_oracle_one_step_sampled(big):
     assert oracle.rel_l2(got, ref) <= step_tol(_conds(dims))
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("p,elements", [
     ((2, 2, 2), (30, 7, 9)),
     ((4, 4, 4), (12, 9, 6)),
@@ -296,8 +296,9 @@ def test_full_size_against_oracle_one_step_sampled(big):
 ])
 def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypatch):
     """The autotuner's candidates (staged 1/2/4 tiles per block, in-place
-    global sweep, two-ended twisted sweep in global memory or staged through
-    shared memory) each match the oracle's dgbtrs-based ADS solve."""
+    global sweep, two-ended twisted sweep in global memory, staged through
+    shared memory or streamed in chunks) each match the oracle's dgbtrs-based
+    ADS solve."""
     monkeypatch.setenv("ADSG_SOLVE_VARIANT", str(variant))
     dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
     ctx = ads.Context(dims)
@@ -311,10 +312,10 @@ def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypa
     ctx.heat_steps_host(s, 1e-5, 2)
     assert oracle.rel_l2(s, pr.heat_steps(u, 1e-5, 2)) <= step_tol(_conds(dims)) * 2
     chosen = ctx.solve_variants()
-    assert all(0 <= v <= 5 for v in chosen)
+    assert all(0 <= v <= 6 for v in chosen)
     if variant in (0, 3):  # always applicable for p <= 4
         assert chosen == [variant] * len(p)
-    if variant in (4, 5):  # the twisted sweeps need n >= 4p + 2 along the direction
+    if variant in (4, 5, 6):  # the twisted sweeps need n >= 4p + 2 along the direction
         for d, v in zip(dims, chosen):
             assert (v == variant) == (d.dofs() >= 4 * d.p + 2)
 
@@ -427,3 +428,28 @@ def test_host_entry_reading_pinned_input_is_exact(p, elements, variant, nsteps, 
     ctx.heat_steps(d, 1e-5, nsteps)
     ctx.synchronize()
     np.testing.assert_array_equal(h, d.cpu().numpy())
+
+
+@pytest.mark.parametrize("p,elements", [((2, 2, 2), (40, 33, 20)), ((4, 4, 4), (30, 20, 18)), ((3, 3), (70, 45))])
+def test_twisted_variants_agree_bitwise(p, elements, cuda, monkeypatch):
+    """The two-ended sweep in global memory (4), with whole lines staged in
+    shared memory (5) and streamed in 32-row chunks (6) perform the same
+    operations in the same order: identical results, plain and row-scaled."""
+    import torch
+
+    out = []
+    for v in ("4", "5", "6"):
+        monkeypatch.setenv("ADSG_SOLVE_VARIANT", v)
+        ctx = ads.Context([ads.Dimension(pp, e) for pp, e in zip(p, elements)])
+        assert ctx.solve_variants() == [int(v)] * len(p)
+        u = np.random.default_rng(4).uniform(-1, 1, ctx.size)
+        x = u.copy()
+        ctx.ads_solve_host(x)
+        ud = torch.from_numpy(u).cuda()
+        nxt = torch.empty_like(ud)
+        ctx.heat_step(ud, nxt, 1e-5)
+        ctx.synchronize()
+        out.append((x, nxt.cpu().numpy()))
+    for x, s in out[1:]:
+        np.testing.assert_array_equal(x, out[0][0])
+        np.testing.assert_array_equal(s, out[0][1])
