@@ -254,18 +254,23 @@ def measured_peaks():
         return {}
 
 
-def profiled_traffic(stage, dofs):
+def profiled_traffic(stage, dofs, workload):
     """DRAM bytes per launch of a stage: the bytes per dof measured by ncu
     (dram__bytes_read.sum + dram__bytes_write.sum, committed in
-    profiles/traffic_per_dof.md) times this workload's dofs, or None."""
+    profiles/traffic_per_dof.md) for this workload -- or, for a workload
+    without its own row, the row of the larger-than-L2 p=4 workload -- times
+    this workload's dofs; None when neither exists."""
     path = os.path.join(ROOT, "profiles", "traffic_per_dof.md")
+    rows = {}
     try:
         for ln in open(path):
-            if ln.startswith(f"| {stage} |"):
-                return float(ln.split("|")[3].strip()) * dofs
-    except (OSError, ValueError, IndexError):
-        pass
-    return None
+            cells = [c.strip() for c in ln.split("|")]
+            if len(cells) > 4 and cells[1] == stage:
+                rows[cells[2]] = float(cells[4])
+    except (OSError, ValueError):
+        return None
+    per_dof = rows.get(workload, rows.get("heat3d_p4_256"))
+    return None if per_dof is None else per_dof * dofs
 
 
 def run_ours(args, cfg):
@@ -389,7 +394,7 @@ def run_ours(args, cfg):
     peaks = measured_peaks()
     roof = {"bound": "fp64", "kernel": dom, "achieved": d["tflops"], "peak": peak_fp64, "unit": "TFLOP/s",
             "frac": d["tflops"] / peak_fp64,
-            "traffic": profiled_traffic(dom, size),
+            "traffic": profiled_traffic(dom, size, args.workload),
             "peak_source": "cuBLAS DGEMM 4096^3 measured live in bench.py (GB300 FP64 is not in "
                            "MEASURED_PEAKS.json)",
             "flop_convention": "FP64 operations of the implemented algorithm (pair sums on symmetric band rows, "
