@@ -410,7 +410,7 @@ def run_ours(args, cfg):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: L2 projection of prod sin(pi x_d) + seeded SplitMix64 noise in [-1e-2, 1e-2]",
         "config": {**cfg, "l2": "flushed before every timed step (512 MiB memset outside the step interval)",
-                   "solve_variants": ctx.solve_variants(), "launch_pdl": ctx.launch_pdl(),
+                   "solve_variants": ctx.solve_variants(), "step_solve_variants": ctx.step_solve_variants(), "launch_pdl": ctx.launch_pdl(),
                    "fused_x": ctx.fused_x(), "step_1block": ctx.step_1block(),
                    "parallelism": f"replicas x{world}", "rhs": "factored quadrature (1D Gauss-assembled bands)"},
         "e2e": {"value": e2e, "unit": "DOF-updates/s", "h2d_bytes_per_step": 8 * size, "d2h_bytes_per_step": 8 * size,

@@ -112,6 +112,7 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_stage_times": (i, [vp, _c_double_p, ctypes.POINTER(ctypes.c_longlong)]),
         "adsg_ctx_stage_work": (i, [vp, _c_double_p, _c_double_p]),
         "adsg_ctx_solve_variants": (i, [vp, _c_int_p]),
+        "adsg_ctx_step_solve_variants": (i, [vp, _c_int_p]),
         "adsg_ctx_launch_pdl": (i, [vp]),
         "adsg_ctx_fused_x": (i, [vp]),
         "adsg_ctx_step_1block": (i, [vp]),
@@ -312,6 +313,12 @@ class Context:
         """Line-solve variant per direction picked by the autotuner (see ads_gb300.h)."""
         v = np.zeros(3, np.int32)
         _check(library().adsg_ctx_solve_variants(self._h, _iptr(v)))
+        return [int(x) for x in v[: len(self.dims)]]
+
+    def step_solve_variants(self) -> list:
+        """Line-solve variant per direction of the explicit step (see ads_gb300.h)."""
+        v = np.zeros(3, np.int32)
+        _check(library().adsg_ctx_step_solve_variants(self._h, _iptr(v)))
         return [int(x) for x in v[: len(self.dims)]]
 
     def launch_pdl(self) -> bool:

@@ -593,6 +593,30 @@ std::map<std::string, int> g_autotune_cache;
 // (0..5) forces one variant where applicable; ADSG_AUTOTUNE_LOG=1 prints each
 // candidate's time to stderr.  A candidate whose launch reports an error is
 // dropped (the error is cleared so that it cannot leak into the next one).
+// Device time of three line solves of direction D on the context's state
+// buffer, after one warm-up launch; a launch error is returned.
+cudaError_t time_line_solve(adsg_ctx* c, const dim_dev& D, const line_layout& L, cudaEvent_t a, cudaEvent_t b,
+                            float* ms) {
+    cudaGetLastError();
+    cudaError_t e = launch_line_solve(c->ping, D, L, 0, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_line_solve(c->ping, D, L, 0, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+    return e;
+}
+
+std::string autotune_key(const adsg_ctx* c, int d) {
+    const dim_dev& D = c->dims[d];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    char key[192];
+    std::snprintf(key, sizeof key, "%d|%d|%d,%d,%d|%d|%d,%d,%d,%d,%d,%d,%d", dev, c->ndim, c->n[0], c->n[1], c->n[2], d,
+                  D.p, D.kl, D.w, D.ku_regular, D.fwd_fast, D.bwd_fast, D.tw_k);
+    return key;
+}
+
 int autotune_solves(adsg_ctx* c) {
     const char* force = std::getenv("ADSG_SOLVE_VARIANT");
     int forced = -1;
@@ -618,11 +642,7 @@ int autotune_solves(adsg_ctx* c) {
         }
         // one decision per (device, shape, direction) and process, so that
         // contexts of the same shape run the same kernels (bitwise equal results)
-        int dev = 0;
-        cudaGetDevice(&dev);
-        char key[192];
-        std::snprintf(key, sizeof key, "%d|%d|%d,%d,%d|%d|%d,%d,%d,%d,%d,%d,%d", dev, c->ndim, c->n[0], c->n[1], c->n[2], d,
-                      D.p, D.kl, D.w, D.ku_regular, D.fwd_fast, D.bwd_fast, D.tw_k);
+        const std::string key = autotune_key(c, d);
         {
             std::lock_guard<std::mutex> g(g_autotune_lock);
             auto it = g_autotune_cache.find(key);
@@ -637,14 +657,8 @@ int autotune_solves(adsg_ctx* c) {
         for (int v = 0; v < SOLVE_NVARIANTS; ++v) {
             if (!line_solve_variant_ok(v, D)) continue;
             D.solve_variant = v;
-            cudaGetLastError();
-            cudaError_t e = launch_line_solve(c->ping, D, L, 0, c->stream);  // warm-up
-            if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
-            for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_line_solve(c->ping, D, L, 0, c->stream);
-            if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
-            if (e == cudaSuccess) e = cudaEventSynchronize(b);
             float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            const cudaError_t e = time_line_solve(c, D, L, a, b, &ms);
             if (e != cudaSuccess) {
                 if (log)
                     std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d variant %d dropped: %s\n", d, D.n, v,
@@ -707,10 +721,18 @@ int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     return enqueue_solve_with(c, c->sdims, next, 0, fused ? 1 : 0);
 }
 
-// Builds the step's view of direction d once its solve variant is chosen.
+// Builds the step's view of direction d once the solve variant of ads_solve
+// is chosen.  With the two-ended tables at hand the step divides the right-hand
+// side's rows by the pivots (folded into the band rows), which lets the
+// two-ended sweeps skip their diagonal multiplies; where ads_solve kept a
+// LAPACK-order variant, those unit-diagonal sweeps are timed against it and
+// the step takes them when they are at least 5% faster.
 int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tables* tw) {
     c->sdims[d] = c->dims[d];
-    if (!tw || !solve_variant_twisted(c->dims[d].solve_variant)) return 0;
+    if (!tw) return 0;
+    const bool tw_chosen = solve_variant_twisted(c->dims[d].solve_variant);
+    const char* force = std::getenv("ADSG_SOLVE_VARIANT");
+    if (!tw_chosen && force && *force) return 0;  // a forced variant rules both views
     twisted_tables u;
     std::vector<double> scale;
     scale_twisted(*tw, h.n, u, scale);
@@ -734,7 +756,7 @@ int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tab
     if (e == cudaSuccess) e = A.upload(&g, u.g.data(), u.g.size(), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors die here
     if (e != cudaSuccess) return fail_cuda(e, "step tables");
-    dim_dev& S = c->sdims[d];
+    dim_dev S = c->dims[d];
     S.mrow = sm;
     S.krow = sk;
     S.tw_lmul = l;
@@ -742,6 +764,61 @@ int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tab
     S.tw_rdiag = rd;
     S.tw_g = g;
     S.tw_unit = 1;
+    if (!tw_chosen) {
+        const std::string key = autotune_key(c, d) + "|step";
+        int pick = -1;
+        {
+            std::lock_guard<std::mutex> lk(g_autotune_lock);
+            auto it = g_autotune_cache.find(key);
+            if (it != g_autotune_cache.end()) pick = it->second;
+        }
+        if (pick < 0) {
+            const char* logv = std::getenv("ADSG_AUTOTUNE_LOG");
+            const bool log = logv && *logv && *logv != '0';
+            const line_layout L = make_line_layout(c->n, c->ndim, d);
+            cudaEvent_t a, b;
+            ADSG_CUDA_TRY(cudaEventCreate(&a), "event");
+            if (cudaEventCreate(&b) != cudaSuccess) {
+                cudaEventDestroy(a);
+                return fail_cuda(cudaGetLastError(), "event");
+            }
+            float plain = 1e30f, best = 1e30f;
+            pick = c->dims[d].solve_variant;
+            if (time_line_solve(c, c->dims[d], L, a, b, &plain) != cudaSuccess) plain = 1e30f;
+            for (int v : {SOLVE_TWISTED, SOLVE_TWISTED_STAGED, SOLVE_TWISTED_CHUNKED}) {
+                S.solve_variant = v;
+                if (!line_solve_variant_ok(v, S)) continue;
+                float ms = 0.f;
+                const cudaError_t te = time_line_solve(c, S, L, a, b, &ms);
+                if (log)
+                    std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d step view variant %d %s %.2f us (plain %.2f)\n",
+                                 d, S.n, v, te == cudaSuccess ? "" : cudaGetErrorString(te), ms * 1000.f / 3,
+                                 plain * 1000.f / 3);
+                if (te != cudaSuccess) {
+                    cudaGetLastError();
+                    const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+                    if (e2 != cudaSuccess) {
+                        cudaEventDestroy(a);
+                        cudaEventDestroy(b);
+                        return fail_cuda(e2, "step autotune");
+                    }
+                    continue;
+                }
+                if (ms < best && ms < 0.95f * plain) {
+                    best = ms;
+                    pick = v;
+                }
+            }
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            cudaGetLastError();
+            std::lock_guard<std::mutex> lk(g_autotune_lock);
+            g_autotune_cache[key] = pick;
+        }
+        if (!solve_variant_twisted(pick)) return 0;  // the plain view stays
+        S.solve_variant = pick;
+    }
+    c->sdims[d] = S;
     c->band_dt = std::nan("");  // the scaled dt bands are built on the next step
     return 0;
 }
@@ -1206,6 +1283,13 @@ int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!variants) return fail(-2, "variants is NULL");
     for (int d = 0; d < 3; ++d) variants[d] = d < ctx->ndim ? ctx->dims[d].solve_variant : -1;
+    return 0;
+}
+
+int adsg_ctx_step_solve_variants(const adsg_ctx* ctx, int* variants) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!variants) return fail(-2, "variants is NULL");
+    for (int d = 0; d < 3; ++d) variants[d] = d < ctx->ndim ? ctx->sdims[d].solve_variant : -1;
     return 0;
 }
 

@@ -1,8 +1,10 @@
 // Element-wise sum-factorised quadrature of the heat form
 //     rhs_a += sum_q w_q J_e ( u v_a - dt kappa(x_q) grad u . grad v_a )
 // (reference examples/heat/heat_3d.hpp:49-67 with an optional coefficient
-// field).  One warp per element: the element's coefficient tile and its 1D
-// basis/derivative rows (basis_data::b) are staged in shared memory, u and
+// field).  One warp per group of elements (several when an element has fewer
+// items per stage than a warp has lanes, see elems_per_warp): each element's
+// coefficient tile and its 1D basis/derivative rows (basis_data::b) are
+// staged in shared memory, u and
 // grad u are interpolated to the q^d points one direction at a time, the
 // pointwise form is applied and the result is projected back with the
 // transposed 1D factors.  Elements are processed in (p+1)^d colours so that no
@@ -27,7 +29,24 @@ struct elem3_smem {
     double V00[N * Q * Q], V01[N * Q * Q], V10[N * Q * Q];  // [bz][qy][qx]
     double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
     double K0[N * N * Q], K1[N * Q * Q];
+    double J;
+    int e[3], f0[3];
+    int valid;
 };
+
+// Elements per warp: every stage of the sum factorisation has (p+1)^d or
+// (p+1)^a q^b items per element, 27 at p = 2 in 3D; one element per warp
+// leaves 5 of 32 lanes idle in every FP64 instruction.  Several elements per
+// warp (their items dealt to the lanes in turn) fill the lanes: 7 x 27 = 189
+// of 192 lane slots at p = 2.
+template <int ITEMS>
+constexpr int elems_per_warp() {
+    // 27 -> 7 (189 of 192 lane slots), 25 -> 5 (125/128), 16 -> 2, 9 -> 7
+    // (63/64), 8 -> 4, 4 -> 8; 64 and 125 items already fill the lanes
+    return ITEMS == 27 ? 7
+                       : (ITEMS == 25 ? 5
+                                      : (ITEMS == 16 ? 2 : (ITEMS == 9 ? 7 : (ITEMS == 8 ? 4 : (ITEMS == 4 ? 8 : 1)))));
+}
 
 // warps per block so that the static shared memory stays within 48 KB
 template <typename S>
@@ -35,48 +54,86 @@ constexpr int warps_for() {
     return sizeof(S) * 4 <= 48 * 1024 ? 4 : (sizeof(S) * 3 <= 48 * 1024 ? 3 : (sizeof(S) * 2 <= 48 * 1024 ? 2 : 1));
 }
 
-// FORM: the general pointwise form of point_form (kappa and dt unused).
-template <int P, int Q, bool FORM = false, int kWarpsPerBlock = warps_for<elem3_smem<P + 1, Q>>()>
+template <typename S, int EPW>
+struct elem_group {
+    S el[EPW];
+};
+
+// f(S, t) for every item t < ITEMS of every valid element of the warp
+// (unrolled: a lane's items are independent, so their loads and FMA chains
+// overlap, which is what hides latency with few warps per SM)
+template <int ITEMS, int EPW, typename S, typename F>
+__device__ __forceinline__ void each_item(S* el, int lane, F&& f) {
+    constexpr int kIters = (EPW * ITEMS + 31) / 32;
+#pragma unroll
+    for (int k = 0; k < kIters; ++k) {
+        const int it = lane + 32 * k;
+        if (it < EPW * ITEMS) {
+            S& e = el[it / ITEMS];
+            if (e.valid) f(e, it % ITEMS);
+        }
+    }
+}
+
+// FORM: the general pointwise form of point_form (kappa and dt unused; one
+// element per warp, whose D terms are summed across the warp).
+template <int P, int Q, bool FORM = false, int EPW = (FORM ? 1 : elems_per_warp<(P + 1) * (P + 1) * (P + 1)>()),
+          int kWarpsPerBlock = warps_for<elem_group<elem3_smem<P + 1, Q>, EPW>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem3_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
                  dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt,
                  point_form F) {
     constexpr int N = P + 1;
-    __shared__ elem3_smem<N, Q> sm_all[kWarpsPerBlock];
+    using S_t = elem3_smem<N, Q>;
+    __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
-    if (wid >= static_cast<long long>(mx) * my * mz) return;
-    elem3_smem<N, Q>& S = sm_all[warp];
-    const int iz = static_cast<int>(wid % mz);
-    const int iy = static_cast<int>((wid / mz) % my);
-    const int ix = static_cast<int>(wid / (static_cast<long long>(mz) * my));
-    const int e[3] = {cx + ix * N, cy + iy * N, cz + iz * N};
-    const int f0 = X.first[e[0]], f1 = Y.first[e[1]], f2 = Z.first[e[2]];
+    const long long count = static_cast<long long>(mx) * my * mz;
+    if (wid * EPW >= count) return;
+    S_t* el = sm_all[warp].el;
+    if (lane < EPW) {
+        S_t& S = el[lane];
+        const long long id = wid * EPW + lane;
+        S.valid = id < count;
+        if (S.valid) {
+            const int iz = static_cast<int>(id % mz);
+            const int iy = static_cast<int>((id / mz) % my);
+            const int ix = static_cast<int>(id / (static_cast<long long>(mz) * my));
+            S.e[0] = cx + ix * N;
+            S.e[1] = cy + iy * N;
+            S.e[2] = cz + iz * N;
+            S.f0[0] = X.first[S.e[0]];
+            S.f0[1] = Y.first[S.e[1]];
+            S.f0[2] = Z.first[S.e[2]];
+            S.J = X.jac[S.e[0]] * Y.jac[S.e[1]] * Z.jac[S.e[2]];
+        }
+    }
+    __syncwarp();
     const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
 
     // stage coefficients and tables
-    for (int t = lane; t < N * N * N; t += 32) {
+    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
-        const long long g = (f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az);
+        const long long g = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
         S.c[t] = u ? u[g] : 0.0;
         S.kc[t] = kappa ? kappa[g] : 0.0;
-    }
-    for (int t = lane; t < Q * N; t += 32) {
+    });
+    each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
-        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
-        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
-        const double* bz = Z.btab + ((static_cast<long long>(e[2]) * Q + q) * 2) * N;
+        const double* bx = X.btab + ((static_cast<long long>(S.e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(S.e[1]) * Q + q) * 2) * N;
+        const double* bz = Z.btab + ((static_cast<long long>(S.e[2]) * Q + q) * 2) * N;
         S.B[0][t] = bx[a];
         S.dB[0][t] = bx[N + a];
         S.B[1][t] = by[a];
         S.dB[1][t] = by[N + a];
         S.B[2][t] = bz[a];
         S.dB[2][t] = bz[N + a];
-    }
+    });
     __syncwarp();
     // x: T0/T1[bz][by][qx]
-    for (int t = lane; t < N * N * Q; t += 32) {
+    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, byz = t / Q;
         double a0 = 0.0, a1 = 0.0, k0 = 0.0;
 #pragma unroll
@@ -89,10 +146,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.T0[t] = a0;
         S.T1[t] = a1;
         if (kappa) S.K0[t] = k0;
-    }
+    });
     __syncwarp();
     // y: V..[bz][qy][qx]
-    for (int t = lane; t < N * Q * Q; t += 32) {
+    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, bz = t / (Q * Q);
         double v00 = 0.0, v01 = 0.0, v10 = 0.0, k1 = 0.0;
 #pragma unroll
@@ -108,13 +165,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.V01[t] = v01;
         S.V10[t] = v10;
         if (kappa) S.K1[t] = k1;
-    }
+    });
     __syncwarp();
     // z + pointwise form: f = W u, g* = -dt kappa W d*u
     // (FORM: f = W (alpha u + gamma), g* = W beta d*u, and W delta summed)
-    const double J = X.jac[e[0]] * Y.jac[e[1]] * Z.jac[e[2]];
     double dsum = 0.0;
-    for (int t = lane; t < Q * Q * Q; t += 32) {
+    each_item<Q * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
         double uv = 0.0, ux = 0.0, uy = 0.0, uz = 0.0, kv = 0.0;
 #pragma unroll
@@ -127,11 +183,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             ux = fma(bz, S.V10[src], ux);
             if (kappa) kv = fma(bz, S.K1[src], kv);
         }
-        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * J;
+        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
         if (FORM) {
             const long long Qx = static_cast<long long>(X.elements) * Q, Qy = static_cast<long long>(Y.elements) * Q;
-            const long long pq = (static_cast<long long>(e[0]) * Q + qx) +
-                                 Qx * ((static_cast<long long>(e[1]) * Q + qy) + Qy * (static_cast<long long>(e[2]) * Q + qz));
+            const long long pq = (static_cast<long long>(S.e[0]) * Q + qx) +
+                                 Qx * ((static_cast<long long>(S.e[1]) * Q + qy) +
+                                       Qy * (static_cast<long long>(S.e[2]) * Q + qz));
             const double al = F.alpha + (F.alpha_q ? F.alpha_q[pq] : 0.0);
             const double be = F.beta + (F.beta_q ? F.beta_q[pq] : 0.0);
             const double ga = F.gamma + (F.gamma_q ? F.gamma_q[pq] : 0.0);
@@ -149,14 +206,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.gy[t] = uy * g;
             S.gz[t] = uz * g;
         }
-    }
-    if (FORM) {
+    });
+    if (FORM) {  // one element per warp
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
     }
     __syncwarp();
     // z back: V00 <- S0[az][qy][qx], V01 <- Sx, V10 <- Sy
-    for (int t = lane; t < N * Q * Q; t += 32) {
+    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, az = t / (Q * Q);
         double s0 = 0.0, sx = 0.0, sy = 0.0;
 #pragma unroll
@@ -171,10 +228,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.V00[t] = s0;
         S.V01[t] = sx;
         S.V10[t] = sy;
-    }
+    });
     __syncwarp();
     // y back: T0 <- R0[az][ay][qx], T1 <- Rx
-    for (int t = lane; t < N * N * Q; t += 32) {
+    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, ay = (t / Q) % N, az = t / (Q * N);
         double r0 = 0.0, rx = 0.0;
 #pragma unroll
@@ -187,10 +244,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         }
         S.T0[t] = r0;
         S.T1[t] = rx;
-    }
+    });
     __syncwarp();
     // x back and scatter (this colour owns every dof of the element)
-    for (int t = lane; t < N * N * N; t += 32) {
+    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
         double o = 0.0;
 #pragma unroll
@@ -199,9 +256,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             o = fma(S.B[0][q * N + ax], S.T0[src], o);
             o = fma(S.dB[0][q * N + ax], S.T1[src], o);
         }
-        const long long g = (f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az);
+        const long long g = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
         rhs[g] += FORM ? o + dsum : o;
-    }
+    });
 }
 
 template <int N, int Q>
@@ -210,40 +267,55 @@ struct elem2_smem {
     double B[2][Q * N], dB[2][Q * N];
     double T0[N * Q], T1[N * Q], K0[N * Q];  // [by][qx]
     double f[Q * Q], gx[Q * Q], gy[Q * Q];
+    double J;
+    int e[2], f0[2];
+    int valid;
 };
 
-template <int P, int Q, bool FORM = false, int kWarpsPerBlock = warps_for<elem2_smem<P + 1, Q>>()>
+template <int P, int Q, bool FORM = false, int EPW = (FORM ? 1 : elems_per_warp<(P + 1) * (P + 1)>()),
+          int kWarpsPerBlock = warps_for<elem_group<elem2_smem<P + 1, Q>, EPW>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem2_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
                  dim_dev X, dim_dev Y, int cx, int cy, int mx, int my, double dt, point_form F) {
     constexpr int N = P + 1;
-    __shared__ elem2_smem<N, Q> sm_all[kWarpsPerBlock];
+    using S_t = elem2_smem<N, Q>;
+    __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
-    if (wid >= static_cast<long long>(mx) * my) return;
-    elem2_smem<N, Q>& S = sm_all[warp];
-    const int iy = static_cast<int>(wid % my);
-    const int ix = static_cast<int>(wid / my);
-    const int e[2] = {cx + ix * N, cy + iy * N};
-    const int f0 = X.first[e[0]], f1 = Y.first[e[1]];
+    const long long count = static_cast<long long>(mx) * my;
+    if (wid * EPW >= count) return;
+    S_t* el = sm_all[warp].el;
+    if (lane < EPW) {
+        S_t& S = el[lane];
+        const long long id = wid * EPW + lane;
+        S.valid = id < count;
+        if (S.valid) {
+            S.e[0] = cx + static_cast<int>(id / my) * N;
+            S.e[1] = cy + static_cast<int>(id % my) * N;
+            S.f0[0] = X.first[S.e[0]];
+            S.f0[1] = Y.first[S.e[1]];
+            S.J = X.jac[S.e[0]] * Y.jac[S.e[1]];
+        }
+    }
+    __syncwarp();
     const long long nx = X.n;
-    for (int t = lane; t < N * N; t += 32) {
-        const long long g = (f0 + t % N) + nx * (f1 + t / N);
+    each_item<N * N, EPW>(el, lane, [&](S_t& S, int t) {
+        const long long g = (S.f0[0] + t % N) + nx * (S.f0[1] + t / N);
         S.c[t] = u ? u[g] : 0.0;
         S.kc[t] = kappa ? kappa[g] : 0.0;
-    }
-    for (int t = lane; t < Q * N; t += 32) {
+    });
+    each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
-        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
-        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
+        const double* bx = X.btab + ((static_cast<long long>(S.e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(S.e[1]) * Q + q) * 2) * N;
         S.B[0][t] = bx[a];
         S.dB[0][t] = bx[N + a];
         S.B[1][t] = by[a];
         S.dB[1][t] = by[N + a];
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * Q; t += 32) {
+    each_item<N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, by = t / Q;
         double a0 = 0.0, a1 = 0.0, k0 = 0.0;
 #pragma unroll
@@ -255,11 +327,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.T0[t] = a0;
         S.T1[t] = a1;
         if (kappa) S.K0[t] = k0;
-    }
+    });
     __syncwarp();
-    const double J = X.jac[e[0]] * Y.jac[e[1]];
     double dsum = 0.0;
-    for (int t = lane; t < Q * Q; t += 32) {
+    each_item<Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = t / Q;
         double uv = 0.0, ux = 0.0, uy = 0.0, kv = 0.0;
 #pragma unroll
@@ -270,10 +341,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             ux = fma(by, S.T1[b * Q + qx], ux);
             if (kappa) kv = fma(by, S.K0[b * Q + qx], kv);
         }
-        const double W = X.wq[qx] * Y.wq[qy] * J;
+        const double W = X.wq[qx] * Y.wq[qy] * S.J;
         if (FORM) {
             const long long Qx = static_cast<long long>(X.elements) * Q;
-            const long long pq = (static_cast<long long>(e[0]) * Q + qx) + Qx * (static_cast<long long>(e[1]) * Q + qy);
+            const long long pq =
+                (static_cast<long long>(S.e[0]) * Q + qx) + Qx * (static_cast<long long>(S.e[1]) * Q + qy);
             const double al = F.alpha + (F.alpha_q ? F.alpha_q[pq] : 0.0);
             const double be = F.beta + (F.beta_q ? F.beta_q[pq] : 0.0);
             const double ga = F.gamma + (F.gamma_q ? F.gamma_q[pq] : 0.0);
@@ -289,14 +361,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.gx[t] = ux * g;
             S.gy[t] = uy * g;
         }
-    }
-    if (FORM) {
+    });
+    if (FORM) {  // one element per warp
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
     }
     __syncwarp();
     // y back: T0 <- S0[ay][qx], T1 <- Sx
-    for (int t = lane; t < N * Q; t += 32) {
+    each_item<N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, ay = t / Q;
         double s0 = 0.0, sx = 0.0;
 #pragma unroll
@@ -308,9 +380,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         }
         S.T0[t] = s0;
         S.T1[t] = sx;
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * N; t += 32) {
+    each_item<N * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int ax = t % N, ay = t / N;
         double o = 0.0;
 #pragma unroll
@@ -318,8 +390,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             o = fma(S.B[0][q * N + ax], S.T0[ay * Q + q], o);
             o = fma(S.dB[0][q * N + ax], S.T1[ay * Q + q], o);
         }
-        rhs[(f0 + ax) + nx * (f1 + ay)] += FORM ? o + dsum : o;
-    }
+        rhs[(S.f0[0] + ax) + nx * (S.f0[1] + ay)] += FORM ? o + dsum : o;
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -338,44 +410,63 @@ struct kg3_smem {
     double Vu00[N * Q * Q], Vu01[N * Q * Q], Vu10[N * Q * Q];              // [bz][qy][qx]
     double Vm00[N * Q * Q], Vm01[N * Q * Q], Vm10[N * Q * Q];
     double s[Q * Q * Q];
+    double J;
+    int e[3], f0[3];
+    int valid;
 };
 
-template <int P, int Q, int kWarpsPerBlock = warps_for<kg3_smem<P + 1, Q>>()>
+template <int P, int Q, int EPW = elems_per_warp<(P + 1) * (P + 1) * (P + 1)>(),
+          int kWarpsPerBlock = warps_for<elem_group<kg3_smem<P + 1, Q>, EPW>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     kgrad3_kernel(const double* __restrict__ u, const double* __restrict__ mu, double* __restrict__ g, dim_dev X,
                   dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt) {
     constexpr int N = P + 1;
-    __shared__ kg3_smem<N, Q> sm_all[kWarpsPerBlock];
+    using S_t = kg3_smem<N, Q>;
+    __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
-    if (wid >= static_cast<long long>(mx) * my * mz) return;
-    kg3_smem<N, Q>& S = sm_all[warp];
-    const int iz = static_cast<int>(wid % mz);
-    const int iy = static_cast<int>((wid / mz) % my);
-    const int ix = static_cast<int>(wid / (static_cast<long long>(mz) * my));
-    const int e[3] = {cx + ix * N, cy + iy * N, cz + iz * N};
-    const int f0 = X.first[e[0]], f1 = Y.first[e[1]], f2 = Z.first[e[2]];
+    const long long count = static_cast<long long>(mx) * my * mz;
+    if (wid * EPW >= count) return;
+    S_t* el = sm_all[warp].el;
+    if (lane < EPW) {
+        S_t& S = el[lane];
+        const long long id = wid * EPW + lane;
+        S.valid = id < count;
+        if (S.valid) {
+            const int iz = static_cast<int>(id % mz);
+            const int iy = static_cast<int>((id / mz) % my);
+            const int ix = static_cast<int>(id / (static_cast<long long>(mz) * my));
+            S.e[0] = cx + ix * N;
+            S.e[1] = cy + iy * N;
+            S.e[2] = cz + iz * N;
+            S.f0[0] = X.first[S.e[0]];
+            S.f0[1] = Y.first[S.e[1]];
+            S.f0[2] = Z.first[S.e[2]];
+            S.J = X.jac[S.e[0]] * Y.jac[S.e[1]] * Z.jac[S.e[2]];
+        }
+    }
+    __syncwarp();
     const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
-    for (int t = lane; t < N * N * N; t += 32) {
-        const long long gi = (f0 + t % N) + nx * (f1 + (t / N) % N) + nxy * (f2 + t / (N * N));
+    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
+        const long long gi = (S.f0[0] + t % N) + nx * (S.f0[1] + (t / N) % N) + nxy * (S.f0[2] + t / (N * N));
         S.c[t] = u[gi];
         S.m[t] = mu[gi];
-    }
-    for (int t = lane; t < Q * N; t += 32) {
+    });
+    each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
-        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
-        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
-        const double* bz = Z.btab + ((static_cast<long long>(e[2]) * Q + q) * 2) * N;
+        const double* bx = X.btab + ((static_cast<long long>(S.e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(S.e[1]) * Q + q) * 2) * N;
+        const double* bz = Z.btab + ((static_cast<long long>(S.e[2]) * Q + q) * 2) * N;
         S.B[0][t] = bx[a];
         S.dB[0][t] = bx[N + a];
         S.B[1][t] = by[a];
         S.dB[1][t] = by[N + a];
         S.B[2][t] = bz[a];
         S.dB[2][t] = bz[N + a];
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * N * Q; t += 32) {
+    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, byz = t / Q;
         double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
 #pragma unroll
@@ -390,9 +481,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.Tu1[t] = a1;
         S.Tm0[t] = b0;
         S.Tm1[t] = b1;
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * Q * Q; t += 32) {
+    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, bz = t / (Q * Q);
         double u00 = 0.0, u01 = 0.0, u10 = 0.0, m00 = 0.0, m01 = 0.0, m10 = 0.0;
 #pragma unroll
@@ -412,10 +503,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.Vm00[t] = m00;
         S.Vm01[t] = m01;
         S.Vm10[t] = m10;
-    }
+    });
     __syncwarp();
-    const double J = X.jac[e[0]] * Y.jac[e[1]] * Z.jac[e[2]];
-    for (int t = lane; t < Q * Q * Q; t += 32) {
+    each_item<Q * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
         double ux = 0.0, uy = 0.0, uz = 0.0, mx_ = 0.0, my_ = 0.0, mz_ = 0.0;
 #pragma unroll
@@ -429,34 +519,34 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             my_ = fma(bz, S.Vm01[src], my_);
             mx_ = fma(bz, S.Vm10[src], mx_);
         }
-        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * J;
+        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
         S.s[t] = -dt * W * (ux * mx_ + uy * my_ + uz * mz_);
-    }
+    });
     __syncwarp();
     // project s onto the value factors: z, then y, then x
-    for (int t = lane; t < N * Q * Q; t += 32) {
+    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, az = t / (Q * Q);
         double a = 0.0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) a = fma(S.B[2][q * N + az], S.s[(q * Q + qy) * Q + qx], a);
         S.Vu00[t] = a;
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * N * Q; t += 32) {
+    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, ay = (t / Q) % N, az = t / (Q * N);
         double a = 0.0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) a = fma(S.B[1][q * N + ay], S.Vu00[(az * Q + q) * Q + qx], a);
         S.Tu0[t] = a;
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * N * N; t += 32) {
+    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
         double a = 0.0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) a = fma(S.B[0][q * N + ax], S.Tu0[(az * N + ay) * Q + q], a);
-        g[(f0 + ax) + nx * (f1 + ay) + nxy * (f2 + az)] += a;
-    }
+        g[(S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az)] += a;
+    });
 }
 
 template <int N, int Q>
@@ -465,38 +555,55 @@ struct kg2_smem {
     double B[2][Q * N], dB[2][Q * N];
     double Tu0[N * Q], Tu1[N * Q], Tm0[N * Q], Tm1[N * Q];
     double s[Q * Q];
+    double J;
+    int e[2], f0[2];
+    int valid;
 };
 
-template <int P, int Q, int kWarpsPerBlock = warps_for<kg2_smem<P + 1, Q>>()>
+template <int P, int Q, int EPW = elems_per_warp<(P + 1) * (P + 1)>(),
+          int kWarpsPerBlock = warps_for<elem_group<kg2_smem<P + 1, Q>, EPW>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     kgrad2_kernel(const double* __restrict__ u, const double* __restrict__ mu, double* __restrict__ g, dim_dev X,
                   dim_dev Y, int cx, int cy, int mx, int my, double dt) {
     constexpr int N = P + 1;
-    __shared__ kg2_smem<N, Q> sm_all[kWarpsPerBlock];
+    using S_t = kg2_smem<N, Q>;
+    __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
-    if (wid >= static_cast<long long>(mx) * my) return;
-    kg2_smem<N, Q>& S = sm_all[warp];
-    const int e[2] = {cx + static_cast<int>(wid / my) * N, cy + static_cast<int>(wid % my) * N};
-    const int f0 = X.first[e[0]], f1 = Y.first[e[1]];
+    const long long count = static_cast<long long>(mx) * my;
+    if (wid * EPW >= count) return;
+    S_t* el = sm_all[warp].el;
+    if (lane < EPW) {
+        S_t& S = el[lane];
+        const long long id = wid * EPW + lane;
+        S.valid = id < count;
+        if (S.valid) {
+            S.e[0] = cx + static_cast<int>(id / my) * N;
+            S.e[1] = cy + static_cast<int>(id % my) * N;
+            S.f0[0] = X.first[S.e[0]];
+            S.f0[1] = Y.first[S.e[1]];
+            S.J = X.jac[S.e[0]] * Y.jac[S.e[1]];
+        }
+    }
+    __syncwarp();
     const long long nx = X.n;
-    for (int t = lane; t < N * N; t += 32) {
-        const long long gi = (f0 + t % N) + nx * (f1 + t / N);
+    each_item<N * N, EPW>(el, lane, [&](S_t& S, int t) {
+        const long long gi = (S.f0[0] + t % N) + nx * (S.f0[1] + t / N);
         S.c[t] = u[gi];
         S.m[t] = mu[gi];
-    }
-    for (int t = lane; t < Q * N; t += 32) {
+    });
+    each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
-        const double* bx = X.btab + ((static_cast<long long>(e[0]) * Q + q) * 2) * N;
-        const double* by = Y.btab + ((static_cast<long long>(e[1]) * Q + q) * 2) * N;
+        const double* bx = X.btab + ((static_cast<long long>(S.e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(S.e[1]) * Q + q) * 2) * N;
         S.B[0][t] = bx[a];
         S.dB[0][t] = bx[N + a];
         S.B[1][t] = by[a];
         S.dB[1][t] = by[N + a];
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * Q; t += 32) {
+    each_item<N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, by = t / Q;
         double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
 #pragma unroll
@@ -511,11 +618,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.Tu1[t] = a1;
         S.Tm0[t] = b0;
         S.Tm1[t] = b1;
-    }
+    });
     __syncwarp();
-    const double J = X.jac[e[0]] * Y.jac[e[1]];
-    double dsum = 0.0;
-    for (int t = lane; t < Q * Q; t += 32) {
+    each_item<Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = t / Q;
         double ux = 0.0, uy = 0.0, mx_ = 0.0, my_ = 0.0;
 #pragma unroll
@@ -526,25 +631,25 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             my_ = fma(dby, S.Tm0[b * Q + qx], my_);
             mx_ = fma(by, S.Tm1[b * Q + qx], mx_);
         }
-        const double W = X.wq[qx] * Y.wq[qy] * J;
+        const double W = X.wq[qx] * Y.wq[qy] * S.J;
         S.s[t] = -dt * W * (ux * mx_ + uy * my_);
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * Q; t += 32) {
+    each_item<N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, ay = t / Q;
         double a = 0.0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) a = fma(S.B[1][q * N + ay], S.s[q * Q + qx], a);
         S.Tu0[t] = a;
-    }
+    });
     __syncwarp();
-    for (int t = lane; t < N * N; t += 32) {
+    each_item<N * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int ax = t % N, ay = t / N;
         double a = 0.0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) a = fma(S.B[0][q * N + ax], S.Tu0[ay * Q + q], a);
-        g[(f0 + ax) + nx * (f1 + ay)] += a;
-    }
+        g[(S.f0[0] + ax) + nx * (S.f0[1] + ay)] += a;
+    });
 }
 
 int colour_count(int E, int c, int N) { return E > c ? (E - c + N - 1) / N : 0; }
@@ -553,8 +658,10 @@ template <int P, bool FORM>
 cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* kappa, double* rhs, double dt,
                    const point_form& F, cudaStream_t s) {
     constexpr int N = P + 1, Q = P + 1;
-    constexpr int W3 = warps_for<elem3_smem<N, Q>>();
-    constexpr int W2 = warps_for<elem2_smem<N, Q>>();
+    constexpr int E3 = FORM ? 1 : elems_per_warp<N * N * N>();
+    constexpr int E2 = FORM ? 1 : elems_per_warp<N * N>();
+    constexpr int W3 = warps_for<elem_group<elem3_smem<N, Q>, E3>>();
+    constexpr int W2 = warps_for<elem_group<elem2_smem<N, Q>, E2>>();
     if (ndim == 3) {
         for (int cx = 0; cx < N; ++cx)
             for (int cy = 0; cy < N; ++cy)
@@ -563,7 +670,7 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                               mz = colour_count(d[2].elements, cz, N);
                     const long long work = static_cast<long long>(mx) * my * mz;
                     if (!work) continue;
-                    const long long blocks = (work + W3 - 1) / W3;
+                    const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
                     elem3_kernel<P, Q, FORM><<<blocks, 32 * W3, 0, s>>>(u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz,
                                                                          mx, my, mz, dt, F);
                 }
@@ -573,7 +680,7 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                 const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N);
                 const long long work = static_cast<long long>(mx) * my;
                 if (!work) continue;
-                const long long blocks = (work + W2 - 1) / W2;
+                const long long blocks = ((work + E2 - 1) / E2 + W2 - 1) / W2;
                 elem2_kernel<P, Q, FORM><<<blocks, 32 * W2, 0, s>>>(u, kappa, rhs, d[0], d[1], cx, cy, mx, my, dt, F);
             }
     }
@@ -584,8 +691,10 @@ template <int P>
 cudaError_t kgrad_p(int ndim, const dim_dev* d, const double* u, const double* mu, double* g, double dt,
                     cudaStream_t s) {
     constexpr int N = P + 1, Q = P + 1;
-    constexpr int W3 = warps_for<kg3_smem<N, Q>>();
-    constexpr int W2 = warps_for<kg2_smem<N, Q>>();
+    constexpr int E3 = elems_per_warp<N * N * N>();
+    constexpr int E2 = elems_per_warp<N * N>();
+    constexpr int W3 = warps_for<elem_group<kg3_smem<N, Q>, E3>>();
+    constexpr int W2 = warps_for<elem_group<kg2_smem<N, Q>, E2>>();
     if (ndim == 3) {
         for (int cx = 0; cx < N; ++cx)
             for (int cy = 0; cy < N; ++cy)
@@ -594,7 +703,7 @@ cudaError_t kgrad_p(int ndim, const dim_dev* d, const double* u, const double* m
                               mz = colour_count(d[2].elements, cz, N);
                     const long long work = static_cast<long long>(mx) * my * mz;
                     if (!work) continue;
-                    kgrad3_kernel<P, Q><<<(work + W3 - 1) / W3, 32 * W3, 0, s>>>(u, mu, g, d[0], d[1], d[2], cx, cy,
+                    kgrad3_kernel<P, Q><<<((work + E3 - 1) / E3 + W3 - 1) / W3, 32 * W3, 0, s>>>(u, mu, g, d[0], d[1], d[2], cx, cy,
                                                                               cz, mx, my, mz, dt);
                 }
     } else {
@@ -603,7 +712,7 @@ cudaError_t kgrad_p(int ndim, const dim_dev* d, const double* u, const double* m
                 const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N);
                 const long long work = static_cast<long long>(mx) * my;
                 if (!work) continue;
-                kgrad2_kernel<P, Q><<<(work + W2 - 1) / W2, 32 * W2, 0, s>>>(u, mu, g, d[0], d[1], cx, cy, mx, my, dt);
+                kgrad2_kernel<P, Q><<<((work + E2 - 1) / E2 + W2 - 1) / W2, 32 * W2, 0, s>>>(u, mu, g, d[0], d[1], cx, cy, mx, my, dt);
             }
     }
     return cudaGetLastError();

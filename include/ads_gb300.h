@@ -175,6 +175,12 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
  * forces a variant where it applies; ADSG_AUTOTUNE_LOG=1 prints the timings.
  * Decisions are cached per shape for the process. */
 int adsg_ctx_solve_variants(const adsg_ctx* ctx, int* variants);
+/* Line-solve variant per direction of the explicit step (adsg_heat_step,
+ * adsg_heat_steps*): the variant above, or, where that is 0-3 and a
+ * two-ended variant with the pivots folded into the right-hand side is at
+ * least 5% faster on this shape, that variant (4-6).  Same layout as
+ * adsg_ctx_solve_variants. */
+int adsg_ctx_step_solve_variants(const adsg_ctx* ctx, int* variants);
 /* 1 when the step's kernels use programmatic dependent launch (chosen at
  * creation by timing a few steps both ways; ADSG_PDL=0/1 forces it), 0 when
  * not, -1 for a NULL context.  Results do not depend on it. */
