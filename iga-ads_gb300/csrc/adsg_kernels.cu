@@ -805,6 +805,16 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
     sweep_global<KL, KU, UNR>(x, L.elem_stride, D);
 }
 
+// 8-byte global -> shared copy that completes asynchronously (zero-filled
+// when !valid, src then only has to be a mapped address); a lane's copies
+// are all in flight until cp_async_wait_all().
+__device__ __forceinline__ void cp_async8(double* dst, const double* src, bool valid) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // Twisted line solve.  Each line is split at n1 = n/2: lanes 0-15 of a warp
 // sweep rows [0, n1) of 16 lines top-down, lanes 16-31 rows [n1, n) of the
@@ -995,10 +1005,12 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const double* src = data + g0 * n;
     const int count = nv * n;
+#pragma unroll 4
     for (int e = lane; e < count; e += 32) {
         const int line = e / n;
-        tile[line * pitch + (e - line * n)] = src[e];
+        cp_async8(tile + line * pitch + (e - line * n), src + e, true);
     }
+    cp_async_wait_all();
     __syncwarp();
     const int line = lane & 15;
     const bool active = line < nv;
@@ -1018,6 +1030,24 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
 }
 
 size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
+
+// Warps per block (4, 2 or 1) for kernels whose warps each hold a tile of
+// per_warp bytes: the one that keeps the most warps resident per SM (228 KB
+// of shared memory, 1 KB reserved per block), the larger on a tie; 0 when
+// one warp's tile does not fit.
+int tile_warps_per_block(size_t per_warp) {
+    int best = 0, best_res = 0;
+    for (int w : {4, 2, 1}) {
+        const size_t blk = per_warp * w;
+        if (blk > 227 * 1024) continue;
+        const int res = static_cast<int>((228 * 1024) / (blk + 1024)) * w;
+        if (res > best_res) {
+            best_res = res;
+            best = w;
+        }
+    }
+    return best;
+}
 
 // ---------------------------------------------------------------------------
 // The two-ended sweep for contiguous lines, streamed in chunks.  A warp owns
@@ -1046,7 +1076,8 @@ __device__ __forceinline__ long long chunk_offset(const chunk_lines& W, int line
 }
 
 // buf[c][l][t] <- chain-local row (first[c] + dir * t) of line l, chain c
-// (0 outside the chain); dir = +1 (forward) or -1 (backward)
+// (0 outside the chain); dir = +1 (forward) or -1 (backward).  (Plain loads:
+// asynchronous copies measured slower here, unlike in the whole-line tile.)
 __device__ __forceinline__ void chunk_stage(double* buf, const chunk_lines& W, const int first[2], int dir) {
     const int lane = threadIdx.x & 31;
     for (int idx = lane; idx < 2 * 16 * kChunk; idx += 32) {
@@ -1253,9 +1284,9 @@ static cudaError_t rhs_x_solve_t(const double* in0, const double* in1, double* o
                                  const double* A1, const dim_dev& d, const line_layout& L, cudaStream_t s) {
     constexpr int UNR = K > 2 ? 4 : 8;
     const size_t per_warp = twisted_staged_smem_per_warp(d.n);
-    const int wpb = per_warp * 4 <= 227 * 1024 ? 4 : (per_warp * 2 <= 227 * 1024 ? 2 : 1);
+    const int wpb = tile_warps_per_block(per_warp);
+    if (wpb == 0) return cudaErrorInvalidConfiguration;
     const size_t smem = per_warp * wpb;
-    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
     auto kern = rhs_x_solve_kernel<K, UNR, UNIT, IN1>;
     if (smem > 48 * 1024) {
         cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(kern), smem);
@@ -1391,9 +1422,9 @@ static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& 
     const bool staged = variant == SOLVE_TWISTED_STAGED;
     if (staged && L.contiguous) {
         const size_t per_warp = twisted_staged_smem_per_warp(d.n);
-        const int wpb = per_warp * 4 <= 227 * 1024 ? 4 : (per_warp * 2 <= 227 * 1024 ? 2 : 1);
+        const int wpb = tile_warps_per_block(per_warp);
+        if (wpb == 0) return cudaErrorInvalidConfiguration;
         const size_t smem = per_warp * wpb;
-        if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
         if (smem > 48 * 1024) {
             cudaError_t e =
                 ensure_smem_attribute(reinterpret_cast<const void*>(line_solve_twisted_staged_kernel<K, UNR, UNIT>), smem);
