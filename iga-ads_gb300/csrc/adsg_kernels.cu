@@ -1031,13 +1031,14 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
 
 size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
 
-// Warps per block (4, 2 or 1) for kernels whose warps each hold a tile of
+// Warps per block (1, 2 or 4) for kernels whose warps each hold a tile of
 // per_warp bytes: the one that keeps the most warps resident per SM (228 KB
-// of shared memory, 1 KB reserved per block), the larger on a tie; 0 when
-// one warp's tile does not fit.
+// of shared memory, 1 KB reserved per block), the smaller on a tie (finer
+// blocks spread the warps over the SMs more evenly); 0 when one warp's tile
+// does not fit.
 int tile_warps_per_block(size_t per_warp) {
     int best = 0, best_res = 0;
-    for (int w : {4, 2, 1}) {
+    for (int w : {1, 2, 4}) {
         const size_t blk = per_warp * w;
         if (blk > 227 * 1024) continue;
         const int res = static_cast<int>((228 * 1024) / (blk + 1024)) * w;
@@ -1413,11 +1414,12 @@ cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out
 template <int K, bool UNIT>
 static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, int variant, cudaStream_t s) {
     constexpr int UNR = K > 2 ? 4 : 8;
+    // one warp (16 lines) per block: the FP64 pipe is per SM, and single-warp
+    // blocks spread the warps over the SMs most evenly
     if (variant == SOLVE_TWISTED_CHUNKED && L.contiguous) {
-        const long long per = 64;  // 4 warps x 16 lines
         return launch_pdl(line_solve_twisted_chunked_kernel<K, UNIT>,
-                          dim3(static_cast<unsigned>((L.nlines + per - 1) / per)), dim3(128),
-                          4 * twisted_chunked_smem_per_warp(), s, data, d, L);
+                          dim3(static_cast<unsigned>((L.nlines + 15) / 16)), dim3(32),
+                          twisted_chunked_smem_per_warp(), s, data, d, L);
     }
     const bool staged = variant == SOLVE_TWISTED_STAGED;
     if (staged && L.contiguous) {
@@ -1434,9 +1436,8 @@ static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& 
         return launch_pdl(line_solve_twisted_staged_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
                           dim3(32 * wpb), smem, s, data, d, L);
     }
-    const long long per = 64;  // 4 warps x 16 lines
-    return launch_pdl(line_solve_twisted_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
-                      dim3(128), 0, s, data, d, L);
+    return launch_pdl(line_solve_twisted_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + 15) / 16)),
+                      dim3(32), 0, s, data, d, L);
 }
 
 template <int KL, int KU>
