@@ -19,16 +19,44 @@ namespace adsg {
 namespace {
 
 
+// One element's buffers.  With the kappa field (KAPPA) every stage buffer
+// has its own storage; without it the coefficients and the x-contracted T0/T1
+// ([bz][by][qx]), dead from the pointwise stage until the y back-projection
+// rewrites T0/T1, share storage with the point values f/g*, which live exactly
+// then (the smaller tile keeps more warps per SM; with kappa the separate
+// layout measured faster).
+template <int N, int Q, bool KAPPA>
+struct elem3_smem;
+
 template <int N, int Q>
-struct elem3_smem {
+struct elem3_smem<N, Q, true> {
     double c[N * N * N];
     double kc[N * N * N];
-    double B[3][Q * N];   // B[d][q*N + a]
+    double B[3][Q * N];  // B[d][q*N + a]
     double dB[3][Q * N];
-    double T0[N * N * Q], T1[N * N * Q];          // x-contracted, [bz][by][qx]
+    double T0[N * N * Q], T1[N * N * Q];
     double V00[N * Q * Q], V01[N * Q * Q], V10[N * Q * Q];  // [bz][qy][qx]
     double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
     double K0[N * N * Q], K1[N * Q * Q];
+    double J;
+    int e[3], f0[3];
+    int valid;
+};
+
+template <int N, int Q>
+struct elem3_smem<N, Q, false> {
+    double B[3][Q * N];
+    double dB[3][Q * N];
+    double V00[N * Q * Q], V01[N * Q * Q], V10[N * Q * Q];
+    union {
+        struct {
+            double c[N * N * N];
+            double T0[N * N * Q], T1[N * N * Q];
+        };
+        struct {
+            double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
+        };
+    };
     double J;
     int e[3], f0[3];
     int valid;
@@ -77,14 +105,15 @@ __device__ __forceinline__ void each_item(S* el, int lane, F&& f) {
 
 // FORM: the general pointwise form of point_form (kappa and dt unused; one
 // element per warp, whose D terms are summed across the warp).
-template <int P, int Q, bool FORM = false, int EPW = (FORM ? 1 : elems_per_warp<(P + 1) * (P + 1) * (P + 1)>()),
-          int kWarpsPerBlock = warps_for<elem_group<elem3_smem<P + 1, Q>, EPW>>()>
+template <int P, int Q, bool FORM, bool KAPPA,
+          int EPW = (FORM ? 1 : elems_per_warp<(P + 1) * (P + 1) * (P + 1)>()),
+          int kWarpsPerBlock = warps_for<elem_group<elem3_smem<P + 1, Q, KAPPA>, EPW>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem3_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
                  dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt,
                  point_form F) {
     constexpr int N = P + 1;
-    using S_t = elem3_smem<N, Q>;
+    using S_t = elem3_smem<N, Q, KAPPA>;
     __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -117,7 +146,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
         const long long g = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
         S.c[t] = u ? u[g] : 0.0;
-        S.kc[t] = kappa ? kappa[g] : 0.0;
+        if constexpr (KAPPA) S.kc[t] = kappa[g];
     });
     each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
@@ -141,11 +170,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             const double cv = S.c[byz * N + b];
             a0 = fma(S.B[0][qx * N + b], cv, a0);
             a1 = fma(S.dB[0][qx * N + b], cv, a1);
-            if (kappa) k0 = fma(S.B[0][qx * N + b], S.kc[byz * N + b], k0);
+            if constexpr (KAPPA) k0 = fma(S.B[0][qx * N + b], S.kc[byz * N + b], k0);
         }
         S.T0[t] = a0;
         S.T1[t] = a1;
-        if (kappa) S.K0[t] = k0;
+        if constexpr (KAPPA) S.K0[t] = k0;
     });
     __syncwarp();
     // y: V..[bz][qy][qx]
@@ -159,12 +188,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             v00 = fma(by, S.T0[src], v00);
             v01 = fma(dby, S.T0[src], v01);
             v10 = fma(by, S.T1[src], v10);
-            if (kappa) k1 = fma(by, S.K0[src], k1);
+            if constexpr (KAPPA) k1 = fma(by, S.K0[src], k1);
         }
         S.V00[t] = v00;
         S.V01[t] = v01;
         S.V10[t] = v10;
-        if (kappa) S.K1[t] = k1;
+        if constexpr (KAPPA) S.K1[t] = k1;
     });
     __syncwarp();
     // z + pointwise form: f = W u, g* = -dt kappa W d*u
@@ -181,7 +210,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             uz = fma(dbz, S.V00[src], uz);
             uy = fma(bz, S.V01[src], uy);
             ux = fma(bz, S.V10[src], ux);
-            if (kappa) kv = fma(bz, S.K1[src], kv);
+            if constexpr (KAPPA) kv = fma(bz, S.K1[src], kv);
         }
         const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
         if (FORM) {
@@ -200,7 +229,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.gz[t] = uz * g;
             dsum = fma(de, W, dsum);
         } else {
-            const double g = (kappa ? -dt * kv : -dt) * W;
+            const double g = (KAPPA ? -dt * kv : -dt) * W;
             S.f[t] = uv * W;
             S.gx[t] = ux * g;
             S.gy[t] = uy * g;
@@ -404,12 +433,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 // ---------------------------------------------------------------------------
 template <int N, int Q>
 struct kg3_smem {
-    double c[N * N * N], m[N * N * N];
     double B[3][Q * N], dB[3][Q * N];
-    double Tu0[N * N * Q], Tu1[N * N * Q], Tm0[N * N * Q], Tm1[N * N * Q];  // [bz][by][qx]
-    double Vu00[N * Q * Q], Vu01[N * Q * Q], Vu10[N * Q * Q];              // [bz][qy][qx]
-    double Vm00[N * Q * Q], Vm01[N * Q * Q], Vm10[N * Q * Q];
-    double s[Q * Q * Q];
+    double Tu0[N * N * Q], Tu1[N * N * Q];                     // [bz][by][qx]
+    double Vu00[N * Q * Q], Vu01[N * Q * Q], Vu10[N * Q * Q];  // [bz][qy][qx]
+    // storage shared by buffers whose lives do not overlap: the coefficients
+    // (read by the x stage only) with mu's y-stage results, mu's x-stage
+    // results (read by the y stage only) with the point values s
+    union {
+        struct {
+            double c[N * N * N], m[N * N * N];
+        };
+        struct {
+            double Vm00[N * Q * Q], Vm01[N * Q * Q], Vm10[N * Q * Q];
+        };
+    };
+    union {
+        struct {
+            double Tm0[N * N * Q], Tm1[N * N * Q];
+        };
+        double s[Q * Q * Q];
+    };
     double J;
     int e[3], f0[3];
     int valid;
@@ -660,7 +703,8 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
     constexpr int N = P + 1, Q = P + 1;
     constexpr int E3 = FORM ? 1 : elems_per_warp<N * N * N>();
     constexpr int E2 = FORM ? 1 : elems_per_warp<N * N>();
-    constexpr int W3 = warps_for<elem_group<elem3_smem<N, Q>, E3>>();
+    constexpr int W3 = warps_for<elem_group<elem3_smem<N, Q, false>, E3>>();
+    constexpr int W3k = warps_for<elem_group<elem3_smem<N, Q, true>, E3>>();
     constexpr int W2 = warps_for<elem_group<elem2_smem<N, Q>, E2>>();
     if (ndim == 3) {
         for (int cx = 0; cx < N; ++cx)
@@ -670,9 +714,15 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                               mz = colour_count(d[2].elements, cz, N);
                     const long long work = static_cast<long long>(mx) * my * mz;
                     if (!work) continue;
-                    const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
-                    elem3_kernel<P, Q, FORM><<<blocks, 32 * W3, 0, s>>>(u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz,
-                                                                         mx, my, mz, dt, F);
+                    if (!FORM && kappa) {
+                        const long long blocks = ((work + E3 - 1) / E3 + W3k - 1) / W3k;
+                        elem3_kernel<P, Q, FORM, true><<<blocks, 32 * W3k, 0, s>>>(
+                            u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
+                    } else {
+                        const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
+                        elem3_kernel<P, Q, FORM, false><<<blocks, 32 * W3, 0, s>>>(
+                            u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
+                    }
                 }
     } else {
         for (int cx = 0; cx < N; ++cx)
