@@ -1550,13 +1550,13 @@ int adsg_adjoint_backward(adsg_adjoint* a, const double* dL_duT_dev, double* gra
                 return st;
         for (int k = k1 - 1; k >= k0; --k) {
             if (int st = enqueue_solve(c, lam, 1)) return st;  // lam <- mu_{k+1} = M^{-T} lambda_{k+1}
-            ADSG_CUDA_TRY(launch_kappa_grad(c->ndim, c->dims, a->seg + static_cast<size_t>(k - k0) * n, lam,
-                                            grad_kappa_dev, a->dt, s),
-                          "kappa gradient");
             ADSG_CUDA_TRY(cudaMemsetAsync(other, 0, bytes, s), "memset");
             {
+                // grad kappa += mu^T (dR/dkappa) u_k and other = R^T mu (R is symmetric)
                 stage_scope sc(c, ADSG_STAGE_RHS_ELEM);
-                ADSG_CUDA_TRY(launch_rhs_elem(c->ndim, c->dims, lam, a->kappa, other, a->dt, s), "R^T mu");
+                ADSG_CUDA_TRY(launch_adjoint_pair(c->ndim, c->dims, a->seg + static_cast<size_t>(k - k0) * n, lam,
+                                                  a->kappa, other, grad_kappa_dev, a->dt, s),
+                              "kappa gradient and R^T mu");
             }
             std::swap(lam, other);  // lam <- lambda_k = R mu_{k+1}
         }

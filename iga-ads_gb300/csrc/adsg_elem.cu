@@ -592,6 +592,233 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     });
 }
 
+// ---------------------------------------------------------------------------
+// One backward step of the adjoint in one pass over the elements: both
+// element operations that read mu = M^-T lambda,
+//     r_a += sum_q W (mu v_a - dt kappa grad mu . grad v_a)        (R(kappa) mu)
+//     g_a += sum_q -dt W (grad u . grad mu) v_a                     (dL/dkappa)
+// share mu's interpolation to the Gauss points (value and gradient), which
+// the two kernels above each did on their own.  Every accumulator takes the
+// operations of elem3_kernel (with kappa) or kgrad3_kernel in their order,
+// so both results are bitwise those of the separate kernels.  Buffers whose
+// lives do not overlap share storage: the coefficients with the y
+// back-projection's results, the x stage's results with the point values,
+// the y stage's results with the z back-projection's.
+// ---------------------------------------------------------------------------
+template <int N, int Q>
+struct adj3_smem {
+    double B[3][Q * N], dB[3][Q * N];
+    union {
+        struct {
+            double cm[N * N * N], cu[N * N * N], kc[N * N * N];
+        };
+        struct {
+            double R0[N * N * Q], Rx[N * N * Q], Ra[N * N * Q];  // [az][ay][qx]
+        };
+    };
+    union {
+        struct {
+            double Tm0[N * N * Q], Tm1[N * N * Q], Tu0[N * N * Q], Tu1[N * N * Q], K0[N * N * Q];  // [bz][by][qx]
+        };
+        struct {
+            double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q], sk[Q * Q * Q];
+        };
+    };
+    union {
+        struct {
+            double Vm00[N * Q * Q], Vm01[N * Q * Q], Vm10[N * Q * Q];  // [bz][qy][qx]
+            double Vu00[N * Q * Q], Vu01[N * Q * Q], Vu10[N * Q * Q], K1[N * Q * Q];
+        };
+        struct {
+            double S0[N * Q * Q], Sx[N * Q * Q], Sy[N * Q * Q], Sa[N * Q * Q];  // [az][qy][qx]
+        };
+    };
+    double J;
+    int e[3], f0[3];
+    int valid;
+};
+
+template <int P, int Q, int EPW = elems_per_warp<(P + 1) * (P + 1) * (P + 1)>(),
+          int kWarpsPerBlock = warps_for<elem_group<adj3_smem<P + 1, Q>, EPW>>()>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    adj3_kernel(const double* __restrict__ u, const double* __restrict__ mu, const double* __restrict__ kappa,
+                double* __restrict__ rmu, double* __restrict__ g, dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy,
+                int cz, int mx, int my, int mz, double dt) {
+    constexpr int N = P + 1;
+    using S_t = adj3_smem<N, Q>;
+    __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
+    const long long count = static_cast<long long>(mx) * my * mz;
+    if (wid * EPW >= count) return;
+    S_t* el = sm_all[warp].el;
+    if (lane < EPW) {
+        S_t& S = el[lane];
+        const long long id = wid * EPW + lane;
+        S.valid = id < count;
+        if (S.valid) {
+            const int iz = static_cast<int>(id % mz);
+            const int iy = static_cast<int>((id / mz) % my);
+            const int ix = static_cast<int>(id / (static_cast<long long>(mz) * my));
+            S.e[0] = cx + ix * N;
+            S.e[1] = cy + iy * N;
+            S.e[2] = cz + iz * N;
+            S.f0[0] = X.first[S.e[0]];
+            S.f0[1] = Y.first[S.e[1]];
+            S.f0[2] = Z.first[S.e[2]];
+            S.J = X.jac[S.e[0]] * Y.jac[S.e[1]] * Z.jac[S.e[2]];
+        }
+    }
+    __syncwarp();
+    const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
+    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
+        const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
+        const long long gi = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
+        S.cm[t] = mu[gi];
+        S.cu[t] = u[gi];
+        S.kc[t] = kappa[gi];
+    });
+    each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
+        const int q = t / N, a = t % N;
+        const double* bx = X.btab + ((static_cast<long long>(S.e[0]) * Q + q) * 2) * N;
+        const double* by = Y.btab + ((static_cast<long long>(S.e[1]) * Q + q) * 2) * N;
+        const double* bz = Z.btab + ((static_cast<long long>(S.e[2]) * Q + q) * 2) * N;
+        S.B[0][t] = bx[a];
+        S.dB[0][t] = bx[N + a];
+        S.B[1][t] = by[a];
+        S.dB[1][t] = by[N + a];
+        S.B[2][t] = bz[a];
+        S.dB[2][t] = bz[N + a];
+    });
+    __syncwarp();
+    // x: mu's value/derivative factors (elem3_kernel's T0/T1), kappa's (K0), u's (kgrad3_kernel's Tu0/Tu1)
+    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
+        const int qx = t % Q, byz = t / Q;
+        double a0 = 0.0, a1 = 0.0, k0 = 0.0, b0 = 0.0, b1 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const double bv = S.B[0][qx * N + b], dv = S.dB[0][qx * N + b];
+            const double cv = S.cm[byz * N + b], uv = S.cu[byz * N + b];
+            a0 = fma(bv, cv, a0);
+            a1 = fma(dv, cv, a1);
+            k0 = fma(bv, S.kc[byz * N + b], k0);
+            b0 = fma(bv, uv, b0);
+            b1 = fma(dv, uv, b1);
+        }
+        S.Tm0[t] = a0;
+        S.Tm1[t] = a1;
+        S.K0[t] = k0;
+        S.Tu0[t] = b0;
+        S.Tu1[t] = b1;
+    });
+    __syncwarp();
+    // y
+    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
+        const int qx = t % Q, qy = (t / Q) % Q, bz = t / (Q * Q);
+        double v00 = 0.0, v01 = 0.0, v10 = 0.0, k1 = 0.0, u00 = 0.0, u01 = 0.0, u10 = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const int src = (bz * N + b) * Q + qx;
+            const double by = S.B[1][qy * N + b], dby = S.dB[1][qy * N + b];
+            v00 = fma(by, S.Tm0[src], v00);
+            v01 = fma(dby, S.Tm0[src], v01);
+            v10 = fma(by, S.Tm1[src], v10);
+            k1 = fma(by, S.K0[src], k1);
+            u00 = fma(by, S.Tu0[src], u00);
+            u01 = fma(dby, S.Tu0[src], u01);
+            u10 = fma(by, S.Tu1[src], u10);
+        }
+        S.Vm00[t] = v00;
+        S.Vm01[t] = v01;
+        S.Vm10[t] = v10;
+        S.K1[t] = k1;
+        S.Vu00[t] = u00;
+        S.Vu01[t] = u01;
+        S.Vu10[t] = u10;
+    });
+    __syncwarp();
+    // z + both pointwise forms
+    each_item<Q * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
+        const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
+        double mv = 0.0, mx_ = 0.0, my_ = 0.0, mz_ = 0.0, kv = 0.0, ux = 0.0, uy = 0.0, uz = 0.0;
+#pragma unroll
+        for (int b = 0; b < N; ++b) {
+            const int src = (b * Q + qy) * Q + qx;
+            const double bz = S.B[2][qz * N + b], dbz = S.dB[2][qz * N + b];
+            mv = fma(bz, S.Vm00[src], mv);
+            mz_ = fma(dbz, S.Vm00[src], mz_);
+            my_ = fma(bz, S.Vm01[src], my_);
+            mx_ = fma(bz, S.Vm10[src], mx_);
+            kv = fma(bz, S.K1[src], kv);
+            uz = fma(dbz, S.Vu00[src], uz);
+            uy = fma(bz, S.Vu01[src], uy);
+            ux = fma(bz, S.Vu10[src], ux);
+        }
+        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
+        const double gk = (-dt * kv) * W;
+        S.f[t] = mv * W;
+        S.gx[t] = mx_ * gk;
+        S.gy[t] = my_ * gk;
+        S.gz[t] = mz_ * gk;
+        S.sk[t] = -dt * W * (ux * mx_ + uy * my_ + uz * mz_);
+    });
+    __syncwarp();
+    // z back: R(kappa) mu with value and derivative factors, the kappa gradient with value factors
+    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
+        const int qx = t % Q, qy = (t / Q) % Q, az = t / (Q * Q);
+        double s0 = 0.0, sx = 0.0, sy = 0.0, sa = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int src = (q * Q + qy) * Q + qx;
+            const double bz = S.B[2][q * N + az], dbz = S.dB[2][q * N + az];
+            s0 = fma(bz, S.f[src], s0);
+            s0 = fma(dbz, S.gz[src], s0);
+            sx = fma(bz, S.gx[src], sx);
+            sy = fma(bz, S.gy[src], sy);
+            sa = fma(bz, S.sk[src], sa);
+        }
+        S.S0[t] = s0;
+        S.Sx[t] = sx;
+        S.Sy[t] = sy;
+        S.Sa[t] = sa;
+    });
+    __syncwarp();
+    // y back
+    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
+        const int qx = t % Q, ay = (t / Q) % N, az = t / (Q * N);
+        double r0 = 0.0, rx = 0.0, ra = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int src = (az * Q + q) * Q + qx;
+            const double by = S.B[1][q * N + ay], dby = S.dB[1][q * N + ay];
+            r0 = fma(by, S.S0[src], r0);
+            r0 = fma(dby, S.Sy[src], r0);
+            rx = fma(by, S.Sx[src], rx);
+            ra = fma(by, S.Sa[src], ra);
+        }
+        S.R0[t] = r0;
+        S.Rx[t] = rx;
+        S.Ra[t] = ra;
+    });
+    __syncwarp();
+    // x back and both scatters (this colour owns every dof of the element)
+    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
+        const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
+        double o = 0.0, a = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int src = (az * N + ay) * Q + q;
+            o = fma(S.B[0][q * N + ax], S.R0[src], o);
+            o = fma(S.dB[0][q * N + ax], S.Rx[src], o);
+            a = fma(S.B[0][q * N + ax], S.Ra[src], a);
+        }
+        const long long gi = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
+        rmu[gi] += o;
+        g[gi] += a;
+    });
+}
+
 template <int N, int Q>
 struct kg2_smem {
     double c[N * N], m[N * N];
@@ -768,7 +995,44 @@ cudaError_t kgrad_p(int ndim, const dim_dev* d, const double* u, const double* m
     return cudaGetLastError();
 }
 
+template <int P>
+cudaError_t adj3_p(const dim_dev* d, const double* u, const double* mu, const double* kappa, double* rmu, double* g,
+                   double dt, cudaStream_t s) {
+    constexpr int N = P + 1, Q = P + 1;
+    constexpr int E3 = elems_per_warp<N * N * N>();
+    constexpr int W3 = warps_for<elem_group<adj3_smem<N, Q>, E3>>();
+    for (int cx = 0; cx < N; ++cx)
+        for (int cy = 0; cy < N; ++cy)
+            for (int cz = 0; cz < N; ++cz) {
+                const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N),
+                          mz = colour_count(d[2].elements, cz, N);
+                const long long work = static_cast<long long>(mx) * my * mz;
+                if (!work) continue;
+                adj3_kernel<P, Q><<<((work + E3 - 1) / E3 + W3 - 1) / W3, 32 * W3, 0, s>>>(
+                    u, mu, kappa, rmu, g, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt);
+            }
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, const double* mu,
+                                const double* kappa, double* rmu, double* g, double dt, cudaStream_t s) {
+    if (ndim != 3) {
+        cudaError_t e = launch_kappa_grad(ndim, dims, u, mu, g, dt, s);
+        return e != cudaSuccess ? e : launch_rhs_elem(ndim, dims, mu, kappa, rmu, dt, s);
+    }
+    const int p = dims[0].p;
+    for (int d = 0; d < ndim; ++d)
+        if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    switch (p) {
+        case 1: return adj3_p<1>(dims, u, mu, kappa, rmu, g, dt, s);
+        case 2: return adj3_p<2>(dims, u, mu, kappa, rmu, g, dt, s);
+        case 3: return adj3_p<3>(dims, u, mu, kappa, rmu, g, dt, s);
+        case 4: return adj3_p<4>(dims, u, mu, kappa, rmu, g, dt, s);
+        default: return cudaErrorNotSupported;
+    }
+}
 
 cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,
                               cudaStream_t s) {

@@ -173,6 +173,11 @@ cudaError_t launch_form_elem(int ndim, const dim_dev* dims, const double* u, con
 // g += mu^T (dR/dkappa) u  (gradient of the element operator w.r.t. kappa coefficients)
 cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,
                               cudaStream_t s);
+// both element operations of one adjoint backward step on mu:
+// rmu += R(kappa) mu and g += mu^T (dR/dkappa) u, in one pass in 3D (results
+// bitwise those of launch_rhs_elem and launch_kappa_grad)
+cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, const double* mu,
+                                const double* kappa, double* rmu, double* g, double dt, cudaStream_t s);
 
 // small vector kernels of the adjoint driver
 cudaError_t launch_axpby(double* y, double a, const double* x, double b, long long n, cudaStream_t s);  // y = a*x + b*y

@@ -41,8 +41,11 @@ def _grads(ctx, adj, dev):
 
 
 @pytest.mark.parametrize("p,elements,nsteps,dt", [((2, 2, 2), (5, 4, 6), 6, 1e-3), ((3, 3), (7, 6), 5, 1e-3),
-                                                   ((4, 4, 4), (3, 3, 3), 3, 1e-4)])
+                                                   ((4, 4, 4), (3, 3, 3), 3, 1e-4), ((1, 1, 1), (6, 5, 4), 5, 1e-3),
+                                                   ((3, 3, 3), (4, 3, 5), 4, 1e-4), ((2, 2, 2), (9, 8, 7), 3, 1e-4)])
 def test_adjoint_against_cpu_reference(p, elements, nsteps, dt, cuda):
+    """3D backward steps run R(kappa) mu and the kappa gradient as one fused
+    element pass (every degree 1-4 here); 2D runs the two kernels."""
     ctx, adj, h, dev = _setup(p, elements, nsteps, dt, seed=sum(elements))
     loss, gu, gk, _ = _grads(ctx, adj, dev)
     pr = oracle.Problem(list(p), list(elements))
