@@ -19,39 +19,43 @@ namespace adsg {
 namespace {
 
 
-// One element's buffers.  With the kappa field (KAPPA) every stage buffer
-// has its own storage; without it the coefficients and the x-contracted T0/T1
-// ([bz][by][qx]), dead from the pointwise stage until the y back-projection
-// rewrites T0/T1, share storage with the point values f/g*, which live exactly
-// then (the smaller tile keeps more warps per SM; with kappa the separate
-// layout measured faster).
-template <int N, int Q, bool KAPPA>
+// One element's buffers (the kappa buffers have one entry without KAPPA).
+// SHARED lays them out so that buffers whose lives do not overlap share
+// storage: the coefficients and the x-contracted T0/T1/K0 ([bz][by][qx]) are
+// dead from the pointwise stage until the y back-projection rewrites T0/T1,
+// which is exactly while the point values f/g* live.  The smaller tile keeps
+// more warps per SM; which layout is faster depends on the form (see
+// elem_p).
+template <int N, int Q, bool KAPPA, bool SHARED>
 struct elem3_smem;
 
-template <int N, int Q>
-struct elem3_smem<N, Q, true> {
+template <int N, int Q, bool KAPPA>
+struct elem3_smem<N, Q, KAPPA, false> {
+    static constexpr int NK = KAPPA ? 1 : 0;
     double c[N * N * N];
-    double kc[N * N * N];
+    double kc[NK * N * N * N + 1 - NK];
     double B[3][Q * N];  // B[d][q*N + a]
     double dB[3][Q * N];
     double T0[N * N * Q], T1[N * N * Q];
     double V00[N * Q * Q], V01[N * Q * Q], V10[N * Q * Q];  // [bz][qy][qx]
     double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
-    double K0[N * N * Q], K1[N * Q * Q];
+    double K0[NK * N * N * Q + 1 - NK], K1[NK * N * Q * Q + 1 - NK];
     double J;
     int e[3], f0[3];
     int valid;
 };
 
-template <int N, int Q>
-struct elem3_smem<N, Q, false> {
+template <int N, int Q, bool KAPPA>
+struct elem3_smem<N, Q, KAPPA, true> {
+    static constexpr int NK = KAPPA ? 1 : 0;
     double B[3][Q * N];
     double dB[3][Q * N];
     double V00[N * Q * Q], V01[N * Q * Q], V10[N * Q * Q];
+    double K1[NK * N * Q * Q + 1 - NK];
     union {
         struct {
-            double c[N * N * N];
-            double T0[N * N * Q], T1[N * N * Q];
+            double c[N * N * N], kc[NK * N * N * N + 1 - NK];
+            double T0[N * N * Q], T1[N * N * Q], K0[NK * N * N * Q + 1 - NK];
         };
         struct {
             double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
@@ -105,15 +109,13 @@ __device__ __forceinline__ void each_item(S* el, int lane, F&& f) {
 
 // FORM: the general pointwise form of point_form (kappa and dt unused; one
 // element per warp, whose D terms are summed across the warp).
-template <int P, int Q, bool FORM, bool KAPPA,
-          int EPW = (FORM ? 1 : elems_per_warp<(P + 1) * (P + 1) * (P + 1)>()),
-          int kWarpsPerBlock = warps_for<elem_group<elem3_smem<P + 1, Q, KAPPA>, EPW>>()>
+template <int P, int Q, bool FORM, bool KAPPA, bool SHARED, int EPW, int kWarpsPerBlock>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem3_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
                  dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt,
                  point_form F) {
     constexpr int N = P + 1;
-    using S_t = elem3_smem<N, Q, KAPPA>;
+    using S_t = elem3_smem<N, Q, KAPPA, SHARED>;
     __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -930,8 +932,16 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
     constexpr int N = P + 1, Q = P + 1;
     constexpr int E3 = FORM ? 1 : elems_per_warp<N * N * N>();
     constexpr int E2 = FORM ? 1 : elems_per_warp<N * N>();
-    constexpr int W3 = warps_for<elem_group<elem3_smem<N, Q, false>, E3>>();
-    constexpr int W3k = warps_for<elem_group<elem3_smem<N, Q, true>, E3>>();
+    // tile layouts and block shapes by measurement, one warp per block: shared
+    // storage without kappa (128^3 p=2: 6.68 ms per evaluation, against 6.95
+    // with three warps per block and 7.83 with separate buffers); with kappa
+    // separate buffers (200 adjoint forward steps at 96^3 p=2: 713 ms, against
+    // 742 with two warps per block, 785-796 with shared storage, 840 with 4
+    // elements per warp)
+    constexpr bool kShared = true, kSharedKappa = false;
+    constexpr int E3k = FORM ? 1 : elems_per_warp<N * N * N>();
+    constexpr int W3 = FORM ? warps_for<elem_group<elem3_smem<N, Q, false, kShared>, E3>>() : 1;
+    constexpr int W3k = 1;
     constexpr int W2 = warps_for<elem_group<elem2_smem<N, Q>, E2>>();
     if (ndim == 3) {
         for (int cx = 0; cx < N; ++cx)
@@ -942,12 +952,12 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                     const long long work = static_cast<long long>(mx) * my * mz;
                     if (!work) continue;
                     if (!FORM && kappa) {
-                        const long long blocks = ((work + E3 - 1) / E3 + W3k - 1) / W3k;
-                        elem3_kernel<P, Q, FORM, true><<<blocks, 32 * W3k, 0, s>>>(
+                        const long long blocks = ((work + E3k - 1) / E3k + W3k - 1) / W3k;
+                        elem3_kernel<P, Q, FORM, true, kSharedKappa, E3k, W3k><<<blocks, 32 * W3k, 0, s>>>(
                             u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
                     } else {
                         const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
-                        elem3_kernel<P, Q, FORM, false><<<blocks, 32 * W3, 0, s>>>(
+                        elem3_kernel<P, Q, FORM, false, kShared, E3, W3><<<blocks, 32 * W3, 0, s>>>(
                             u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
                     }
                 }
