@@ -588,11 +588,6 @@ int enqueue_solve(adsg_ctx* c, double* x, int trans) { return enqueue_solve_with
 std::mutex g_autotune_lock;
 std::map<std::string, int> g_autotune_cache;
 
-// Autotuner: time every applicable line-solve variant per direction on the
-// context's own state buffer (zeros) and keep the fastest.  ADSG_SOLVE_VARIANT
-// (0..5) forces one variant where applicable; ADSG_AUTOTUNE_LOG=1 prints each
-// candidate's time to stderr.  A candidate whose launch reports an error is
-// dropped (the error is cleared so that it cannot leak into the next one).
 // Device time of three line solves of direction D on the context's state
 // buffer, after one warm-up launch; a launch error is returned.
 cudaError_t time_line_solve(adsg_ctx* c, const dim_dev& D, const line_layout& L, cudaEvent_t a, cudaEvent_t b,
@@ -617,6 +612,11 @@ std::string autotune_key(const adsg_ctx* c, int d) {
     return key;
 }
 
+// Autotuner: time every applicable line-solve variant per direction on the
+// context's own state buffer (zeros) and keep the fastest.  ADSG_SOLVE_VARIANT
+// (0..6) forces one variant where applicable; ADSG_AUTOTUNE_LOG=1 prints each
+// candidate's time to stderr.  A candidate whose launch reports an error is
+// dropped (the error is cleared so that it cannot leak into the next one).
 int autotune_solves(adsg_ctx* c) {
     const char* force = std::getenv("ADSG_SOLVE_VARIANT");
     int forced = -1;
