@@ -1246,6 +1246,9 @@ __global__ void __launch_bounds__(128) rhs_x_solve_kernel(const double* __restri
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const long long base = g0 * n;
     const int count = nv * n;
+    // unrolled so that several outputs' loads are in flight at once: few warps
+    // per SM hold these tiles
+#pragma unroll 4
     for (int e = lane; e < count; e += 32) {
         const int line = e / n, r = e - line * n;
         const double* a0 = A0 + static_cast<long long>(r) * BW;
@@ -1323,6 +1326,27 @@ __device__ __forceinline__ void small_sweeps(double* R, const dim_dev& D, int nl
     }
 }
 
+// Issue L1 prefetches of `count` doubles from p (one per 128-byte line,
+// spread over the block's threads); nothing waits for them.
+__device__ __forceinline__ void prefetch_l1(const double* p, long long count) {
+    const char* c = reinterpret_cast<const char*>(p);
+    const long long bytes = count * static_cast<long long>(sizeof(double));
+    for (long long off = static_cast<long long>(threadIdx.x) * 128; off < bytes; off += static_cast<long long>(blockDim.x) * 128)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(c + off));
+}
+
+// every table the one-block step reads, so that its phases find them in L1
+// rather than each taking its own trip to memory
+template <int K>
+__device__ __forceinline__ void prefetch_step_tables(const dim_dev& D, bool x_pass) {
+    const long long band = static_cast<long long>(D.n) * (2 * K + 1);
+    prefetch_l1(D.mrow, band);
+    prefetch_l1(x_pass ? D.kdt : D.nrow, band);
+    prefetch_l1(D.tw_lmul, 2LL * D.tw_rows * K);
+    prefetch_l1(D.tw_ucol, 2LL * D.tw_rows * K);
+    prefetch_l1(D.tw_g, 4LL * K * K);
+}
+
 template <int K>
 __global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restrict__ u, double* __restrict__ out,
                                                            dim_dev X, dim_dev Y) {
@@ -1333,7 +1357,9 @@ __global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restr
     double* A = sm + N;
     double* C = sm + 2 * N;
     double* R = sm + 3 * N;
-    pdl_wait_and_release();
+    pdl_wait_and_release();  // the tables may come from the previous launch (the dt bands)
+    prefetch_step_tables<K>(X, true);
+    prefetch_step_tables<K>(Y, false);
     for (int g = threadIdx.x; g < N; g += blockDim.x) U[g] = u[g];
     __syncthreads();
     // y pass: A = My u, C = Ny u (pair sums on the symmetric rows, as launch_band_pass)
