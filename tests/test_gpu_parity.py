@@ -313,8 +313,9 @@ def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypa
     assert oracle.rel_l2(s, pr.heat_steps(u, 1e-5, 2)) <= step_tol(_conds(dims)) * 2
     chosen = ctx.solve_variants()
     assert all(0 <= v <= 6 for v in chosen)
-    if variant in (0, 3):  # always applicable for p <= 4
+    if variant in (0, 3):  # always applicable for p <= 4; a forced variant rules the step's view too
         assert chosen == [variant] * len(p)
+        assert ctx.step_solve_variants() == chosen
     if variant in (4, 5, 6):  # the twisted sweeps need n >= 4p + 2 along the direction
         for d, v in zip(dims, chosen):
             assert (v == variant) == (d.dofs() >= 4 * d.p + 2)
@@ -428,6 +429,28 @@ def test_host_entry_reading_pinned_input_is_exact(p, elements, variant, nsteps, 
     ctx.heat_steps(d, 1e-5, nsteps)
     ctx.synchronize()
     np.testing.assert_array_equal(h, d.cpu().numpy())
+
+
+@pytest.mark.parametrize("p,elements", [((2, 2, 2), (40, 33, 20)), ((4, 4, 4), (30, 20, 18)), ((3, 2), (70, 45))])
+def test_step_view_takes_its_own_variant(p, elements, cuda, monkeypatch):
+    """Unforced, the explicit step keeps ads_solve's variant per direction or,
+    where that is LAPACK-order (0-3), may take a two-ended one (4-6) on its
+    row-scaled tables; either way the step matches the oracle."""
+    import torch
+
+    monkeypatch.delenv("ADSG_SOLVE_VARIANT", raising=False)
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    plain, step = ctx.solve_variants(), ctx.step_solve_variants()
+    for a, b in zip(plain, step):
+        assert a == b or (a <= 3 and b in (4, 5, 6))
+    pr = oracle.Problem(list(p), list(elements))
+    u = np.random.default_rng(9).uniform(-1, 1, pr.size)
+    ud = torch.from_numpy(u).cuda()
+    nxt = torch.empty_like(ud)
+    ctx.heat_step(ud, nxt, 1e-5)
+    ctx.synchronize()
+    assert oracle.rel_l2(nxt.cpu().numpy(), pr.heat_steps(u, 1e-5, 1)) <= step_tol(_conds(dims))
 
 
 @pytest.mark.parametrize("p,elements", [((2, 2, 2), (40, 33, 20)), ((4, 4, 4), (30, 20, 18)), ((3, 3), (70, 45))])
