@@ -35,6 +35,12 @@ __device__ __forceinline__ void pdl_wait_and_release() {
     asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
+// Kernels that run as one wave of long-lived warps (the line solves) only
+// wait: their dependents launch when the last block exits, so the next
+// kernel's blocks do not sit on the SMs beside the sweeps, while the launch
+// still overlaps the grid's completion.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 static thread_local int t_pdl_mode = 0;  // set per context around its launches
 
 void set_launch_pdl(int on) { t_pdl_mode = on ? 1 : 0; }
@@ -624,7 +630,7 @@ __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ dat
     const int lane = threadIdx.x & 31;
     const long long line0 = static_cast<long long>(blockIdx.x) * 32;
     if (line0 >= L.nlines) return;
-    pdl_wait_and_release();
+    pdl_wait();
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
     double* s = smem + kPadLo * kPitch;
     for (int r = 0; r < kPadLo; ++r) smem[r * kPitch + lane] = 0.0;
@@ -800,7 +806,7 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
     const int lane = threadIdx.x & 31;
     const long long g = static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) * 32 + (threadIdx.x >> 5) * 32 + lane;
     if (g >= L.nlines) return;
-    pdl_wait_and_release();
+    pdl_wait();
     double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
     sweep_global<KL, KU, UNR>(x, L.elem_stride, D);
 }
@@ -976,7 +982,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restr
     const bool active = g < L.nlines;
     const unsigned mask = __ballot_sync(0xffffffffu, active);  // lanes g and g^16 share a line
     if (!active) return;
-    pdl_wait_and_release();
+    pdl_wait();
     double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
     const long long es = L.elem_stride;
     const long long off = static_cast<long long>(chain) * D.tw_rows;
@@ -1000,7 +1006,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
     const int n = D.n, pitch = twisted_pitch(n);
     const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
     if (g0 >= L.nlines) return;  // whole warp
-    pdl_wait_and_release();
+    pdl_wait();
     const int nv = static_cast<int>(min(16LL, L.nlines - g0));
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const double* src = data + g0 * n;
@@ -1106,7 +1112,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double*
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4, line = lane & 15;
     const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
     if (g0 >= L.nlines) return;  // whole warp
-    pdl_wait_and_release();
+    pdl_wait();
     chunk_lines W;
     W.data = data + g0 * D.n;
     W.n = D.n;
@@ -1241,7 +1247,7 @@ __global__ void __launch_bounds__(128) rhs_x_solve_kernel(const double* __restri
     const int n = D.n, pitch = twisted_pitch(n);
     const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
     if (g0 >= L.nlines) return;  // whole warp
-    pdl_wait_and_release();
+    pdl_wait();
     const int nv = static_cast<int>(min(16LL, L.nlines - g0));
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const long long base = g0 * n;
@@ -1485,7 +1491,7 @@ __global__ void __launch_bounds__(32 * WPB) line_solve_staged_kernel(double* __r
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long line0 = (static_cast<long long>(blockIdx.x) * WPB + warp) * 32;
     if (line0 >= L.nlines) return;
-    pdl_wait_and_release();
+    pdl_wait();
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
     double* base = smem + static_cast<size_t>(warp) * (D.n + kPadLo + kPadHi) * kPitch;
     double* s = base + kPadLo * kPitch;
