@@ -361,6 +361,16 @@ def run_ours(args, cfg):
         fl = ctx.stage_work()["rhs_elem"][0]
         elem = {"avg_us": 1e3 * t[0] / t[1], "tflops": fl / (t[0] / t[1] * 1e-3) / 1e12,
                 "gflop_per_launch": fl / 1e9, "note": "(p+1)^d colour launches per evaluation"}
+        # the same with a diffusion field kappa (the adjoint's forward operator)
+        kap = torch.from_numpy(inputs.kappa_field(dims, seed=12)).to(dev)
+        for _ in range(3):
+            ctx.heat_rhs_elem(bufs[0], bufs[1], dt, kappa=kap)
+        ctx.stage_times()
+        for _ in range(5):
+            ctx.heat_rhs_elem(bufs[0], bufs[1], dt, kappa=kap)
+        t = ctx.stage_times()["rhs_elem"]
+        elem["kappa_avg_us"] = 1e3 * t[0] / t[1]
+        del kap
     ctx.enable_stage_timers(False)
 
     # --- e2e: the reference-facing host entry point with pinned host buffers ---
