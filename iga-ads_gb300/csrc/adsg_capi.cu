@@ -420,6 +420,22 @@ struct adsg_ctx {
     cudaGraphExec_t graph = nullptr;
     double graph_dt = std::nan("");
     double* graph_u = nullptr;
+    // single-step graphs of adsg_heat_step, specialised on (prev, next, dt):
+    // a replayed graph runs the step's kernels back to back with shorter gaps
+    // than stream launches (130^3 p=2: 191.5 against 201.6 us per step)
+    struct step_graph {
+        const double* prev;
+        double* next;
+        double dt;
+        cudaGraphExec_t exec;
+    };
+    std::vector<step_graph> step_graphs;  // most recently used last
+    long long step_graph_hits = 0, step_graph_misses = 0;
+    int step_graphs_on = 1;  // chosen at creation: replay pays on all but launch-bound grids
+    void drop_step_graphs() {
+        for (auto& g : step_graphs) cudaGraphExecDestroy(g.exec);
+        step_graphs.clear();
+    }
     // stage timers
     bool timing = false;
     bool capturing = false;
@@ -459,6 +475,7 @@ struct adsg_ctx {
 
     ~adsg_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
+        drop_step_graphs();
         if (stream) cudaStreamSynchronize(stream);
         if (qpool) cudaFree(qpool);
         for (auto& t : pending) {
@@ -823,34 +840,96 @@ int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tab
     return 0;
 }
 
+// adsg_heat_step through a cached single-step graph.  Steps issued while the
+// stream is being captured (a batch recording its own graph), with stage
+// timers on, or by a caller that keeps changing buffers (more misses than the
+// small cache can serve) are enqueued directly.  The same kernels run either
+// way, so results do not depend on the path.
+constexpr size_t kStepGraphs = 4;
+
+int step_via_graph(adsg_ctx* c, const double* prev, double* next, double dt) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        cs = cudaStreamCaptureStatusActive;  // unknown: take the direct path
+    }
+    const bool thrashing = c->step_graph_misses > 2 * c->step_graph_hits + 16;
+    if (cs != cudaStreamCaptureStatusNone || c->timing || thrashing || !c->step_graphs_on)
+        return enqueue_step(c, prev, next, dt);
+    int st = ensure_dt_bands(c, dt);  // the graph reads the dt bands in place
+    if (st) return st;
+    auto& v = c->step_graphs;
+    for (size_t i = 0; i < v.size(); ++i)
+        if (v[i].prev == prev && v[i].next == next && v[i].dt == dt) {
+            const adsg_ctx::step_graph g = v[i];
+            v.erase(v.begin() + static_cast<long>(i));
+            v.push_back(g);
+            ++c->step_graph_hits;
+            ADSG_CUDA_TRY(cudaGraphLaunch(g.exec, c->stream), "step graph launch");
+            return 0;
+        }
+    ++c->step_graph_misses;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return enqueue_step(c, prev, next, dt);
+    }
+    c->capturing = true;
+    st = enqueue_step(c, prev, next, dt);
+    c->capturing = false;
+    const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = (st == 0 && ec == cudaSuccess) ? cudaGraphInstantiate(&exec, g, 0) : cudaErrorUnknown;
+    if (g) cudaGraphDestroy(g);
+    if (st) return st;
+    if (ei != cudaSuccess) {  // capture not possible here: the direct path
+        cudaGetLastError();
+        return enqueue_step(c, prev, next, dt);
+    }
+    if (v.size() >= kStepGraphs) {
+        cudaGraphExecDestroy(v.front().exec);
+        v.erase(v.begin());
+    }
+    v.push_back({prev, next, dt, exec});
+    ADSG_CUDA_TRY(cudaGraphLaunch(exec, c->stream), "step graph launch");
+    return 0;
+}
+
 // Step tuner: time a few explicit steps under each launch mode and keep the
-// fastest.  Two switches, neither of which changes any result bit:
-// programmatic dependent launch (ADSG_PDL=0/1 forces it) and, where the x
-// direction uses the staged two-ended solve, fusing the x band pass into that
-// solve (ADSG_FUSE_X=0/1 forces it).
+// fastest; then time the chosen mode replayed from single-step graphs against
+// direct launches.  None of the switches changes any result bit: programmatic
+// dependent launch (ADSG_PDL=0/1 forces it), fusing the x band pass into the
+// staged two-ended x solve where that is the x variant (ADSG_FUSE_X), the
+// one-block step of small 2D grids (ADSG_STEP_1BLOCK) and the graph replay
+// (ADSG_STEP_GRAPHS).
 int autotune_launch_mode(adsg_ctx* c) {
     auto forced = [](const char* name) -> int {
         const char* v = std::getenv(name);
         return v && (*v == '0' || *v == '1') ? *v - '0' : -1;
     };
-    const int f_pdl = forced("ADSG_PDL"), f_fuse = forced("ADSG_FUSE_X"), f_one = forced("ADSG_STEP_1BLOCK");
+    const int f_pdl = forced("ADSG_PDL"), f_fuse = forced("ADSG_FUSE_X"), f_one = forced("ADSG_STEP_1BLOCK"),
+              f_graph = forced("ADSG_STEP_GRAPHS");
     const bool can_fuse = fusion_ok(c), can_one = step_1block_ok(c);
-    std::vector<int> modes;  // bit 0: pdl, bit 1: fuse, bit 2: one-block step
-    for (int m = 0; m < 8; ++m) {
-        const int pdl = m & 1, fuse = (m >> 1) & 1, one = (m >> 2) & 1;
+    std::vector<int> modes;  // bit 0: pdl, bit 1: fuse, bit 2: one-block step, bit 3: graph replay
+    for (int m = 0; m < 16; ++m) {
+        const int pdl = m & 1, fuse = (m >> 1) & 1, one = (m >> 2) & 1, graph = (m >> 3) & 1;
         if (fuse && !can_fuse) continue;
         if (one && !can_one) continue;
         if (one && fuse) continue;  // the one-block step has no separate x pass
         if (f_pdl >= 0 && pdl != f_pdl) continue;
         if (f_fuse >= 0 && fuse != (f_fuse && can_fuse)) continue;
         if (f_one >= 0 && one != (f_one && can_one)) continue;
+        if (f_graph >= 0 && graph != f_graph) continue;
         modes.push_back(m);
     }
     if (modes.empty()) modes.push_back(0);
     auto apply = [&](int m) {
+        c->drop_step_graphs();  // a graph holds the launches of the mode it was captured under
+        c->step_graph_hits = c->step_graph_misses = 0;
         c->pdl = m & 1;
         c->fuse_x = (m >> 1) & 1;
         c->step_1block = (m >> 2) & 1;
+        c->step_graphs_on = (m >> 3) & 1;
     };
     if (modes.size() == 1) {
         apply(modes[0]);
@@ -870,11 +949,15 @@ int autotune_launch_mode(adsg_ctx* c) {
     const int reps = 4;
     for (size_t i = 0; i < modes.size() && e == cudaSuccess && rc == 0; ++i) {
         apply(modes[i]);
-        rc = enqueue_step(c, c->ping, tmp, 1e-6);  // warm-up (also builds the dt bands)
+        auto step = [&](const double* p, double* q) {
+            return c->step_graphs_on ? step_via_graph(c, p, q, 1e-6) : enqueue_step(c, p, q, 1e-6);
+        };
+        rc = step(c->ping, tmp);  // warm-up (also builds the dt bands and captures the graphs)
+        if (rc == 0) rc = step(tmp, c->ping);
         if (rc == 0) e = cudaEventRecord(a, c->stream);
         for (int r = 0; r < reps && rc == 0 && e == cudaSuccess; ++r) {
-            rc = enqueue_step(c, c->ping, tmp, 1e-6);
-            if (rc == 0) rc = enqueue_step(c, tmp, c->ping, 1e-6);
+            rc = step(c->ping, tmp);
+            if (rc == 0) rc = step(tmp, c->ping);
         }
         if (rc == 0 && e == cudaSuccess) e = cudaEventRecord(b, c->stream);
         if (rc == 0 && e == cudaSuccess) e = cudaEventSynchronize(b);
@@ -885,7 +968,7 @@ int autotune_launch_mode(adsg_ctx* c) {
             best_mode = modes[i];
         }
     }
-    apply(best_mode);
+    apply(best_mode);  // also drops the graphs, which name the tuner's buffers
     if (a) cudaEventDestroy(a);
     if (b) cudaEventDestroy(b);
     cudaFree(tmp);
@@ -1120,6 +1203,7 @@ int adsg_ctx_set_stream(adsg_ctx* ctx, void* cuda_stream) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;
     }
+    ctx->drop_step_graphs();
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
@@ -1212,7 +1296,7 @@ int adsg_heat_step(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, 
     const char* b = reinterpret_cast<const char*>(u_next_dev);
     const size_t bytes = sizeof(double) * static_cast<size_t>(ctx->size);
     if (a < b + bytes && b < a + bytes) return fail(-3, "u_prev and u_next overlap");
-    return enqueue_step(ctx, u_prev_dev, u_next_dev, dt);
+    return step_via_graph(ctx, u_prev_dev, u_next_dev, dt);
 }
 
 int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps) {
@@ -1298,6 +1382,8 @@ int adsg_ctx_launch_pdl(const adsg_ctx* ctx) { return ctx ? ctx->pdl : -1; }
 int adsg_ctx_fused_x(const adsg_ctx* ctx) { return ctx ? ctx->fuse_x : -1; }
 
 int adsg_ctx_step_1block(const adsg_ctx* ctx) { return ctx ? ctx->step_1block : -1; }
+
+int adsg_ctx_step_graphs(const adsg_ctx* ctx) { return ctx ? ctx->step_graphs_on : -1; }
 
 int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
     if (!ctx) return fail(-1, "ctx is NULL");

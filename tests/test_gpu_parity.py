@@ -431,6 +431,37 @@ def test_host_entry_reading_pinned_input_is_exact(p, elements, variant, nsteps, 
     np.testing.assert_array_equal(h, d.cpu().numpy())
 
 
+def test_step_graph_cache_matches_direct_launches(cuda, monkeypatch):
+    """adsg_heat_step replays a cached single-step graph per (prev, next, dt);
+    with stage timers on it launches directly.  Same kernels: bitwise equal,
+    also across dt changes (the dt bands are rebuilt in place before a replay)
+    and after the cache has evicted entries."""
+    import torch
+
+    monkeypatch.setenv("ADSG_STEP_GRAPHS", "1")
+    ctx = ads.Context([ads.Dimension(2, 20), ads.Dimension(3, 14), ads.Dimension(2, 9)])
+    assert ctx.step_graphs()
+    rng = np.random.default_rng(21)
+    bufs = [torch.from_numpy(rng.uniform(-1, 1, ctx.size)).cuda() for _ in range(6)]
+
+    def run(timers):
+        ctx.enable_stage_timers(timers)
+        outs = []
+        for k in range(12):
+            src, dst = bufs[k % 3], bufs[3 + (k * 7) % 3]
+            dt = (1e-4, 3e-5)[k % 2]
+            ctx.heat_step(src, dst, dt)
+            ctx.synchronize()
+            outs.append(dst.cpu().numpy().copy())
+        ctx.enable_stage_timers(False)
+        return outs
+
+    a, b, c = run(False), run(True), run(False)
+    for x, y, z in zip(a, b, c):
+        np.testing.assert_array_equal(x, y)
+        np.testing.assert_array_equal(x, z)
+
+
 @pytest.mark.parametrize("p,elements", [((2, 2, 2), (40, 33, 20)), ((4, 4, 4), (30, 20, 18)), ((3, 2), (70, 45))])
 def test_step_view_takes_its_own_variant(p, elements, cuda, monkeypatch):
     """Unforced, the explicit step keeps ads_solve's variant per direction or,
