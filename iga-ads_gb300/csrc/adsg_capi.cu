@@ -432,9 +432,17 @@ struct adsg_ctx {
     std::vector<step_graph> step_graphs;  // most recently used last
     long long step_graph_hits = 0, step_graph_misses = 0;
     int step_graphs_on = 1;  // chosen at creation: replay pays on all but launch-bound grids
+    // the host-buffer steps (upload pass, steps, download) of one pinned buffer
+    cudaGraphExec_t host_graph = nullptr;
+    const double* host_graph_u = nullptr;
+    double host_graph_dt = std::nan("");
+    int host_graph_steps = 0;
     void drop_step_graphs() {
         for (auto& g : step_graphs) cudaGraphExecDestroy(g.exec);
         step_graphs.clear();
+        if (host_graph) cudaGraphExecDestroy(host_graph);
+        host_graph = nullptr;
+        host_graph_u = nullptr;
     }
     // stage timers
     bool timing = false;
@@ -1023,6 +1031,55 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
         std::swap(cur, nxt);
     }
     ADSG_CUDA_TRY(cudaMemcpyAsync(u_out, cur, sizeof(double) * c->size, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    return 0;
+}
+
+// The same, replayed from a graph cached per (pinned buffer, dt, nsteps) when
+// the context replays its steps from graphs; pageable buffers (which a graph
+// cannot copy to), a stream under capture and stage timers take the direct
+// path.  Same operations either way.
+int heat_steps_host_graph(adsg_ctx* c, double* u, double dt, int nsteps) {
+    bool pinned = false;
+    {
+        cudaPointerAttributes attr{};
+        pinned = cudaPointerGetAttributes(&attr, u) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        cs = cudaStreamCaptureStatusActive;
+    }
+    if (!pinned || !c->step_graphs_on || c->timing || cs != cudaStreamCaptureStatusNone)
+        return heat_steps_host_direct(c, u, u, dt, nsteps);
+    int st = ensure_dt_bands(c, dt);
+    if (st) return st;
+    if (!(c->host_graph && c->host_graph_u == u && c->host_graph_dt == dt && c->host_graph_steps == nsteps)) {
+        if (c->host_graph) cudaGraphExecDestroy(c->host_graph);
+        c->host_graph = nullptr;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return heat_steps_host_direct(c, u, u, dt, nsteps);
+        }
+        c->capturing = true;
+        st = heat_steps_host_direct(c, u, u, dt, nsteps);
+        c->capturing = false;
+        const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = (st == 0 && ec == cudaSuccess) ? cudaGraphInstantiate(&exec, g, 0) : cudaErrorUnknown;
+        if (g) cudaGraphDestroy(g);
+        if (st) return st;
+        if (ei != cudaSuccess) {
+            cudaGetLastError();
+            return heat_steps_host_direct(c, u, u, dt, nsteps);
+        }
+        c->host_graph = exec;
+        c->host_graph_u = u;
+        c->host_graph_dt = dt;
+        c->host_graph_steps = nsteps;
+    }
+    ADSG_CUDA_TRY(cudaGraphLaunch(c->host_graph, c->stream), "host step graph launch");
     return 0;
 }
 
@@ -1993,7 +2050,7 @@ int adsg_heat_steps_host(adsg_ctx* ctx, double* u_host, double dt, int nsteps) {
     if (!ctx->host_io) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->host_io, ctx->size), "io alloc");
     const size_t bytes = sizeof(double) * ctx->size;
     if (ctx->ndim >= 2) {
-        int st = heat_steps_host_direct(ctx, u_host, u_host, dt, nsteps);
+        int st = heat_steps_host_graph(ctx, u_host, dt, nsteps);
         if (st) return st;
         ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
         return 0;

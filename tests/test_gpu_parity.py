@@ -407,28 +407,33 @@ def test_heat_step_against_oracle(p, elements, cuda):
 ])
 @pytest.mark.parametrize("nsteps", [1, 3])
 @pytest.mark.parametrize("pinned", [False, True])
-def test_host_entry_reading_pinned_input_is_exact(p, elements, variant, nsteps, pinned, cuda, monkeypatch):
+@pytest.mark.parametrize("graphs", ["0", "1"])
+def test_host_entry_reading_pinned_input_is_exact(p, elements, variant, nsteps, pinned, graphs, cuda, monkeypatch):
     """adsg_heat_steps_host: from pinned buffers the first band pass reads the
     input in host memory directly (column sweeps); from pageable ones the
-    input is copied first.  Either way the result equals the device-resident
-    steps bitwise."""
+    input is copied first; with graph replay on, pinned buffers replay a
+    cached graph of the whole call (the second call here).  Every way the
+    result equals the device-resident steps bitwise."""
     import torch
 
     if variant:
         monkeypatch.setenv("ADSG_SOLVE_VARIANT", variant)
+    monkeypatch.setenv("ADSG_STEP_GRAPHS", graphs)
     dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
     ctx = ads.Context(dims)
+    assert ctx.step_graphs() == (graphs == "1")
     u0 = np.random.default_rng(5).uniform(-1, 1, ctx.size)
     if pinned:
         ht = torch.from_numpy(u0.copy()).pin_memory()
         h = ht.numpy()
     else:
         h = u0.copy()
-    ctx.heat_steps_host(h, 1e-5, nsteps)
     d = torch.from_numpy(u0).cuda()
-    ctx.heat_steps(d, 1e-5, nsteps)
-    ctx.synchronize()
-    np.testing.assert_array_equal(h, d.cpu().numpy())
+    for _ in range(2):
+        ctx.heat_steps_host(h, 1e-5, nsteps)
+        ctx.heat_steps(d, 1e-5, nsteps)
+        ctx.synchronize()
+        np.testing.assert_array_equal(h, d.cpu().numpy())
 
 
 def test_step_graph_cache_matches_direct_launches(cuda, monkeypatch):
