@@ -610,6 +610,31 @@ int enqueue_solve_with(adsg_ctx* c, const dim_dev* D, double* x, int trans, int 
 
 int enqueue_solve(adsg_ctx* c, double* x, int trans) { return enqueue_solve_with(c, c->dims, x, trans); }
 
+// The explicit step's solves (the step's own view, sdims).  After the fused x
+// pass + x solve: y, then z.  Otherwise the outer directions first and x
+// last, so that the last sweep runs over contiguous lines and its tile can
+// be written anywhere: into `out` when given (e.g. the caller's pinned
+// buffer, mapped), in place otherwise.  The order differs from ads_solve's
+// x, y, z only by rounding (the directions' inverses commute).
+bool step_x_out_ok(const adsg_ctx* c) {
+    return line_solve_out_ok(c->sdims[0], make_line_layout(c->n, c->ndim, 0));
+}
+
+int enqueue_step_solves(adsg_ctx* c, double* x, bool fused, double* out = nullptr) {
+    if (fused) return enqueue_solve_with(c, c->sdims, x, 0, 1);
+    pdl_scope pdl(c->pdl);
+    for (int d = c->ndim - 1; d >= 0; --d) {
+        const line_layout L = make_line_layout(c->n, c->ndim, d);
+        stage_scope sc(c, ADSG_STAGE_SOLVE_X + d);
+        if (d == 0 && out && out != x) {
+            ADSG_CUDA_TRY(launch_line_solve_out(x, out, c->sdims[0], L, c->stream), "line solve (to output)");
+        } else {
+            ADSG_CUDA_TRY(launch_line_solve(x, c->sdims[d], L, 0, c->stream), "line solve");
+        }
+    }
+    return 0;
+}
+
 std::mutex g_autotune_lock;
 std::map<std::string, int> g_autotune_cache;
 
@@ -743,7 +768,7 @@ int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     const bool fused = c->fuse_x && fusion_ok(c);
     st = enqueue_rhs_with(c, c->sdims, prev, next, dt, fused);
     if (st) return st;
-    return enqueue_solve_with(c, c->sdims, next, 0, fused ? 1 : 0);
+    return enqueue_step_solves(c, next, fused);
 }
 
 // Builds the step's view of direction d once the solve variant of ads_solve
@@ -1022,12 +1047,23 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
     } else {
         ADSG_CUDA_TRY(cudaMemcpyAsync(cur, u_in, sizeof(double) * c->size, cudaMemcpyHostToDevice, c->stream), "H2D");
     }
+    // a pinned u_out (mapped) takes the last step's x sweep straight from its
+    // tiles: the download runs under that sweep instead of after it
+    double* out_dev = nullptr;
+    {
+        cudaPointerAttributes attr{};
+        if (cudaPointerGetAttributes(&attr, u_out) == cudaSuccess && attr.type == cudaMemoryTypeHost)
+            out_dev = static_cast<double*>(attr.devicePointer);
+        cudaGetLastError();
+    }
     for (int step = 0; step < nsteps; ++step) {
         const bool fused = c->fuse_x && fusion_ok(c);
         st = enqueue_rhs_with(c, D, cur, nxt, dt, fused, /*outer_done=*/step == 0 && direct_in);
         if (st) return st;
-        st = enqueue_solve_with(c, D, nxt, 0, fused ? 1 : 0);
+        const bool to_host = step + 1 == nsteps && !fused && out_dev && step_x_out_ok(c) && c->size >= (1LL << 18);
+        st = enqueue_step_solves(c, nxt, fused, to_host ? out_dev : nullptr);
         if (st) return st;
+        if (to_host) return 0;
         std::swap(cur, nxt);
     }
     ADSG_CUDA_TRY(cudaMemcpyAsync(u_out, cur, sizeof(double) * c->size, cudaMemcpyDeviceToHost, c->stream), "D2H");

@@ -999,7 +999,10 @@ __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restr
 __host__ __device__ inline int twisted_pitch(int n) { return n | 1; }
 
 template <int K, int UNR, bool UNIT>
-__global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* __restrict__ data, dim_dev D,
+// out: where the solved tile is written (data itself, or another buffer of
+// the same layout such as mapped pinned host memory: the write-back is
+// coalesced, 256 contiguous bytes per warp instruction)
+__global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(const double* data, double* out, dim_dev D,
                                                                         line_layout L) {
     extern __shared__ double smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4;
@@ -1028,7 +1031,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(double* 
                                     D.tw_ucol + off * K, D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
     }
     __syncwarp();
-    double* dst = data + g0 * n;
+    double* dst = out + g0 * n;
     for (int e = lane; e < count; e += 32) {
         const int ln = e / n;
         dst[e] = tile[ln * pitch + (e - ln * n)];
@@ -1308,8 +1311,8 @@ static cudaError_t rhs_x_solve_t(const double* in0, const double* in1, double* o
 }
 
 // ---------------------------------------------------------------------------
-// One-block step for small 2D grids: adsg_heat_step's y pass, x pass, x sweep
-// and y sweep in one launch, separated by block barriers, on a grid whose
+// One-block step for small 2D grids: adsg_heat_step's y pass, x pass, y sweep
+// and x sweep in one launch, separated by block barriers, on a grid whose
 // four working tensors fit in shared memory.  Launch latency, not work,
 // bounds such grids (four dependent launches of a few microseconds each).
 // The passes are band_out and the sweeps twisted_chain, so the operations and
@@ -1381,9 +1384,10 @@ __global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restr
     for (int g = threadIdx.x; g < N; g += blockDim.x)
         band_out<K, true, false, false, false>(g, A, C, R, nullptr, X.kdt, X.mrow, nullptr, nx, 1, 0, 0);
     __syncthreads();
-    small_sweeps<K, UNR>(R, X, ny, nx, 1);  // x-lines: rows of R
-    __syncthreads();
+    // the step's solve order: the outer direction first, x last
     small_sweeps<K, UNR>(R, Y, nx, 1, nx);  // y-lines: columns of R
+    __syncthreads();
+    small_sweeps<K, UNR>(R, X, ny, nx, 1);  // x-lines: rows of R
     __syncthreads();
     for (int g = threadIdx.x; g < N; g += blockDim.x) out[g] = R[g];
 }
@@ -1444,8 +1448,10 @@ cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out
 }
 
 template <int K, bool UNIT>
-static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, int variant, cudaStream_t s) {
+static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& L, int variant, cudaStream_t s,
+                             double* out = nullptr) {
     constexpr int UNR = K > 2 ? 4 : 8;
+    if (!out) out = data;
     // one warp (16 lines) per block: the FP64 pipe is per SM, and single-warp
     // blocks spread the warps over the SMs most evenly
     if (variant == SOLVE_TWISTED_CHUNKED && L.contiguous) {
@@ -1466,8 +1472,9 @@ static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& 
         }
         const long long per = 16LL * wpb;
         return launch_pdl(line_solve_twisted_staged_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)),
-                          dim3(32 * wpb), smem, s, data, d, L);
+                          dim3(32 * wpb), smem, s, static_cast<const double*>(data), out, d, L);
     }
+    if (out != data) return cudaErrorNotSupported;  // only the tiled sweep writes elsewhere
     return launch_pdl(line_solve_twisted_kernel<K, UNR, UNIT>, dim3(static_cast<unsigned>((L.nlines + 15) / 16)),
                       dim3(32), 0, s, data, d, L);
 }
@@ -1548,6 +1555,31 @@ bool line_solve_variant_ok(int variant, const dim_dev& d) {
     if (variant == SOLVE_STAGED_2) return line_solve_smem_per_warp(d.n) * 2 <= 227 * 1024;
     if (variant == SOLVE_STAGED_4) return line_solve_smem_per_warp(d.n) * 4 <= 227 * 1024;
     return true;
+}
+
+bool line_solve_out_ok(const dim_dev& d, const line_layout& L) {
+    return L.contiguous && d.solve_variant == SOLVE_TWISTED_STAGED && line_solve_variant_ok(SOLVE_TWISTED_STAGED, d);
+}
+
+cudaError_t launch_line_solve_out(const double* data, double* out, const dim_dev& d, const line_layout& L,
+                                  cudaStream_t s) {
+    if (!line_solve_out_ok(d, L)) return cudaErrorNotSupported;
+    if (L.nlines <= 0) return cudaSuccess;
+    double* in = const_cast<double*>(data);  // read only: the tiled sweep writes out
+    if (d.tw_unit) {
+        switch (d.tw_k) {
+            case 1: return twisted_t<1, true>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+            case 2: return twisted_t<2, true>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+            case 3: return twisted_t<3, true>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+            default: return twisted_t<4, true>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+        }
+    }
+    switch (d.tw_k) {
+        case 1: return twisted_t<1, false>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+        case 2: return twisted_t<2, false>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+        case 3: return twisted_t<3, false>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+        default: return twisted_t<4, false>(in, d, L, SOLVE_TWISTED_STAGED, s, out);
+    }
 }
 
 cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans, cudaStream_t s) {

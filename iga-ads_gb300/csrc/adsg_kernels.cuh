@@ -141,6 +141,12 @@ cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* k
 // trans = 0: dgbtrs 'N', trans = 1: dgbtrs 'T', along every line of layout L.
 cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout& L, int trans,
                               cudaStream_t s);
+// The same solve of contiguous lines with the result written to out (e.g.
+// mapped pinned host memory) instead of in place; only the tiled two-ended
+// sweep (variant 5) does this (line_solve_out_ok).
+bool line_solve_out_ok(const dim_dev& d, const line_layout& L);
+cudaError_t launch_line_solve_out(const double* data, double* out, const dim_dev& d, const line_layout& L,
+                                  cudaStream_t s);
 size_t line_solve_smem_per_warp(int n);
 bool line_solve_variant_ok(int variant, const dim_dev& d);
 // x band pass (out = A0 (.) in0 [+ A1 (.) in1]) fused with the two-ended x
