@@ -127,8 +127,10 @@ int adsg_ads_solve_t(adsg_ctx* ctx, double* rhs_dev);
  * ads_solve): u_next = M^-1 R u_prev.  u_prev_dev and u_next_dev must not
  * overlap.  Because the right-hand side stays internal, directions solved
  * with the two-ended sweep receive it row-scaled by their factors' diagonal
- * (folded into the band rows) and skip the backward sweep's multiply; the
- * result equals adsg_heat_rhs + adsg_ads_solve up to rounding. */
+ * (folded into the band rows) and skip the backward sweep's multiply, and
+ * the directions are solved outermost first and x last (x first when the x
+ * band pass is fused with the x solve); the result equals adsg_heat_rhs +
+ * adsg_ads_solve up to rounding. */
 int adsg_heat_step(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, double dt);
 
 /* nsteps of simulation_base::run's loop with heat_3d's step
