@@ -865,7 +865,10 @@ int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tab
             std::lock_guard<std::mutex> lk(g_autotune_lock);
             g_autotune_cache[key] = pick;
         }
-        if (!solve_variant_twisted(pick)) return 0;  // the plain view stays
+        if (!solve_variant_twisted(pick)) {  // the plain view stays, with the plain dt bands
+            c->snrow[d] = c->skdt[d] = nullptr;
+            return 0;
+        }
         S.solve_variant = pick;
     }
     c->sdims[d] = S;
