@@ -189,7 +189,8 @@ int adsg_ctx_step_solve_variants(const adsg_ctx* ctx, int* variants);
 int adsg_ctx_launch_pdl(const adsg_ctx* ctx);
 /* 1 when adsg_heat_step fuses the x band pass into the x solve (possible when
  * x uses solve variant 5; chosen at creation by timing, ADSG_FUSE_X=0/1
- * forces it), 0 when not, -1 for a NULL context.  Results do not depend on it. */
+ * forces it), 0 when not, -1 for a NULL context.  The fused step solves x
+ * first, the unfused one x last: results agree to rounding. */
 int adsg_ctx_fused_x(const adsg_ctx* ctx);
 /* 1 when adsg_heat_step runs a whole 2D step in one block (grids whose four
  * working tensors fit in 200 KB of shared memory, both directions on the
