@@ -426,183 +426,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 }
 
 // ---------------------------------------------------------------------------
-// Gradient of a quadratic functional with respect to the diffusion field:
-//     g_c += -dt sum_e sum_q W B_c(x_q) grad u(x_q) . grad mu(x_q)
-// i.e. mu^T (dR/dkappa_c) u for the operator R(kappa) applied by the element
-// kernel above.  Same warp-per-element sum factorisation and colouring:
-// gradients of u and mu are interpolated direction by direction, the
-// pointwise product is formed and projected onto the value factors.
-// ---------------------------------------------------------------------------
-template <int N, int Q>
-struct kg3_smem {
-    double B[3][Q * N], dB[3][Q * N];
-    double Tu0[N * N * Q], Tu1[N * N * Q];                     // [bz][by][qx]
-    double Vu00[N * Q * Q], Vu01[N * Q * Q], Vu10[N * Q * Q];  // [bz][qy][qx]
-    // storage shared by buffers whose lives do not overlap: the coefficients
-    // (read by the x stage only) with mu's y-stage results, mu's x-stage
-    // results (read by the y stage only) with the point values s
-    union {
-        struct {
-            double c[N * N * N], m[N * N * N];
-        };
-        struct {
-            double Vm00[N * Q * Q], Vm01[N * Q * Q], Vm10[N * Q * Q];
-        };
-    };
-    union {
-        struct {
-            double Tm0[N * N * Q], Tm1[N * N * Q];
-        };
-        double s[Q * Q * Q];
-    };
-    double J;
-    int e[3], f0[3];
-    int valid;
-};
-
-template <int P, int Q, int EPW = elems_per_warp<(P + 1) * (P + 1) * (P + 1)>(),
-          int kWarpsPerBlock = warps_for<elem_group<kg3_smem<P + 1, Q>, EPW>>()>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-    kgrad3_kernel(const double* __restrict__ u, const double* __restrict__ mu, double* __restrict__ g, dim_dev X,
-                  dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt) {
-    constexpr int N = P + 1;
-    using S_t = kg3_smem<N, Q>;
-    __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const long long wid = static_cast<long long>(blockIdx.x) * kWarpsPerBlock + warp;
-    const long long count = static_cast<long long>(mx) * my * mz;
-    if (wid * EPW >= count) return;
-    S_t* el = sm_all[warp].el;
-    if (lane < EPW) {
-        S_t& S = el[lane];
-        const long long id = wid * EPW + lane;
-        S.valid = id < count;
-        if (S.valid) {
-            const int iz = static_cast<int>(id % mz);
-            const int iy = static_cast<int>((id / mz) % my);
-            const int ix = static_cast<int>(id / (static_cast<long long>(mz) * my));
-            S.e[0] = cx + ix * N;
-            S.e[1] = cy + iy * N;
-            S.e[2] = cz + iz * N;
-            S.f0[0] = X.first[S.e[0]];
-            S.f0[1] = Y.first[S.e[1]];
-            S.f0[2] = Z.first[S.e[2]];
-            S.J = X.jac[S.e[0]] * Y.jac[S.e[1]] * Z.jac[S.e[2]];
-        }
-    }
-    __syncwarp();
-    const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
-    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
-        const long long gi = (S.f0[0] + t % N) + nx * (S.f0[1] + (t / N) % N) + nxy * (S.f0[2] + t / (N * N));
-        S.c[t] = u[gi];
-        S.m[t] = mu[gi];
-    });
-    each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
-        const int q = t / N, a = t % N;
-        const double* bx = X.btab + ((static_cast<long long>(S.e[0]) * Q + q) * 2) * N;
-        const double* by = Y.btab + ((static_cast<long long>(S.e[1]) * Q + q) * 2) * N;
-        const double* bz = Z.btab + ((static_cast<long long>(S.e[2]) * Q + q) * 2) * N;
-        S.B[0][t] = bx[a];
-        S.dB[0][t] = bx[N + a];
-        S.B[1][t] = by[a];
-        S.dB[1][t] = by[N + a];
-        S.B[2][t] = bz[a];
-        S.dB[2][t] = bz[N + a];
-    });
-    __syncwarp();
-    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
-        const int qx = t % Q, byz = t / Q;
-        double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
-#pragma unroll
-        for (int b = 0; b < N; ++b) {
-            const double bv = S.B[0][qx * N + b], dv = S.dB[0][qx * N + b];
-            a0 = fma(bv, S.c[byz * N + b], a0);
-            a1 = fma(dv, S.c[byz * N + b], a1);
-            b0 = fma(bv, S.m[byz * N + b], b0);
-            b1 = fma(dv, S.m[byz * N + b], b1);
-        }
-        S.Tu0[t] = a0;
-        S.Tu1[t] = a1;
-        S.Tm0[t] = b0;
-        S.Tm1[t] = b1;
-    });
-    __syncwarp();
-    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
-        const int qx = t % Q, qy = (t / Q) % Q, bz = t / (Q * Q);
-        double u00 = 0.0, u01 = 0.0, u10 = 0.0, m00 = 0.0, m01 = 0.0, m10 = 0.0;
-#pragma unroll
-        for (int b = 0; b < N; ++b) {
-            const int src = (bz * N + b) * Q + qx;
-            const double by = S.B[1][qy * N + b], dby = S.dB[1][qy * N + b];
-            u00 = fma(by, S.Tu0[src], u00);
-            u01 = fma(dby, S.Tu0[src], u01);
-            u10 = fma(by, S.Tu1[src], u10);
-            m00 = fma(by, S.Tm0[src], m00);
-            m01 = fma(dby, S.Tm0[src], m01);
-            m10 = fma(by, S.Tm1[src], m10);
-        }
-        S.Vu00[t] = u00;
-        S.Vu01[t] = u01;
-        S.Vu10[t] = u10;
-        S.Vm00[t] = m00;
-        S.Vm01[t] = m01;
-        S.Vm10[t] = m10;
-    });
-    __syncwarp();
-    each_item<Q * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
-        const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
-        double ux = 0.0, uy = 0.0, uz = 0.0, mx_ = 0.0, my_ = 0.0, mz_ = 0.0;
-#pragma unroll
-        for (int b = 0; b < N; ++b) {
-            const int src = (b * Q + qy) * Q + qx;
-            const double bz = S.B[2][qz * N + b], dbz = S.dB[2][qz * N + b];
-            uz = fma(dbz, S.Vu00[src], uz);
-            uy = fma(bz, S.Vu01[src], uy);
-            ux = fma(bz, S.Vu10[src], ux);
-            mz_ = fma(dbz, S.Vm00[src], mz_);
-            my_ = fma(bz, S.Vm01[src], my_);
-            mx_ = fma(bz, S.Vm10[src], mx_);
-        }
-        const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
-        S.s[t] = -dt * W * (ux * mx_ + uy * my_ + uz * mz_);
-    });
-    __syncwarp();
-    // project s onto the value factors: z, then y, then x
-    each_item<N * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
-        const int qx = t % Q, qy = (t / Q) % Q, az = t / (Q * Q);
-        double a = 0.0;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) a = fma(S.B[2][q * N + az], S.s[(q * Q + qy) * Q + qx], a);
-        S.Vu00[t] = a;
-    });
-    __syncwarp();
-    each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
-        const int qx = t % Q, ay = (t / Q) % N, az = t / (Q * N);
-        double a = 0.0;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) a = fma(S.B[1][q * N + ay], S.Vu00[(az * Q + q) * Q + qx], a);
-        S.Tu0[t] = a;
-    });
-    __syncwarp();
-    each_item<N * N * N, EPW>(el, lane, [&](S_t& S, int t) {
-        const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
-        double a = 0.0;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) a = fma(S.B[0][q * N + ax], S.Tu0[(az * N + ay) * Q + q], a);
-        g[(S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az)] += a;
-    });
-}
-
-// ---------------------------------------------------------------------------
 // One backward step of the adjoint in one pass over the elements: both
 // element operations that read mu = M^-T lambda,
 //     r_a += sum_q W (mu v_a - dt kappa grad mu . grad v_a)        (R(kappa) mu)
 //     g_a += sum_q -dt W (grad u . grad mu) v_a                     (dL/dkappa)
 // share mu's interpolation to the Gauss points (value and gradient), which
-// the two kernels above each did on their own.  Every accumulator takes the
-// operations of elem3_kernel (with kappa) or kgrad3_kernel in their order,
-// so both results are bitwise those of the separate kernels.  Buffers whose
+// a separate gradient pass would repeat.  The R(kappa) mu accumulators take
+// elem3_kernel's operations (with kappa) in its order, so that part is
+// bitwise elem3_kernel's; the gradient interpolates grad u and grad mu
+// direction by direction and projects the pointwise product onto the value
+// factors (kgrad2_kernel's scheme in 3D).  Buffers whose
 // lives do not overlap share storage: the coefficients with the y
 // back-projection's results, the x stage's results with the point values,
 // the y stage's results with the z back-projection's.
@@ -694,7 +527,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.dB[2][t] = bz[N + a];
     });
     __syncwarp();
-    // x: mu's value/derivative factors (elem3_kernel's T0/T1), kappa's (K0), u's (kgrad3_kernel's Tu0/Tu1)
+    // x: mu's value/derivative factors (elem3_kernel's T0/T1), kappa's (K0), u's (Tu0/Tu1)
     each_item<N * N * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, byz = t / Q;
         double a0 = 0.0, a1 = 0.0, k0 = 0.0, b0 = 0.0, b1 = 0.0;
@@ -821,6 +654,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     });
 }
 
+// ---------------------------------------------------------------------------
+// Gradient of a quadratic functional with respect to the diffusion field, 2D:
+//     g_c += -dt sum_e sum_q W B_c(x_q) grad u(x_q) . grad mu(x_q)
+// i.e. mu^T (dR/dkappa_c) u for the operator R(kappa) applied by the element
+// kernels above.  Same sum factorisation and colouring: gradients of u and
+// mu are interpolated direction by direction, the pointwise product is formed
+// and projected onto the value factors.  (3D runs this inside adj3_kernel.)
+// ---------------------------------------------------------------------------
 template <int N, int Q>
 struct kg2_smem {
     double c[N * N], m[N * N];
@@ -975,33 +816,18 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
 }
 
 template <int P>
-cudaError_t kgrad_p(int ndim, const dim_dev* d, const double* u, const double* mu, double* g, double dt,
-                    cudaStream_t s) {
+cudaError_t kgrad2_p(const dim_dev* d, const double* u, const double* mu, double* g, double dt, cudaStream_t s) {
     constexpr int N = P + 1, Q = P + 1;
-    constexpr int E3 = elems_per_warp<N * N * N>();
     constexpr int E2 = elems_per_warp<N * N>();
-    constexpr int W3 = warps_for<elem_group<kg3_smem<N, Q>, E3>>();
     constexpr int W2 = warps_for<elem_group<kg2_smem<N, Q>, E2>>();
-    if (ndim == 3) {
-        for (int cx = 0; cx < N; ++cx)
-            for (int cy = 0; cy < N; ++cy)
-                for (int cz = 0; cz < N; ++cz) {
-                    const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N),
-                              mz = colour_count(d[2].elements, cz, N);
-                    const long long work = static_cast<long long>(mx) * my * mz;
-                    if (!work) continue;
-                    kgrad3_kernel<P, Q><<<((work + E3 - 1) / E3 + W3 - 1) / W3, 32 * W3, 0, s>>>(u, mu, g, d[0], d[1], d[2], cx, cy,
-                                                                              cz, mx, my, mz, dt);
-                }
-    } else {
-        for (int cx = 0; cx < N; ++cx)
-            for (int cy = 0; cy < N; ++cy) {
-                const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N);
-                const long long work = static_cast<long long>(mx) * my;
-                if (!work) continue;
-                kgrad2_kernel<P, Q><<<((work + E2 - 1) / E2 + W2 - 1) / W2, 32 * W2, 0, s>>>(u, mu, g, d[0], d[1], cx, cy, mx, my, dt);
-            }
-    }
+    for (int cx = 0; cx < N; ++cx)
+        for (int cy = 0; cy < N; ++cy) {
+            const int mx = colour_count(d[0].elements, cx, N), my = colour_count(d[1].elements, cy, N);
+            const long long work = static_cast<long long>(mx) * my;
+            if (!work) continue;
+            kgrad2_kernel<P, Q><<<((work + E2 - 1) / E2 + W2 - 1) / W2, 32 * W2, 0, s>>>(u, mu, g, d[0], d[1], cx, cy, mx,
+                                                                                       my, dt);
+        }
     return cudaGetLastError();
 }
 
@@ -1046,15 +872,15 @@ cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, 
 
 cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,
                               cudaStream_t s) {
-    if (ndim < 2) return cudaErrorNotSupported;
+    if (ndim != 2) return cudaErrorNotSupported;  // 3D: launch_adjoint_pair
     const int p = dims[0].p;
     for (int d = 0; d < ndim; ++d)
         if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
     switch (p) {
-        case 1: return kgrad_p<1>(ndim, dims, u, mu, g, dt, s);
-        case 2: return kgrad_p<2>(ndim, dims, u, mu, g, dt, s);
-        case 3: return kgrad_p<3>(ndim, dims, u, mu, g, dt, s);
-        case 4: return kgrad_p<4>(ndim, dims, u, mu, g, dt, s);
+        case 1: return kgrad2_p<1>(dims, u, mu, g, dt, s);
+        case 2: return kgrad2_p<2>(dims, u, mu, g, dt, s);
+        case 3: return kgrad2_p<3>(dims, u, mu, g, dt, s);
+        case 4: return kgrad2_p<4>(dims, u, mu, g, dt, s);
         default: return cudaErrorNotSupported;
     }
 }

@@ -176,12 +176,13 @@ cudaError_t launch_form_elem(int ndim, const dim_dev* dims, const double* u, con
                              cudaStream_t s);
 
 // element-wise sum-factorised quadrature (optional kappa field) -----------
-// g += mu^T (dR/dkappa) u  (gradient of the element operator w.r.t. kappa coefficients)
+// g += mu^T (dR/dkappa) u  (gradient of the element operator w.r.t. kappa
+// coefficients), 2D; in 3D the gradient runs inside launch_adjoint_pair
 cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, const double* mu, double* g, double dt,
                               cudaStream_t s);
 // both element operations of one adjoint backward step on mu:
-// rmu += R(kappa) mu and g += mu^T (dR/dkappa) u, in one pass in 3D (results
-// bitwise those of launch_rhs_elem and launch_kappa_grad)
+// rmu += R(kappa) mu and g += mu^T (dR/dkappa) u, in one pass in 3D (the
+// R(kappa) mu part bitwise launch_rhs_elem's), in two kernels in 2D
 cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, const double* mu,
                                 const double* kappa, double* rmu, double* g, double dt, cudaStream_t s);
 
