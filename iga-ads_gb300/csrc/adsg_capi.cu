@@ -351,169 +351,7 @@ int make_twisted_tables(int n, int kl, int ku, int ldab, const double* ab, const
 
 using namespace adsg;
 
-#define ADSG_CUDA_TRY(expr, where)                          \
-    do {                                                    \
-        cudaError_t e_ = (expr);                            \
-        if (e_ != cudaSuccess) return fail_cuda(e_, where); \
-    } while (0)
-
-namespace {
-
-// Device allocations of one context, freed together.
-struct dev_arena {
-    std::vector<void*> blocks;
-    ~dev_arena() {
-        for (void* p : blocks) cudaFree(p);
-    }
-    template <typename T>
-    cudaError_t alloc(T** out, size_t count) {
-        void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-        if (e != cudaSuccess) return e;
-        blocks.push_back(p);
-        *out = static_cast<T*>(p);
-        return cudaSuccess;
-    }
-    template <typename T>
-    cudaError_t upload(T** out, const T* src, size_t count, cudaStream_t s) {
-        cudaError_t e = alloc(out, count);
-        if (e != cudaSuccess) return e;
-        return cudaMemcpyAsync(*out, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
-    }
-};
-
-}  // namespace
-
-namespace adsg {
-void detach_adjoints(adsg_ctx* c);
-}
-
-struct adsg_ctx {
-    int ndim = 0;
-    int n[3] = {1, 1, 1};
-    long long size = 0;
-    dim_dev dims[3];
-    double* nrow[3] = {nullptr, nullptr, nullptr};
-    double* kdt[3] = {nullptr, nullptr, nullptr};
-    // The explicit step's own view of each direction.  Where the direction is
-    // solved with a two-ended sweep, its band rows are pre-multiplied by
-    // 1 / U(r, r) of that sweep's factors and the solve tables are the unit-
-    // diagonal ones: the RHS passes deliver the row-scaled right-hand side at
-    // no extra cost and the backward sweeps drop their multiply.  Elsewhere
-    // sdims[d] equals dims[d].
-    dim_dev sdims[3];
-    double* snrow[3] = {nullptr, nullptr, nullptr};
-    double* skdt[3] = {nullptr, nullptr, nullptr};
-    double band_dt = std::nan("");
-    double* scratch[4] = {nullptr, nullptr, nullptr, nullptr};
-    double* ping = nullptr;  // second state buffer of the step loop
-    double uext_sum[3] = {0, 0, 0};  // sum over columns of the applied U extents
-    double* host_io = nullptr;
-    double* red = nullptr;  // 1025 doubles: dot-product partials + result
-    std::vector<double> xq[3];  // Gauss points per direction (empty if not described)
-    double* qpool = nullptr;    // Gauss-point work space (grown on demand)
-    size_t qpool_size = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    dev_arena arena;
-    // graph of two steps u -> ping -> u, specialised on (u, dt)
-    cudaGraphExec_t graph = nullptr;
-    double graph_dt = std::nan("");
-    double* graph_u = nullptr;
-    // single-step graphs of adsg_heat_step, specialised on (prev, next, dt):
-    // a replayed graph runs the step's kernels back to back with shorter gaps
-    // than stream launches (130^3 p=2: 191.5 against 201.6 us per step)
-    struct step_graph {
-        const double* prev;
-        double* next;
-        double dt;
-        cudaGraphExec_t exec;
-    };
-    std::vector<step_graph> step_graphs;  // most recently used last
-    long long step_graph_hits = 0, step_graph_misses = 0;
-    int step_graphs_on = 1;  // chosen at creation: replay pays on all but launch-bound grids
-    // the host-buffer steps (upload pass, steps, download) of one pinned buffer
-    cudaGraphExec_t host_graph = nullptr;
-    const double* host_graph_u = nullptr;
-    double host_graph_dt = std::nan("");
-    int host_graph_steps = 0;
-    void drop_step_graphs() {
-        for (auto& g : step_graphs) cudaGraphExecDestroy(g.exec);
-        step_graphs.clear();
-        if (host_graph) cudaGraphExecDestroy(host_graph);
-        host_graph = nullptr;
-        host_graph_u = nullptr;
-    }
-    // stage timers
-    bool timing = false;
-    bool capturing = false;
-    struct timed { int stage; cudaEvent_t a, b; };
-    std::vector<timed> pending;
-    std::vector<cudaEvent_t> spare;
-    double stage_ms[ADSG_NSTAGES] = {};
-    long long stage_launches[ADSG_NSTAGES] = {};
-    // adjoints created on this context (detached when the context goes first)
-    std::vector<adsg_adjoint*> adjoints;
-    int pdl = 0;     // programmatic dependent launch for the step kernels (chosen at creation)
-    int fuse_x = 0;  // the step fuses the x band pass with the x solve (chosen at creation)
-    int step_1block = 0;  // small 2D grids: the whole step in one block (chosen at creation)
-
-    cudaEvent_t take_event() {
-        if (!spare.empty()) {
-            cudaEvent_t e = spare.back();
-            spare.pop_back();
-            return e;
-        }
-        cudaEvent_t e = nullptr;
-        cudaEventCreate(&e);
-        return e;
-    }
-    void drain() {
-        for (auto& t : pending) {
-            float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
-                stage_ms[t.stage] += ms;
-                stage_launches[t.stage] += 1;
-            }
-            spare.push_back(t.a);
-            spare.push_back(t.b);
-        }
-        pending.clear();
-    }
-
-    ~adsg_ctx() {
-        if (graph) cudaGraphExecDestroy(graph);
-        drop_step_graphs();
-        if (stream) cudaStreamSynchronize(stream);
-        if (qpool) cudaFree(qpool);
-        for (auto& t : pending) {
-            cudaEventDestroy(t.a);
-            cudaEventDestroy(t.b);
-        }
-        for (auto e : spare) cudaEventDestroy(e);
-        if (own_stream && stream) cudaStreamDestroy(stream);
-    }
-};
-
-// Brackets one kernel launch with timer events when timers are on.
-struct stage_scope {
-    adsg_ctx* c;
-    int stage;
-    cudaEvent_t a = nullptr;
-    stage_scope(adsg_ctx* ctx, int st) : c(ctx), stage(st) {
-        if (c->timing && !c->capturing) {
-            a = c->take_event();
-            cudaEventRecord(a, c->stream);
-        }
-    }
-    ~stage_scope() {
-        if (a) {
-            cudaEvent_t b = c->take_event();
-            cudaEventRecord(b, c->stream);
-            c->pending.push_back({stage, a, b});
-        }
-    }
-};
+#include "adsg_context.cuh"
 
 namespace {
 
@@ -1127,6 +965,8 @@ int heat_steps_host_graph(adsg_ctx* c, double* u, double dt, int nsteps) {
 namespace adsg {
 cudaStream_t ctx_stream(adsg_ctx* c) { return c->stream; }
 int ctx_prepare_dt(adsg_ctx* c, double dt) { return ensure_dt_bands(c, dt); }
+int ctx_rhs(adsg_ctx* c, const double* u, double* rhs, double dt) { return enqueue_rhs(c, u, rhs, dt); }
+int ctx_solve(adsg_ctx* c, double* x, int trans) { return enqueue_solve(c, x, trans); }
 }  // namespace adsg
 
 extern "C" {
@@ -1572,511 +1412,6 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
                                     flops[ADSG_STAGE_RHS_X] + flops[ADSG_STAGE_SOLVE_X] + flops[ADSG_STAGE_SOLVE_Y] +
                                     flops[ADSG_STAGE_SOLVE_Z];
     bytes[ADSG_STAGE_STEP_1BLOCK] = 16.0 * total;
-    return 0;
-}
-
-// ---------------------------------------------------------------------------
-// Adjoint: reverse-mode gradients of a loss of u(T) with respect to the
-// initial coefficients and the diffusion-field coefficients kappa, for the
-// kappa-weighted explicit step u_{k+1} = M^{-1} R(kappa) u_k.  R is symmetric,
-// so the adjoint step is lambda_k = R(kappa) M^{-T} lambda_{k+1}; dL/dkappa
-// accumulates mu_{k+1}^T (dR/dkappa) u_k with mu_{k+1} = M^{-T} lambda_{k+1}.
-// Forward states are checkpointed every C steps (C = ceil(sqrt(N)) by
-// default) and each segment is recomputed once during the backward sweep.
-// ---------------------------------------------------------------------------
-struct adsg_adjoint {
-    adsg_ctx* ctx = nullptr;  // null once the context is destroyed
-    int nsteps = 0, every = 1, nck = 0;
-    double dt = 0.0;
-    bool forward_done = false;
-    double* ck = nullptr;     // nck states
-    double* seg = nullptr;    // every states
-    double* work[2] = {nullptr, nullptr};
-    double* kappa = nullptr;  // copy of the field used by the forward pass
-    double* partial = nullptr;
-    double* scalar = nullptr;
-    dev_arena arena;
-};
-
-extern "C++" {
-namespace adsg {
-
-void detach_adjoints(adsg_ctx* c) {
-    for (adsg_adjoint* a : c->adjoints) a->ctx = nullptr;
-    c->adjoints.clear();
-}
-
-}  // namespace adsg
-}
-
-namespace {
-
-int elem_step(adsg_adjoint* a, const double* u, double* out) {
-    adsg_ctx* c = a->ctx;
-    ADSG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * c->size, c->stream), "memset");
-    {
-        stage_scope sc(c, ADSG_STAGE_RHS_ELEM);
-        ADSG_CUDA_TRY(launch_rhs_elem(c->ndim, c->dims, u, a->kappa, out, a->dt, c->stream), "element rhs");
-    }
-    return enqueue_solve(c, out, 0);
-}
-
-}  // namespace
-
-int adsg_adjoint_create(adsg_ctx* ctx, int nsteps, double dt, int checkpoint_every, adsg_adjoint** out) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (nsteps < 1) return fail(-2, "nsteps must be >= 1");
-    if (!std::isfinite(dt)) return fail(-3, "dt must be finite");
-    if (checkpoint_every < 0) return fail(-4, "checkpoint_every must be >= 0");
-    if (!out) return fail(-5, "out is NULL");
-    if (ctx->ndim < 2) return fail(ADSG_ERR_UNSUPPORTED, "the adjoint needs a 2D or 3D context");
-    for (int d = 0; d < ctx->ndim; ++d)
-        if (ctx->dims[d].p != ctx->dims[0].p || ctx->dims[d].q != ctx->dims[d].p + 1)
-            return fail(ADSG_ERR_UNSUPPORTED, "the adjoint needs the same degree and p+1 Gauss points in every direction");
-    auto* a = new (std::nothrow) adsg_adjoint;
-    if (!a) return fail(ADSG_ERR_NOMEM, "host allocation failed");
-    a->ctx = ctx;
-    a->nsteps = nsteps;
-    a->dt = dt;
-    a->every = checkpoint_every > 0 ? checkpoint_every
-                                    : std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(nsteps)))));
-    a->every = std::min(a->every, nsteps);
-    a->nck = (nsteps + a->every - 1) / a->every;
-    const size_t n = static_cast<size_t>(ctx->size);
-    cudaError_t e = a->arena.alloc(&a->ck, n * a->nck);
-    if (e == cudaSuccess) e = a->arena.alloc(&a->seg, n * a->every);
-    if (e == cudaSuccess) e = a->arena.alloc(&a->work[0], n);
-    if (e == cudaSuccess) e = a->arena.alloc(&a->work[1], n);
-    if (e == cudaSuccess) e = a->arena.alloc(&a->kappa, n);
-    if (e == cudaSuccess) e = a->arena.alloc(&a->partial, 1024);
-    if (e == cudaSuccess) e = a->arena.alloc(&a->scalar, 1);
-    if (e != cudaSuccess) {
-        delete a;
-        return fail_cuda(e, "adjoint allocation");
-    }
-    ctx->adjoints.push_back(a);
-    *out = a;
-    return 0;
-}
-
-int adsg_adjoint_destroy(adsg_adjoint* a) {
-    if (!a) return 0;
-    if (a->ctx) {
-        cudaStreamSynchronize(a->ctx->stream);
-        auto& v = a->ctx->adjoints;
-        v.erase(std::remove(v.begin(), v.end(), a), v.end());
-    }
-    delete a;  // freeing device memory waits for the device
-    return 0;
-}
-
-int adsg_adjoint_checkpoints(const adsg_adjoint* a, int* every, int* count) {
-    if (!a) return fail(-1, "adjoint is NULL");
-    if (every) *every = a->every;
-    if (count) *count = a->nck;
-    return 0;
-}
-
-int adsg_adjoint_forward(adsg_adjoint* a, const double* u0_dev, const double* kappa_dev, double* uT_dev) {
-    if (!a) return fail(-1, "adjoint is NULL");
-    if (!u0_dev) return fail(-2, "u0 is NULL");
-    if (!kappa_dev) return fail(-3, "kappa is NULL");
-    if (!uT_dev) return fail(-4, "uT is NULL");
-    if (!a->ctx) return fail(-1, "the adjoint's context was destroyed");
-    adsg_ctx* c = a->ctx;
-    const size_t bytes = sizeof(double) * c->size;
-    cudaStream_t s = c->stream;
-    ADSG_CUDA_TRY(cudaMemcpyAsync(a->kappa, kappa_dev, bytes, cudaMemcpyDeviceToDevice, s), "copy kappa");
-    ADSG_CUDA_TRY(cudaMemcpyAsync(a->ck, u0_dev, bytes, cudaMemcpyDeviceToDevice, s), "checkpoint 0");
-    const double* cur = a->ck;
-    for (int k = 0; k < a->nsteps; ++k) {
-        double* nxt = a->work[k & 1];
-        if (int st = elem_step(a, cur, nxt)) return st;
-        const int kk = k + 1;
-        if (kk < a->nsteps && kk % a->every == 0) {
-            double* slot = a->ck + static_cast<size_t>(kk / a->every) * c->size;
-            ADSG_CUDA_TRY(cudaMemcpyAsync(slot, nxt, bytes, cudaMemcpyDeviceToDevice, s), "checkpoint");
-            cur = slot;
-        } else {
-            cur = nxt;
-        }
-    }
-    ADSG_CUDA_TRY(cudaMemcpyAsync(uT_dev, cur, bytes, cudaMemcpyDeviceToDevice, s), "copy u(T)");
-    a->forward_done = true;
-    return 0;
-}
-
-int adsg_adjoint_backward(adsg_adjoint* a, const double* dL_duT_dev, double* grad_u0_dev, double* grad_kappa_dev) {
-    if (!a) return fail(-1, "adjoint is NULL");
-    if (!dL_duT_dev) return fail(-2, "dL/du(T) is NULL");
-    if (!grad_u0_dev) return fail(-3, "grad_u0 is NULL");
-    if (!grad_kappa_dev) return fail(-4, "grad_kappa is NULL");
-    if (!a->forward_done) return fail(-1, "adsg_adjoint_forward must run first");
-    if (!a->ctx) return fail(-1, "the adjoint's context was destroyed");
-    adsg_ctx* c = a->ctx;
-    const size_t n = static_cast<size_t>(c->size);
-    const size_t bytes = sizeof(double) * n;
-    cudaStream_t s = c->stream;
-    double* lam = a->work[0];
-    double* other = a->work[1];
-    ADSG_CUDA_TRY(cudaMemcpyAsync(lam, dL_duT_dev, bytes, cudaMemcpyDeviceToDevice, s), "copy lambda");
-    ADSG_CUDA_TRY(cudaMemsetAsync(grad_kappa_dev, 0, bytes, s), "zero grad kappa");
-    for (int sidx = a->nck - 1; sidx >= 0; --sidx) {
-        const int k0 = sidx * a->every;
-        const int k1 = std::min(k0 + a->every, a->nsteps);
-        // recompute u_{k0} .. u_{k1-1} from the checkpoint
-        ADSG_CUDA_TRY(cudaMemcpyAsync(a->seg, a->ck + static_cast<size_t>(sidx) * n, bytes, cudaMemcpyDeviceToDevice, s),
-                      "segment start");
-        for (int i = 0; i + 1 < k1 - k0; ++i)
-            if (int st = elem_step(a, a->seg + static_cast<size_t>(i) * n, a->seg + static_cast<size_t>(i + 1) * n))
-                return st;
-        for (int k = k1 - 1; k >= k0; --k) {
-            if (int st = enqueue_solve(c, lam, 1)) return st;  // lam <- mu_{k+1} = M^{-T} lambda_{k+1}
-            ADSG_CUDA_TRY(cudaMemsetAsync(other, 0, bytes, s), "memset");
-            {
-                // grad kappa += mu^T (dR/dkappa) u_k and other = R^T mu (R is symmetric)
-                stage_scope sc(c, ADSG_STAGE_RHS_ELEM);
-                ADSG_CUDA_TRY(launch_adjoint_pair(c->ndim, c->dims, a->seg + static_cast<size_t>(k - k0) * n, lam,
-                                                  a->kappa, other, grad_kappa_dev, a->dt, s),
-                              "kappa gradient and R^T mu");
-            }
-            std::swap(lam, other);  // lam <- lambda_k = R mu_{k+1}
-        }
-    }
-    ADSG_CUDA_TRY(cudaMemcpyAsync(grad_u0_dev, lam, bytes, cudaMemcpyDeviceToDevice, s), "copy grad u0");
-    return 0;
-}
-
-int adsg_mass_loss(adsg_ctx* ctx, const double* u_dev, const double* target_dev, double* scratch_dev, double* loss_host,
-                   double* grad_dev) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!u_dev) return fail(-2, "u is NULL");
-    if (!target_dev) return fail(-3, "target is NULL");
-    if (!scratch_dev) return fail(-4, "scratch is NULL");
-    if (!loss_host) return fail(-5, "loss is NULL");
-    if (!grad_dev) return fail(-6, "grad is NULL");
-    if (grad_dev == scratch_dev) return fail(-6, "grad must not alias scratch");
-    const long long n = ctx->size;
-    cudaStream_t s = ctx->stream;
-    // scratch <- u - target ; grad <- M scratch (the factored mass operator, dt = 0)
-    ADSG_CUDA_TRY(cudaMemcpyAsync(scratch_dev, u_dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy");
-    ADSG_CUDA_TRY(launch_axpby(scratch_dev, -1.0, target_dev, 1.0, n, s), "difference");
-    if (int st = enqueue_rhs(ctx, scratch_dev, grad_dev, 0.0)) return st;
-    if (!ctx->red) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->red, 1025), "reduction alloc");
-    ADSG_CUDA_TRY(launch_dot(scratch_dev, grad_dev, n, ctx->red, ctx->red + 1024, s), "dot");
-    ADSG_CUDA_TRY(cudaMemcpyAsync(loss_host, ctx->red + 1024, sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
-    ADSG_CUDA_TRY(launch_axpby(grad_dev, 0.0, grad_dev, 2.0, n, s), "scale");
-    ADSG_CUDA_TRY(cudaStreamSynchronize(s), "synchronize");
-    return 0;
-}
-
-// ---------------------------------------------------------------------------
-// Gauss-point utilities
-// ---------------------------------------------------------------------------
-namespace {
-
-long long quad_extent(const adsg_ctx* c, int d) { return static_cast<long long>(c->dims[d].elements) * c->dims[d].q; }
-
-long long quad_total(const adsg_ctx* c) {
-    long long t = 1;
-    for (int d = 0; d < c->ndim; ++d) t *= quad_extent(c, d);
-    return t;
-}
-
-int qpool_get(adsg_ctx* c, size_t doubles, double** out) {
-    if (c->qpool_size < doubles) {
-        if (c->qpool) {
-            cudaStreamSynchronize(c->stream);
-            cudaFree(c->qpool);
-            c->qpool = nullptr;
-            c->qpool_size = 0;
-        }
-        ADSG_CUDA_TRY(cudaMalloc(&c->qpool, doubles * sizeof(double)), "Gauss-point work space");
-        c->qpool_size = doubles;
-    }
-    *out = c->qpool;
-    return 0;
-}
-
-// interpolate u to the Gauss points: val (and the ndim derivatives in grad)
-int enqueue_eval_quad(adsg_ctx* c, const double* u, double* val, double* grad) {
-    const int nd = c->ndim;
-    const long long n0 = c->n[0], n1 = nd > 1 ? c->n[1] : 1, n2 = nd > 2 ? c->n[2] : 1;
-    const long long Q0 = quad_extent(c, 0), Q1 = nd > 1 ? quad_extent(c, 1) : 1, Q2 = nd > 2 ? quad_extent(c, 2) : 1;
-    const long long NQ = Q0 * Q1 * Q2;
-    cudaStream_t s = c->stream;
-    if (nd == 1) {
-        ADSG_CUDA_TRY(launch_quad_interp(u, val, grad, c->dims[0], 1, 1, s), "interp x");
-        return 0;
-    }
-    const size_t a = static_cast<size_t>(Q0 * n1 * n2), b = static_cast<size_t>(Q0 * Q1 * n2);
-    double* w = nullptr;
-    if (int st = qpool_get(c, 2 * a + 3 * b, &w)) return st;
-    double *A0 = w, *A1 = w + a, *B00 = w + 2 * a, *B01 = B00 + b, *B10 = B01 + b;
-    const bool g = grad != nullptr;
-    ADSG_CUDA_TRY(launch_quad_interp(u, A0, g ? A1 : nullptr, c->dims[0], 1, n1 * n2, s), "interp x");
-    if (nd == 2) {
-        ADSG_CUDA_TRY(launch_quad_interp(A0, val, g ? grad + NQ : nullptr, c->dims[1], Q0, 1, s), "interp y");
-        if (g) ADSG_CUDA_TRY(launch_quad_interp(A1, grad, nullptr, c->dims[1], Q0, 1, s), "interp y");
-        return 0;
-    }
-    ADSG_CUDA_TRY(launch_quad_interp(A0, B00, g ? B01 : nullptr, c->dims[1], Q0, n2, s), "interp y");
-    if (g) ADSG_CUDA_TRY(launch_quad_interp(A1, B10, nullptr, c->dims[1], Q0, n2, s), "interp y");
-    ADSG_CUDA_TRY(launch_quad_interp(B00, val, g ? grad + 2 * NQ : nullptr, c->dims[2], Q0 * Q1, 1, s), "interp z");
-    if (g) {
-        ADSG_CUDA_TRY(launch_quad_interp(B01, grad + NQ, nullptr, c->dims[2], Q0 * Q1, 1, s), "interp z");
-        ADSG_CUDA_TRY(launch_quad_interp(B10, grad, nullptr, c->dims[2], Q0 * Q1, 1, s), "interp z");
-    }
-    return 0;
-}
-
-int enqueue_load_vector(adsg_ctx* c, const double* fq, double* out) {
-    const int nd = c->ndim;
-    const long long n0 = c->n[0], n1 = nd > 1 ? c->n[1] : 1;
-    const long long Q1 = nd > 1 ? quad_extent(c, 1) : 1, Q2 = nd > 2 ? quad_extent(c, 2) : 1;
-    cudaStream_t s = c->stream;
-    if (nd == 1) {
-        ADSG_CUDA_TRY(launch_quad_project(fq, out, c->dims[0], c->dims[0].erange, 1, 1, s), "project x");
-        return 0;
-    }
-    const size_t a = static_cast<size_t>(n0 * Q1 * Q2), b = static_cast<size_t>(n0 * n1 * Q2);
-    double* w = nullptr;
-    if (int st = qpool_get(c, a + (nd == 3 ? b : 0), &w)) return st;
-    ADSG_CUDA_TRY(launch_quad_project(fq, w, c->dims[0], c->dims[0].erange, 1, Q1 * Q2, s), "project x");
-    if (nd == 2) {
-        ADSG_CUDA_TRY(launch_quad_project(w, out, c->dims[1], c->dims[1].erange, n0, 1, s), "project y");
-        return 0;
-    }
-    ADSG_CUDA_TRY(launch_quad_project(w, w + a, c->dims[1], c->dims[1].erange, n0, Q2, s), "project y");
-    ADSG_CUDA_TRY(launch_quad_project(w + a, out, c->dims[2], c->dims[2].erange, n0 * n1, 1, s), "project z");
-    return 0;
-}
-
-}  // namespace
-
-long long adsg_quad_size(const adsg_ctx* ctx) { return ctx ? quad_total(ctx) : 0; }
-
-int adsg_count_nonfinite(adsg_ctx* ctx, const double* u_dev, long long* count_out) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!u_dev) return fail(-2, "u is NULL");
-    if (!count_out) return fail(-3, "count is NULL");
-    if (!ctx->red) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->red, 1025), "reduction alloc");
-    auto* cnt = reinterpret_cast<unsigned long long*>(ctx->red + 1024);
-    ADSG_CUDA_TRY(launch_count_nonfinite(u_dev, ctx->size, cnt, ctx->stream), "count");
-    unsigned long long host = 0;
-    ADSG_CUDA_TRY(cudaMemcpyAsync(&host, cnt, sizeof(host), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
-    *count_out = static_cast<long long>(host);
-    return 0;
-}
-
-int adsg_load_vector(adsg_ctx* ctx, const double* fq_dev, double* out_dev) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!fq_dev) return fail(-2, "fq is NULL");
-    if (!out_dev) return fail(-3, "out is NULL");
-    return enqueue_load_vector(ctx, fq_dev, out_dev);
-}
-
-int adsg_projection(adsg_ctx* ctx, const double* fq_dev, double* out_dev) {
-    if (int st = adsg_load_vector(ctx, fq_dev, out_dev)) return st;
-    return enqueue_solve(ctx, out_dev, 0);
-}
-
-int adsg_eval_quad(adsg_ctx* ctx, const double* u_dev, double* val_dev, double* grad_dev) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!u_dev) return fail(-2, "u is NULL");
-    if (!val_dev) return fail(-3, "val is NULL");
-    return enqueue_eval_quad(ctx, u_dev, val_dev, grad_dev);
-}
-
-int adsg_norms(adsg_ctx* ctx, const double* u_dev, double* l2_out, double* h1_out) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!u_dev) return fail(-2, "u is NULL");
-    if (!l2_out) return fail(-3, "l2 is NULL");
-    if (!h1_out) return fail(-4, "h1 is NULL");
-    double* w = nullptr;
-    if (int st = qpool_get(ctx, static_cast<size_t>(ctx->size), &w)) return st;
-    if (!ctx->red) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->red, 1025), "reduction alloc");
-    double vals[2];
-    const double dts[2] = {0.0, -1.0};  // rhs(dt) = M u - dt K u: dt = 0 -> M u, dt = -1 -> (M + K) u
-    for (int k = 0; k < 2; ++k) {
-        if (int st = enqueue_rhs(ctx, u_dev, w, dts[k])) return st;
-        ADSG_CUDA_TRY(launch_dot(u_dev, w, ctx->size, ctx->red, ctx->red + 1024, ctx->stream), "dot");
-        ADSG_CUDA_TRY(cudaMemcpyAsync(&vals[k], ctx->red + 1024, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
-                      "D2H");
-        ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
-    }
-    *l2_out = std::sqrt(std::max(vals[0], 0.0));
-    *h1_out = std::sqrt(std::max(vals[1], 0.0));
-    return 0;
-}
-
-int adsg_errors(adsg_ctx* ctx, const double* u_dev, const double* fq_dev, const double* fgrad_dev, double* l2_out,
-                double* h1_out) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!u_dev) return fail(-2, "u is NULL");
-    if (!fq_dev) return fail(-3, "fq is NULL");
-    if (!l2_out) return fail(-5, "l2 is NULL");
-    if (!h1_out) return fail(-6, "h1 is NULL");
-    const long long NQ = quad_total(ctx);
-    const int nd = ctx->ndim;
-    // the interpolation's own work space first, then the point tensors after it
-    const long long n1 = nd > 1 ? ctx->n[1] : 1, n2 = nd > 2 ? ctx->n[2] : 1;
-    const long long Q0 = quad_extent(ctx, 0), Q1 = nd > 1 ? quad_extent(ctx, 1) : 1;
-    const size_t work = nd == 1 ? 0 : static_cast<size_t>(2 * Q0 * n1 * n2 + 3 * Q0 * Q1 * n2);
-    double* w = nullptr;
-    if (int st = qpool_get(ctx, work + static_cast<size_t>(NQ) * (1 + nd), &w)) return st;
-    double* val = w + work;
-    double* grad = val + NQ;
-    // enqueue_eval_quad uses the front of the pool; keep the point tensors behind it
-    if (int st = enqueue_eval_quad(ctx, u_dev, val, fgrad_dev ? grad : nullptr)) return st;
-    if (!ctx->red) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->red, 1025), "reduction alloc");
-    double l2 = 0.0, g2 = 0.0;
-    field_set F;
-    F.nf = 1;
-    F.a[0] = val;
-    F.b[0] = fq_dev;
-    ADSG_CUDA_TRY(launch_quad_wdiff(F, ctx->dims, nd, NQ, ctx->red, ctx->red + 1024, ctx->stream), "weighted sum");
-    ADSG_CUDA_TRY(cudaMemcpyAsync(&l2, ctx->red + 1024, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
-    if (fgrad_dev) {
-        field_set G;
-        G.nf = nd;
-        for (int k = 0; k < nd; ++k) {
-            G.a[k] = grad + k * NQ;
-            G.b[k] = fgrad_dev + k * NQ;
-        }
-        ADSG_CUDA_TRY(launch_quad_wdiff(G, ctx->dims, nd, NQ, ctx->red, ctx->red + 1024, ctx->stream), "weighted sum");
-        ADSG_CUDA_TRY(cudaMemcpyAsync(&g2, ctx->red + 1024, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-        ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
-        *h1_out = std::sqrt(l2 + g2);
-    } else {
-        *h1_out = -1.0;
-    }
-    *l2_out = std::sqrt(l2);
-    return 0;
-}
-
-int adsg_quad_points(const adsg_ctx* ctx, int d, double* xq_host) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (d < 0 || d >= ctx->ndim) return fail(-2, "direction out of range");
-    if (!xq_host) return fail(-3, "xq is NULL");
-    if (ctx->xq[d].empty()) return fail(ADSG_ERR_UNSUPPORTED, "the descriptor gave no Gauss points (xq)");
-    std::memcpy(xq_host, ctx->xq[d].data(), sizeof(double) * ctx->xq[d].size());
-    return 0;
-}
-
-// ---------------------------------------------------------------------------
-// Generalised ADS: per-line bands along one special direction.
-// ---------------------------------------------------------------------------
-struct adsg_line_bands {
-    line_tables T;
-    long long nlines = 0;
-    int* line_matrix = nullptr;
-    int ku = 0;
-    dev_arena arena;
-};
-
-int adsg_line_bands_create(int n, int kl, int ku, int ldab, int nmat, const double* ab, const int* ipiv,
-                           long long nlines, const int* line_matrix, adsg_line_bands** out) {
-    if (n < 1) return fail(-1, "n must be >= 1");
-    if (kl < 0 || kl > 16) return fail(-2, "kl must be in [0, 16]");
-    if (ku < 0 || kl + ku > 32) return fail(-3, "ku must be >= 0 and kl + ku <= 32");
-    if (ldab < 2 * kl + ku + 1) return fail(-4, "ldab < 2*kl+ku+1");
-    if (nmat < 1) return fail(-5, "nmat must be >= 1");
-    if (!ab) return fail(-6, "ab is NULL");
-    if (!ipiv) return fail(-7, "ipiv is NULL");
-    if (nlines < 1) return fail(-8, "nlines must be >= 1");
-    if (!line_matrix) return fail(-9, "line_matrix is NULL");
-    if (!out) return fail(-10, "out is NULL");
-    for (long long l = 0; l < nlines; ++l)
-        if (line_matrix[l] < 0 || line_matrix[l] >= nmat) return fail(-9, "line_matrix entry out of range");
-    std::vector<double> lmul, ucol, rdiag;
-    std::vector<int> piv, uext;
-    int tkl = 1, tw = 1;
-    for (int m = 0; m < nmat; ++m) {
-        const int* pm = ipiv + static_cast<size_t>(m) * n;
-        for (int j = 0; j < n; ++j)
-            if (pm[j] < j + 1 || pm[j] > std::min(n, j + 1 + kl)) return fail(-7, "pivot outside the band");
-        solve_tables t;
-        if (make_solve_tables(n, kl, ku, ldab, ab + static_cast<size_t>(m) * ldab * n, pm, t))
-            return fail(ADSG_ERR_SINGULAR, "zero diagonal in a factorised band");
-        tkl = t.kl;
-        tw = t.w;
-        lmul.insert(lmul.end(), t.lmul.begin(), t.lmul.begin() + static_cast<long long>(n) * t.kl);
-        ucol.insert(ucol.end(), t.ucol.begin(), t.ucol.end());
-        rdiag.insert(rdiag.end(), t.rdiag.begin(), t.rdiag.end());
-        piv.insert(piv.end(), t.piv.begin(), t.piv.end());
-        uext.insert(uext.end(), t.uext.begin(), t.uext.end());
-    }
-    auto* b = new (std::nothrow) adsg_line_bands;
-    if (!b) return fail(ADSG_ERR_NOMEM, "host allocation failed");
-    b->T.n = n;
-    b->T.kl = tkl;
-    b->T.w = tw;
-    b->T.nmat = nmat;
-    b->nlines = nlines;
-    b->ku = ku;
-    double *dl, *du, *dr;
-    int *dp, *de;
-    cudaError_t e = b->arena.upload(&dl, lmul.data(), lmul.size(), nullptr);
-    if (e == cudaSuccess) e = b->arena.upload(&du, ucol.data(), ucol.size(), nullptr);
-    if (e == cudaSuccess) e = b->arena.upload(&dr, rdiag.data(), rdiag.size(), nullptr);
-    if (e == cudaSuccess) e = b->arena.upload(&dp, piv.data(), piv.size(), nullptr);
-    if (e == cudaSuccess) e = b->arena.upload(&de, uext.data(), uext.size(), nullptr);
-    if (e == cudaSuccess) e = b->arena.upload(&b->line_matrix, line_matrix, static_cast<size_t>(nlines), nullptr);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
-    if (e != cudaSuccess) {
-        delete b;
-        return fail_cuda(e, "line bands upload");
-    }
-    b->T.lmul = dl;
-    b->T.ucol = du;
-    b->T.rdiag = dr;
-    b->T.piv = dp;
-    b->T.uext = de;
-    *out = b;
-    return 0;
-}
-
-int adsg_line_bands_destroy(adsg_line_bands* b) {
-    delete b;
-    return 0;
-}
-
-int adsg_ads_solve_general(adsg_ctx* ctx, int special_dim, const adsg_line_bands* lines, double* rhs_dev) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (special_dim < 0 || special_dim >= ctx->ndim) return fail(-2, "special_dim out of range");
-    if (!lines) return fail(-3, "lines is NULL");
-    if (!rhs_dev) return fail(-4, "rhs is NULL");
-    if (lines->T.n != ctx->n[special_dim]) return fail(-3, "line bands size differs from the special dimension");
-    const line_layout Ls = make_line_layout(ctx->n, ctx->ndim, special_dim);
-    if (lines->nlines != Ls.nlines) return fail(-3, "line_matrix length differs from the number of lines");
-    {
-        stage_scope sc(ctx, ADSG_STAGE_SOLVE_X + special_dim);
-        ADSG_CUDA_TRY(launch_line_solve_permat(rhs_dev, lines->T, Ls, lines->line_matrix, ctx->n[0],
-                                               ctx->ndim > 2 ? ctx->n[2] : 1, special_dim, ctx->ndim, ctx->stream),
-                      "special direction solve");
-    }
-    // then the standard directions, cyclically after the special one
-    for (int k = 1; k < ctx->ndim; ++k) {
-        const int d = (special_dim + k) % ctx->ndim;
-        const line_layout L = make_line_layout(ctx->n, ctx->ndim, d);
-        stage_scope sc(ctx, ADSG_STAGE_SOLVE_X + d);
-        ADSG_CUDA_TRY(launch_line_solve(rhs_dev, ctx->dims[d], L, 0, ctx->stream), "line solve");
-    }
-    return 0;
-}
-
-int adsg_ads_solve_general_host(adsg_ctx* ctx, int special_dim, const adsg_line_bands* lines, double* rhs_host) {
-    if (!ctx) return fail(-1, "ctx is NULL");
-    if (!rhs_host) return fail(-4, "rhs is NULL");
-    if (!ctx->host_io) ADSG_CUDA_TRY(ctx->arena.alloc(&ctx->host_io, ctx->size), "io alloc");
-    const size_t bytes = sizeof(double) * ctx->size;
-    ADSG_CUDA_TRY(cudaMemcpyAsync(ctx->host_io, rhs_host, bytes, cudaMemcpyHostToDevice, ctx->stream), "H2D");
-    if (int st = adsg_ads_solve_general(ctx, special_dim, lines, ctx->host_io)) return st;
-    ADSG_CUDA_TRY(cudaMemcpyAsync(rhs_host, ctx->host_io, bytes, cudaMemcpyDeviceToHost, ctx->stream), "D2H");
-    ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
     return 0;
 }
 
