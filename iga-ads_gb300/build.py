@@ -23,7 +23,7 @@ LIB = os.path.join(HERE, "ads_gb300", "libads_gb300.so")
 
 CUDA_SOURCES = ["adsg_kernels.cu", "adsg_elem.cu", "adsg_capi.cu", "adsg_adjoint.cu", "adsg_points.cu", "adsg_general.cu",
                 "adsg_batch.cu", "adsg_noalloc.cu", "adsg_quad.cu"]
-CXX_SOURCES = ["adsg_host.cpp"]
+CXX_SOURCES = ["adsg_host.cpp", "adsg_tables.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
