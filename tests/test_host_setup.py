@@ -75,3 +75,26 @@ def test_initial_field_is_seeded_and_smooth_plus_noise():
     u = inputs.splitmix_uniform(7, 100000)
     assert 0.0 <= u.min() and u.max() < 1.0
     assert abs(u.mean() - 0.5) < 0.01
+
+
+def test_direction_tables_on_the_host(tmp_path):
+    """tests/cpp/tables_check.cpp, built from the engine's host sources alone:
+    LAPACK-order solve tables, the symmetric row range of the pair-sum passes,
+    the two-ended factorisation (built exactly for n >= 4k+2, self-checked
+    against the LAPACK-order solve) and its row-scaled form, degrees 1-4."""
+    import shutil
+    import subprocess
+
+    from conftest import ROOT
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+    csrc = os.path.join(ROOT, "iga-ads_gb300", "csrc")
+    exe = str(tmp_path / "tables_check")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", csrc, "-I", cuda_inc, "-o", exe,
+           os.path.join(ROOT, "tests", "cpp", "tables_check.cpp"), os.path.join(csrc, "adsg_tables.cpp"),
+           os.path.join(csrc, "adsg_host.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.strip().endswith("ok"), out.stdout[-2000:]
