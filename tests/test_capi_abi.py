@@ -95,3 +95,16 @@ def test_device_entry_points_reject_null_context():
     assert lib.adsg_ads_solve(None, None, None) == -1
     assert lib.adsg_heat_steps(None, None, 1.0, 1) == -1
     assert lib.adsg_ctx_destroy(None) == 0
+
+
+def test_every_engine_source_is_built():
+    """iga-ads_gb300/build.py lists every CUDA and C++ source of the engine
+    (a source left out would silently drop its entry points)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("engine_build", os.path.join(ROOT, "iga-ads_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    csrc = os.path.join(ROOT, "iga-ads_gb300", "csrc")
+    on_disk = sorted(f for f in os.listdir(csrc) if f.endswith((".cu", ".cpp")))
+    assert sorted(b.CUDA_SOURCES + b.CXX_SOURCES) == on_disk
