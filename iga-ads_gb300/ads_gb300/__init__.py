@@ -143,6 +143,8 @@ def library() -> ctypes.CDLL:
         "adsg_batch_engine": (i, [vp]),
         "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
+        "adsg_dgbtrs_checked_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
+                                     _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -552,7 +554,9 @@ def ads_solve(ctx: Context, rhs, buf=None) -> None:
 def dgbtrs(trans: str, n: int, kl: int, ku: int, nrhs: int, ab: np.ndarray, ldab: int,
            ipiv: np.ndarray, b: np.ndarray, ldb: int) -> int:
     """LAPACK dgbtrs_ with the same arguments (host arrays, column-major b), solved
-    on the GPU through adsg_dgbtrs_.  Returns info (0 or -k for argument k)."""
+    on the GPU through adsg_dgbtrs_.  Returns info: 0, -k for argument k, or
+    positive when b was left unsolved (a zero U diagonal at that column, or
+    n + 1 when the GPU solve could not run; AdsError is raised for the latter)."""
     ab = np.ascontiguousarray(ab, dtype=np.float64)
     ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
     _host(b)

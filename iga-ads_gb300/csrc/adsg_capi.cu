@@ -675,12 +675,6 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         delete c;
         return fail(-2, "tensor larger than 2^31 dofs");
     }
-    for (int d = 0; d < ndim; ++d) {
-        if (line_solve_smem_per_warp(dims[d].n) > 220 * 1024) {
-            delete c;
-            return fail(ADSG_ERR_UNSUPPORTED, "more than 850 dofs along one dimension");
-        }
-    }
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault);
     if (e != cudaSuccess) {
         delete c;
@@ -1149,8 +1143,17 @@ int adsg_heat_rhs_host(adsg_ctx* ctx, const double* u_prev_host, double* rhs_hos
 
 int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs, const double* ab,
                  const int* ldab, const int* ipiv, double* b, const int* ldb, int* info) {
-    auto ret = [&](int code, const char* msg) {
-        if (info) *info = code < 0 ? code : 0;
+    // info as LAPACK defines it for a bad argument (-k = k-th argument).  Where
+    // b is left unsolved for any other reason, info is positive as well, so a
+    // caller that reads only info sees the failure: the 1-based column of a
+    // zero U diagonal (dgbtrf's meaning of a positive info), or n + 1 when the
+    // GPU solve could not run (band too wide, CUDA failure).  The message is
+    // also written to stderr, as LAPACK's xerbla does.
+    const int n_unsolved = (n ? *n : 0) + 1;
+    auto ret = [&](int code, const char* msg, int pos_info = -1) {
+        const int v = code < 0 ? code : (pos_info > 0 ? pos_info : n_unsolved);
+        if (info) *info = v;
+        std::fprintf(stderr, "adsg_dgbtrs_: %s (info %d)\n", msg, v);
         return fail(code, msg);
     };
     if (!trans) return ret(-1, "trans is NULL");
@@ -1167,11 +1170,12 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
     if (!ipiv) return ret(-8, "ipiv is NULL");
     if (!b) return ret(-9, "b is NULL");
     if (*kl > 16 || *kl + *ku > 32) return ret(ADSG_ERR_UNSUPPORTED, "band wider than kl=16, kl+ku=32");
-    if (line_solve_smem_per_warp(*n) > 220 * 1024) return ret(ADSG_ERR_UNSUPPORTED, "n > 850");
     if (info) *info = 0;
     if (*n == 0 || *nrhs == 0) return 0;
     for (int j = 0; j < *n; ++j)
         if (ipiv[j] < j + 1 || ipiv[j] > std::min(*n, j + 1 + *kl)) return ret(-8, "pivot outside the band of a dgbtrf factorisation");
+    for (int j = 0; j < *n; ++j)
+        if (ab[static_cast<size_t>(j) * *ldab + *kl + *ku] == 0.0) return ret(ADSG_ERR_SINGULAR, "zero diagonal in U", j + 1);
     solve_tables tb;
     if (make_solve_tables(*n, *kl, *ku, *ldab, ab, ipiv, tb)) return ret(ADSG_ERR_SINGULAR, "zero diagonal in U");
 
@@ -1220,8 +1224,22 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     if (e != cudaSuccess) {
-        if (info) *info = 0;
+        if (info) *info = n_unsolved;
+        std::fprintf(stderr, "adsg_dgbtrs_: CUDA failure: %s (info %d)\n", cudaGetErrorString(e), n_unsolved);
         return fail_cuda(e, "dgbtrs");
+    }
+    return 0;
+}
+
+int adsg_dgbtrs_checked_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs,
+                         const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb, int* info) {
+    int local = 0;
+    int* ip = info ? info : &local;
+    const int rc = adsg_dgbtrs_(trans, n, kl, ku, nrhs, ab, ldab, ipiv, b, ldb, ip);
+    if (rc != 0 || *ip != 0) {
+        std::fprintf(stderr, "adsg_dgbtrs_checked_: the right-hand sides were not solved (info %d, %s); aborting\n", *ip,
+                     adsg_last_error());
+        std::abort();
     }
     return 0;
 }

@@ -422,30 +422,31 @@ __device__ __forceinline__ void stage_out(double* __restrict__ data, const doubl
     }
 }
 
-// dgbtrs 'N' on one staged line x[j*kPitch] (generic bands): the L-solve with
-// row exchanges (dgbtrs's forward loop), then the U-solve (dtbsv 'Upper','N',
+// dgbtrs 'N' on one line x[j*es] (generic bands): the L-solve with row
+// exchanges (dgbtrs's forward loop), then the U-solve (dtbsv 'Upper','N',
 // 'Non-unit') with the diagonal applied as a reciprocal, column by column in
-// LAPACK's order, through shared memory.
-__device__ __forceinline__ void sweep_n_generic(double* x, const dim_dev& D) {
+// LAPACK's order.  es is kPitch for a line staged in shared memory, or the
+// line's element stride in global memory.
+__device__ __forceinline__ void sweep_n_generic(double* x, const dim_dev& D, const long long es = kPitch) {
     const int n = D.n, kl = D.kl, w = D.w;
     for (int j = 0; j < n - 1; ++j) {
         const int l = __ldg(D.piv + j);
         if (l != j) {
-            const double t = x[l * kPitch];
-            x[l * kPitch] = x[j * kPitch];
-            x[j * kPitch] = t;
+            const double t = x[l * es];
+            x[l * es] = x[j * es];
+            x[j * es] = t;
         }
-        const double y = -x[j * kPitch];
+        const double y = -x[j * es];
         const int lm = min(kl, n - 1 - j);
         const double* lj = D.lmul + static_cast<long long>(j) * kl;
-        for (int i = 1; i <= lm; ++i) x[(j + i) * kPitch] = fma(y, __ldg(lj + i - 1), x[(j + i) * kPitch]);
+        for (int i = 1; i <= lm; ++i) x[(j + i) * es] = fma(y, __ldg(lj + i - 1), x[(j + i) * es]);
     }
     for (int j = n - 1; j >= 0; --j) {
-        const double v = x[j * kPitch] * __ldg(D.rdiag + j);
-        x[j * kPitch] = v;
+        const double v = x[j * es] * __ldg(D.rdiag + j);
+        x[j * es] = v;
         const int ext = __ldg(D.uext + j);
         const double* uj = D.ucol + static_cast<long long>(j) * w;
-        for (int dd = 1; dd <= ext; ++dd) x[(j - dd) * kPitch] = fma(-v, __ldg(uj + dd - 1), x[(j - dd) * kPitch]);
+        for (int dd = 1; dd <= ext; ++dd) x[(j - dd) * es] = fma(-v, __ldg(uj + dd - 1), x[(j - dd) * es]);
     }
 }
 
@@ -594,26 +595,26 @@ __device__ __forceinline__ void sweep_n_reg(double* x, const dim_dev& D) {
 
 // dgbtrs 'T': U^T-solve (dtbsv 'Upper','T'), then L^T with the row exchanges
 // undone in reverse order.
-__device__ __forceinline__ void sweep_t(double* x, const dim_dev& D) {
+__device__ __forceinline__ void sweep_t(double* x, const dim_dev& D, const long long es = kPitch) {
     const int n = D.n, kl = D.kl, w = D.w;
     for (int j = 0; j < n; ++j) {
-        double t = x[j * kPitch];
+        double t = x[j * es];
         const int ext = __ldg(D.uext + j);
         const double* uj = D.ucol + static_cast<long long>(j) * w;
-        for (int dd = ext; dd >= 1; --dd) t = fma(-__ldg(uj + dd - 1), x[(j - dd) * kPitch], t);
-        x[j * kPitch] = t * __ldg(D.rdiag + j);
+        for (int dd = ext; dd >= 1; --dd) t = fma(-__ldg(uj + dd - 1), x[(j - dd) * es], t);
+        x[j * es] = t * __ldg(D.rdiag + j);
     }
     for (int j = n - 2; j >= 0; --j) {
         const int lm = min(kl, n - 1 - j);
         const double* lj = D.lmul + static_cast<long long>(j) * kl;
         double t = 0.0;
-        for (int i = 1; i <= lm; ++i) t = fma(x[(j + i) * kPitch], __ldg(lj + i - 1), t);
-        x[j * kPitch] -= t;
+        for (int i = 1; i <= lm; ++i) t = fma(x[(j + i) * es], __ldg(lj + i - 1), t);
+        x[j * es] -= t;
         const int l = __ldg(D.piv + j);
         if (l != j) {
-            const double s = x[l * kPitch];
-            x[l * kPitch] = x[j * kPitch];
-            x[j * kPitch] = s;
+            const double s = x[l * es];
+            x[l * es] = x[j * es];
+            x[j * es] = s;
         }
     }
 }
@@ -648,6 +649,22 @@ __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ dat
 }
 
 size_t line_solve_smem_per_warp(int n) { return static_cast<size_t>(n + kPadLo + kPadHi) * kPitch * sizeof(double); }
+
+// Lines too long for a shared-memory tile (more than ~850 rows): each lane
+// sweeps its own line in place in global memory with the generic sweeps, 'N'
+// or 'T', any band.  Same operations in the same order as the staged generic
+// kernel, so the results are bitwise those of line_solve_kernel<0, 0>.
+__global__ void __launch_bounds__(128) line_solve_long_kernel(double* __restrict__ data, dim_dev D, line_layout L,
+                                                              int trans) {
+    const long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= L.nlines) return;
+    pdl_wait();
+    double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    if (trans)
+        sweep_t(x, D, L.elem_stride);
+    else
+        sweep_n_generic(x, D, L.elem_stride);
+}
 
 // ---------------------------------------------------------------------------
 // Line solve without shared memory: each lane sweeps its own line directly in
@@ -1630,6 +1647,9 @@ cudaError_t launch_line_solve(double* data, const dim_dev& d, const line_layout&
         if (kl == 3) return line_solve_variant<3, 3>(v, data, d, L, s);
         if (kl == 4) return line_solve_variant<4, 4>(v, data, d, L, s);
     }
+    if (line_solve_smem_per_warp(d.n) > 227 * 1024)
+        return launch_pdl(line_solve_long_kernel, dim3(static_cast<unsigned>((L.nlines + 127) / 128)), dim3(128), 0, s,
+                          data, d, L, trans);
     if (kl == 1 && ku <= 1 && w <= 2 && w >= 1) return line_solve_t<1, 1>(data, d, L, trans, s);
     if (kl == 1 && ku <= 2 && w <= 3 && w >= 2) return line_solve_t<1, 2>(data, d, L, trans, s);
     if (kl == 2 && ku <= 2 && w <= 4 && w >= 2) return line_solve_t<2, 2>(data, d, L, trans, s);

@@ -12,7 +12,9 @@
 //
 // Calls share the array: two calls whose work overlaps on the GPU (different
 // streams, or different host threads) race on it and must be serialised by
-// the caller.  Every element of the array that a call reads is written
+// the caller.  Calls on one stream are ordered and need nothing more: each
+// call waits, on the host, until the previous call's table upload has read
+// the host staging buffer before rewriting it.  Every element of the array that a call reads is written
 // earlier in the same call (band tables are uploaded whole, every
 // intermediate tensor is written by the pass before the one that reads it),
 // so nothing has to start at zero and no content of a previous call is used.
@@ -39,14 +41,20 @@ constexpr long long kScratchDoubles = 4 * kMaxDofs + kTableDoubles;
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 // Host staging of the band tables (static: the entry point allocates nothing).
+// The upload from it is asynchronous, and on a host whose memory the GPU
+// reads directly the copy may read the buffer after the call has returned; so
+// an event recorded after each upload is waited for before the next call
+// rewrites the buffer.
 static double g_host_tables[kTableDoubles];
 static std::mutex g_lock;
 
 constexpr int kMaxDevices = 64;
 static double* g_dev_ptr[kMaxDevices] = {};
+static cudaEvent_t g_upload_done[kMaxDevices] = {};
+static cudaEvent_t g_pending = nullptr;  // the upload that last read g_host_tables
 
 // Per-device set-up, once per device with that device current.
-int scratch_address(double** out) {
+int scratch_address(double** out, cudaEvent_t* event) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail_cuda(e, "cudaGetDevice");
@@ -55,9 +63,12 @@ int scratch_address(double** out) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return fail_cuda(e, "cudaGetSymbolAddress(scratch)");
+        e = cudaEventCreateWithFlags(&g_upload_done[dev], cudaEventDisableTiming);
+        if (e != cudaSuccess) return fail_cuda(e, "cudaEventCreate(upload)");
         g_dev_ptr[dev] = static_cast<double*>(p);
     }
     *out = g_dev_ptr[dev];
+    *event = g_upload_done[dev];
     return 0;
 }
 
@@ -110,8 +121,15 @@ extern "C" int adsg_heat_rhs_noalloc(int ndim, const adsg_dim_desc* dims, const 
 
     std::lock_guard<std::mutex> guard(g_lock);
     double* base = nullptr;
-    int st = scratch_address(&base);
+    cudaEvent_t upload_done = nullptr;
+    int st = scratch_address(&base, &upload_done);
     if (st) return st;
+    if (g_pending) {
+        // the previous call's upload must have read the staging buffer
+        const cudaError_t w = cudaEventSynchronize(g_pending);
+        if (w != cudaSuccess) return fail_cuda(w, "wait for the previous upload");
+        g_pending = nullptr;
+    }
     double* T[4] = {base, base + kMaxDofs, base + 2 * kMaxDofs, base + 3 * kMaxDofs};
     double* tables_dev = base + 4 * kMaxDofs;
 
@@ -139,6 +157,13 @@ extern "C" int adsg_heat_rhs_noalloc(int ndim, const adsg_dim_desc* dims, const 
     }
     cudaError_t e = cudaMemcpyAsync(tables_dev, g_host_tables, off * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return fail_cuda(e, "upload band tables");
+    e = cudaEventRecord(upload_done, s);
+    if (e != cudaSuccess) {
+        // without the event the buffer cannot be rewritten safely: finish the copy now
+        cudaStreamSynchronize(s);
+        return fail_cuda(e, "record the upload");
+    }
+    g_pending = upload_done;
 
     const int nx = dims[0].n;
     if (ndim == 1) {

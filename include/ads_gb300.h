@@ -221,12 +221,27 @@ int adsg_heat_rhs_host(adsg_ctx* ctx, const double* u_prev_host, double* rhs_hos
 /* Drop-in for LAPACK dgbtrs_ as the reference declares it
  * (include/ads/lin/lapack.hpp:27-39, called from lin/band_solve.hpp:26-31):
  * same arguments, by pointer, host memory, column-major B with ldb >= n.
- * Solves on the GPU (all nrhs columns in parallel) and synchronises.
- * *info = 0 on success or -k for an invalid k-th argument; the return value
- * is the same status. */
+ * Solves on the GPU (all nrhs columns in parallel) and synchronises.  Any n;
+ * kl <= 16 and kl + ku <= 32.
+ * *info = 0 on success, -k for an invalid k-th argument (as LAPACK), and
+ * positive whenever B is left unsolved for another reason: the 1-based column
+ * of an exactly zero U diagonal (dgbtrf's meaning), or n + 1 when the GPU
+ * solve could not run (band wider than the limits above, a CUDA failure;
+ * adsg_last_error() has the reason).  Every nonzero info is also reported on
+ * stderr.  The return value is 0 or the ADSG status. */
 int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs,
                  const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
                  int* info);
+
+/* adsg_dgbtrs_ for callers that never read info, such as the reference's own
+ * lin::solve_with_factorized (band_solve.hpp:26-31 ignores it): on any
+ * nonzero info it prints the reason and aborts the process, as reference
+ * LAPACK's xerbla stops on a bad argument, instead of letting the program go
+ * on with unsolved right-hand sides.  Bind the reference to this one
+ * (-Ddgbtrs_=adsg_dgbtrs_checked_).  Returns 0. */
+int adsg_dgbtrs_checked_(const char* trans, const int* n, const int* kl, const int* ku, const int* nrhs,
+                         const double* ab, const int* ldab, const int* ipiv, double* b, const int* ldb,
+                         int* info);
 
 /* ---- general pointwise forms (the other problems' compute_rhs) -------------
  * rhs_a = sum_e sum_q w_q J_e [ A u v_a + B grad u . grad v_a + G v_a + D ]
@@ -369,10 +384,13 @@ int adsg_batch_engine(const adsg_batch* b);
  * (NULL: the legacy default stream) and allocates nothing, neither device nor
  * host memory.
  *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress) with that device current and creates one event
+ *    for that device; make that first call before any stream capture.
  *  - All calls share the array: calls whose work overlaps on the GPU race and
  *    must be serialised by the caller.  Nothing carries over between calls.
+ *    Calls on one stream need no synchronisation between them: a call waits
+ *    on the host until the previous call's upload of the band tables has
+ *    read the library's host staging buffer before it rewrites it.
  *  - Tensors above ADSG_NOALLOC_MAX_DOFS dofs or dimensions above
  *    ADSG_NOALLOC_MAX_N dofs are rejected with -2 and a message. */
 #define ADSG_NOALLOC_MAX_DOFS (1 << 19)

@@ -14,9 +14,59 @@
 #include <utility>
 #include <vector>
 
+#include <atomic>
+#include <mutex>
+#include <thread>
+
 #include "ads/executor/sequential.hpp"
 #include "ads/lin/band_solve.hpp"
 #include "ads/simulation.hpp"
+
+// Galois 6.0 is not installed, so executor/galois.hpp declares nothing here
+// (its body is under ADS_USE_GALOIS).  This stand-in has the interface of
+// galois_executor (executor/galois.hpp:19-46): for_each runs the function on
+// every item of a range from a pool of threads, in no fixed order, and
+// synchronized runs a function under one lock.  Written on std::thread and
+// std::mutex; with one thread it visits the items in range order.
+namespace ads {
+class galois_executor {
+    mutable std::mutex lock_;
+    int threads_ = 1;
+
+public:
+    explicit galois_executor(int threads) { thread_count(threads); }
+    void thread_count(int threads) { threads_ = threads < 1 ? 1 : threads; }
+
+    template <typename Fun>
+    void synchronized(Fun fun) const {
+        std::lock_guard<std::mutex> guard{lock_};
+        fun();
+    }
+
+    template <typename Range, typename Fun>
+    void for_each(Range range, Fun&& fun) const {
+        using std::begin;
+        using std::end;
+        using item = typename std::decay<decltype(*begin(range))>::type;
+        std::vector<item> items;
+        for (auto it = begin(range); it != end(range); ++it) items.push_back(*it);
+        std::atomic<std::size_t> next{0};
+        const std::size_t chunk = 16;
+        auto work = [&] {
+            for (;;) {
+                std::size_t i = next.fetch_add(chunk);
+                if (i >= items.size()) return;
+                std::size_t stop = std::min(items.size(), i + chunk);
+                for (; i < stop; ++i) fun(items[i]);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 1; t < threads_; ++t) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+    }
+};
+}  // namespace ads
 
 // The reference's examples/heat/heat_3d.hpp keeps compute_rhs private; open
 // it up so the literal reference loop (eval_fun inside the dof loop) runs.
@@ -34,16 +84,20 @@ namespace {
 
 // 3D heat step in the executor form of heat_2d.hpp:166-192 /
 // scalability/test3d.hpp:223-251 (eval_fun hoisted, local element tile,
-// synchronized scatter), driven by the reference's sequential_executor.
-class heat3_driver : public ads::simulation_3d {
+// synchronized scatter), driven by the reference's sequential_executor or by
+// the galois_executor stand-in above on several threads.
+template <typename Exec>
+class heat3_driver_t : public ads::simulation_3d {
 public:
     vector_type u, u_prev;
-    ads::sequential_executor executor;
+    Exec executor;
 
-    explicit heat3_driver(const ads::config_3d& c)
+    template <typename... Args>
+    explicit heat3_driver_t(const ads::config_3d& c, Args... exec_args)
     : simulation_3d{c}
     , u{shape()}
-    , u_prev{shape()} { }
+    , u_prev{shape()}
+    , executor{exec_args...} { }
 
     void compute_rhs() {
         auto& rhs = u;
@@ -75,15 +129,18 @@ public:
     }
 };
 
-class heat2_driver : public ads::simulation_2d {
+template <typename Exec>
+class heat2_driver_t : public ads::simulation_2d {
 public:
     vector_type u, u_prev;
-    ads::sequential_executor executor;
+    Exec executor;
 
-    explicit heat2_driver(const ads::config_2d& c)
+    template <typename... Args>
+    explicit heat2_driver_t(const ads::config_2d& c, Args... exec_args)
     : simulation_2d{c}
     , u{shape()}
-    , u_prev{shape()} { }
+    , u_prev{shape()}
+    , executor{exec_args...} { }
 
     void compute_rhs() {
         auto& rhs = u;
@@ -118,6 +175,9 @@ public:
         solve(u);
     }
 };
+
+using heat3_driver = heat3_driver_t<ads::sequential_executor>;
+using heat2_driver = heat2_driver_t<ads::sequential_executor>;
 
 // scalability_3d::compute_rhs (examples/scalability/test3d.hpp:66-95) and
 // flow::compute_rhs (examples/flow/flow.hpp:77-98), loop for loop, on the
@@ -314,6 +374,30 @@ int ref_heat_steps(int ndim, int p, int elements, double dt, int nsteps, double*
         }
     } else if (ndim == 2) {
         heat2_driver s{ads::config_2d{dim, dim, steps, 1}};
+        s.prepare();
+        load(s.u, u);
+        for (int i = 0; i < nsteps; ++i) s.step();
+        store(s.u, u);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+// nsteps explicit heat steps from u (in/out) in the executor form, with the
+// element loop on nthreads threads of the galois_executor stand-in (the
+// scatter order, and so the rounding, varies from run to run as under Galois).
+int ref_heat_steps_mt(int ndim, int p, int elements, double dt, int nsteps, double* u, int nthreads) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{nsteps, dt};
+    if (ndim == 3) {
+        heat3_driver_t<ads::galois_executor> s{ads::config_3d{dim, dim, dim, steps, 1}, nthreads};
+        s.prepare();
+        load(s.u, u);
+        for (int i = 0; i < nsteps; ++i) s.step();
+        store(s.u, u);
+    } else if (ndim == 2) {
+        heat2_driver_t<ads::galois_executor> s{ads::config_2d{dim, dim, steps, 1}, nthreads};
         s.prepare();
         load(s.u, u);
         for (int i = 0; i < nsteps; ++i) s.step();

@@ -1,19 +1,27 @@
-"""Parity tolerances.
+"""Parity tolerances and how they are reported.
 
-The contract is relative L2 <= 1e-12 per step and <= 1e-10 after a full run.
-Those bounds are attainable as stated when the Kronecker mass matrix is well
-conditioned (p <= 2: cond(M_1D) ~ 10).  A step solves M u = rhs, so any two
-correct implementations whose RHS differ by rounding (~1e-15 relative, e.g.
-the reference's literal heat_3d loop vs its executor form) differ after the
-solve by up to cond(M_x (x) M_y (x) M_z) times that.  For p = 3, 4 the product of
-the 1D condition numbers reaches 2e4 .. 3.3e5, and the reference disagrees
-with itself at the 1e-12 .. 1e-11 level.  The bounds are therefore scaled by
-prod(cond_d) / 1e3 when that exceeds one (never loosened for p <= 2 in 2D,
-and by at most ~1.2 for p = 2 in 3D).
+The contract is relative L2 <= 1e-12 per step and <= 1e-10 after a full run,
+against the reference's own CPU step.  Where the reference disagrees with
+itself by more than that -- its literal heat_3d loop against its executor
+form, and its executor on several threads (the scatter order changes the
+rounding) against the sequential one, measured per case and stored in the
+golden fixtures -- the bound is twice that measured self-disagreement
+instead: two correct implementations cannot be asked to agree more closely
+than the reference agrees with itself.  That happens at p = 3, 4, where the
+Kronecker mass matrix amplifies rounding of the right-hand side by up to
+its condition number (2e4 .. 3.3e5).
+
+Every check prints the measured error next to its bound (pytest -s, or -rA
+for passing tests' output), so the distance to 1e-12 is visible, not only
+pass/fail.
 """
 from __future__ import annotations
 
 import numpy as np
+
+STEP = 1e-12   # per step
+RUN = 1e-10    # after a full run
+RHS = 1e-13    # the right-hand side before the solve
 
 
 def mass_condition(mass_ab: np.ndarray, p: int) -> float:
@@ -28,13 +36,26 @@ def mass_condition(mass_ab: np.ndarray, p: int) -> float:
     return float(np.linalg.cond(M))
 
 
-def scale(conds) -> float:
-    return max(1.0, float(np.prod(conds)) / 1e3)
+def bound(contract: float, self_disagreement: float = 0.0, factor: float = 2.0) -> float:
+    return max(contract, factor * float(self_disagreement))
 
 
-def step_tol(conds) -> float:
-    return 1e-12 * scale(conds)
+def check(label: str, err: float, contract: float, self_disagreement: float = 0.0, factor: float = 2.0) -> None:
+    """Assert err <= max(contract, factor x the reference's self-disagreement)
+    and print both."""
+    b = bound(contract, self_disagreement, factor)
+    print(f"[parity] {label}: rel L2 {err:.3e}  bound {b:.2e}  (contract {contract:.0e}, "
+          f"reference self-disagreement {float(self_disagreement):.2e})")
+    assert np.isfinite(err) and err <= b, f"{label}: rel L2 {err:.3e} above {b:.2e}"
 
 
-def run_tol(conds) -> float:
-    return 1e-10 * scale(conds)
+def oracle_self(pr, u, dt, nsteps, threads=(2, 3, 5)) -> float:
+    """The oracle's disagreement with itself over nsteps steps from u: its
+    sequential element loop against its executor form (element tiles and a
+    locked scatter, the galois_executor pattern) on several threads -- the
+    same pair of correct forms whose difference the fixtures record for the
+    reference itself.  The largest relative L2 difference."""
+    import oracle
+
+    ref = pr.heat_steps(u, dt, nsteps)
+    return max(oracle.rel_l2(pr.heat_steps(u, dt, nsteps, nthreads=t), ref) for t in threads)

@@ -2,7 +2,8 @@
 
 Run in a container where the reference sources are present:
     make -C oracle ref           # builds oracle/_ref/libadsref.so from them
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # the small cases
+    python tests/golden/make_golden.py --runs   # the full-size runs (hours)
 
 Every output array below is produced by the reference implementation
 (oracle/_ref: the reference's src/ads/*.cpp and headers compiled as they lie,
@@ -175,6 +176,44 @@ def known_answers(L):
     return out
 
 
+def rel_l2(a, b):
+    s = max(np.abs(a).max(), np.abs(b).max())
+    return float(np.linalg.norm((a - b) / s) / max(np.linalg.norm(a / s), 1e-300)) if s else 0.0
+
+
+def self_disagreement(L, nd, p, E, dt, nsteps, u0, mode, u1, uN, trials=6):
+    """How far the reference's own correct forms of the same step fall from
+    the fixture's: the literal heat_3d loop against the executor form (3D)
+    and the executor on several threads (galois_executor stand-in: the
+    scatter order, and so the rounding, changes from run to run) against the
+    sequential one; the largest relative L2 difference over all of them,
+    after 1 and after nsteps steps.  Also the solve's sensitivity to its
+    input's last bit: the reference's ads_solve of u0 with every entry moved
+    by up to one ulp, against that of u0."""
+    L.ref_heat_steps_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp,
+                                    ctypes.c_int]
+    d1 = dN = 0.0
+    forms = [("mt", t) for t in range(trials)]
+    if nd == 3:
+        forms.append(("literal" if mode == 0 else "executor", 0))
+    for form, t in forms:
+        a, b = u0.copy(), u0.copy()
+        if form == "mt":
+            L.ref_heat_steps_mt(nd, p, E, dt, 1, dp(a), 2 + t)
+            L.ref_heat_steps_mt(nd, p, E, dt, nsteps, dp(b), 2 + t)
+        else:
+            other = 1 if form == "literal" else 0
+            L.ref_heat_steps(nd, p, E, dt, 1, dp(a), other)
+            L.ref_heat_steps(nd, p, E, dt, nsteps, dp(b), other)
+        d1, dN = max(d1, rel_l2(a, u1)), max(dN, rel_l2(b, uN))
+    rng = np.random.default_rng(1234)
+    x = u0 * (1.0 + rng.uniform(-1, 1, u0.size) * 2.0 ** -53)
+    y = u0.copy()
+    L.ref_ads_solve(nd, p, E, dp(x))
+    L.ref_ads_solve(nd, p, E, dp(y))
+    return dict(self_u1=np.float64(d1), self_uN=np.float64(dN), solve_ulp_sensitivity=np.float64(rel_l2(x, y)))
+
+
 def heat_case(L, nd, p, E, dt, nsteps, seed, mode=0):
     n = E + p
     size = n ** nd
@@ -191,8 +230,10 @@ def heat_case(L, nd, p, E, dt, nsteps, seed, mode=0):
     L.ref_heat_steps(nd, p, E, dt, 1, dp(u1), mode)
     uN = u0.copy()
     L.ref_heat_steps(nd, p, E, dt, nsteps, dp(uN), mode)
-    return dict(ndim=np.int32(nd), p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps),
-                seed=np.int64(seed), mode=np.int32(mode), projection=proj, u0=u0, rhs=rhs, solve=sol, u1=u1, uN=uN)
+    out = dict(ndim=np.int32(nd), p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps),
+               seed=np.int64(seed), mode=np.int32(mode), projection=proj, u0=u0, rhs=rhs, solve=sol, u1=u1, uN=uN)
+    out.update(self_disagreement(L, nd, p, E, dt, nsteps, u0, mode, u1, uN))
+    return out
 
 
 CASES = [
@@ -232,7 +273,88 @@ FORM_CASES = [
 ]
 
 
+# Full-size runs of the 3D configurations: 130^3 dofs p=2 for 50 steps at
+# dt=1e-6, and 260^3 dofs p=4 for 20 steps at dt=1e-6 (unstable at that dt:
+# its top modes grow ~16.6x per step).  The reference runs them with its
+# element loop on the galois_executor stand-in (all host threads); the fixture
+# keeps whole planes of the state after the first and the last step plus
+# global statistics, since the full fields (17.6 / 140.6 MB) do not belong in
+# the repository.  The initial field is ads_gb300.inputs.initial_field (the
+# sin projection plus SplitMix64 noise, seed 0), which the GPU test recreates.
+RUNS = [
+    # (name, p, elements, dt, nsteps, seed)
+    ("run_3d_p2_e128", 2, 128, 1e-6, 50, 0),
+    ("run_3d_p4_e256", 4, 256, 1e-6, 20, 0),
+]
+
+
+def mass_apply(u, shape, bands):
+    """(Mz (x) My (x) Mx) u for an x-fastest tensor, from LAPACK-layout bands."""
+    v = u.reshape(shape[::-1])
+    for axis, (ab, p) in zip((2, 1, 0), bands):
+        n = shape[2 - axis]
+        ldab = 3 * p + 1
+        M = np.zeros((n, n))
+        for j in range(n):
+            for i in range(max(0, j - p), min(n, j + p + 1)):
+                M[i, j] = ab[j * ldab + 2 * p + i - j]
+        v = np.moveaxis(np.tensordot(M, np.moveaxis(v, axis, 0), axes=(1, 0)), 0, axis)
+    return v.ravel()
+
+
+def snapshot(u, n, mass_ab, p, prefix, planes):
+    """Planes of an x-fastest n^3 field plus global statistics."""
+    s = np.abs(u).max()
+    out = {prefix + "max": np.float64(s), prefix + "norm": np.float64(np.linalg.norm(u / s) * s)}
+    Mu = mass_apply(u / s, (n, n, n), [(mass_ab, p)] * 3)
+    out[prefix + "mass_norm"] = np.float64(np.sqrt(np.dot(u / s, Mu)) * s)
+    t = u.reshape(n, n, n)  # [k][j][i]
+    if "z" in planes:
+        out[prefix + "plane_z"] = np.ascontiguousarray(t[n // 2])
+    if "y" in planes:
+        out[prefix + "plane_y"] = np.ascontiguousarray(t[:, n // 3, :])
+    return out
+
+
+def run_case(L, name, p, E, dt, nsteps, seed, nthreads):
+    import time
+
+    sys.path.insert(0, os.path.join(ROOT, "iga-ads_gb300"))
+    import ads_gb300 as ads
+    from ads_gb300 import inputs
+
+    L.ref_heat_steps_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp,
+                                    ctypes.c_int]
+    dims = [ads.Dimension(p, E) for _ in range(3)]
+    u = inputs.initial_field(dims, seed=seed)
+    n = E + p
+    mass = tables(L, p, E)["mass"]
+    out = dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps), seed=np.int64(seed),
+               threads=np.int32(nthreads), plane_z_index=np.int32(n // 2), plane_y_index=np.int32(n // 3))
+    out["u0_norm"] = np.float64(np.linalg.norm(u))
+    out["u0_sum"] = np.float64(u.sum())
+    t0 = time.time()
+    assert L.ref_heat_steps_mt(3, p, E, dt, 1, dp(u), nthreads) == 0
+    out.update(snapshot(u, n, mass, p, "u1_", "z"))
+    print(f"{name}: step 1 done in {time.time() - t0:.0f} s", flush=True)
+    assert L.ref_heat_steps_mt(3, p, E, dt, nsteps - 1, dp(u), nthreads) == 0
+    out.update(snapshot(u, n, mass, p, "uN_", "zy"))
+    out["seconds"] = np.float64(time.time() - t0)
+    print(f"{name}: {nsteps} steps done in {time.time() - t0:.0f} s", flush=True)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, flush=True)
+
+
+def main_runs(names, nthreads):
+    L = load_ref()
+    for name, p, E, dt, nsteps, seed in RUNS:
+        if not names or name in names:
+            run_case(L, name, p, E, dt, nsteps, seed, nthreads)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--runs":
+        return main_runs(sys.argv[2:], os.cpu_count() or 1)
     L = load_ref()
     for name, which, p, E, dt, seed in FORM_CASES:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **form_case(L, which, p, E, dt, seed))

@@ -8,6 +8,7 @@ import glob
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -76,6 +77,45 @@ def test_dgbtrs_argument_errors_match_lapack(kw, code):
 def test_dgbtrs_empty_problem_is_a_no_op():
     assert _dgbtrs(n=0, ldb=1) == (0, 0)
     assert _dgbtrs(nrhs=0) == (0, 0)
+
+
+def test_dgbtrs_unsolved_cases_report_positive_info_without_gpu():
+    """A caller that reads only info sees every case where b is left
+    unsolved: a band beyond the supported width (info = n + 1) and an exactly
+    zero U diagonal (info = its 1-based column).  Both are decided before any
+    device call."""
+    n, kl, ku = 40, 17, 17
+    ldab = 2 * kl + ku + 1
+    ab = np.ones(ldab * n)
+    b = np.arange(float(n))
+    code, info = _dgbtrs(n=n, kl=kl, ku=ku, nrhs=1, ldab=ldab, ldb=n, ab=ab, b=b)
+    assert code == 1005 and info == n + 1
+    np.testing.assert_array_equal(b, np.arange(float(n)))
+    n, kl, ku = 6, 1, 1
+    ldab = 4
+    ab = np.ones(ldab * n)
+    ab[3 * ldab + kl + ku] = 0.0  # U(4, 4) = 0
+    code, info = _dgbtrs(n=n, kl=kl, ku=ku, nrhs=1, ldab=ldab, ldb=n, ab=ab, b=np.ones(n))
+    assert code == 1003 and info == 4
+
+
+def test_dgbtrs_checked_aborts_where_info_would_be_ignored():
+    """The entry for callers that never read info (the reference's own
+    band_solve.hpp) stops the process with the reason instead of returning
+    an unsolved b.  Run in a child process; the failing case is rejected on
+    the host, before any device call."""
+    code = (
+        "import ctypes, numpy as np, sys; sys.path.insert(0, %r); import ads_gb300 as a\n"
+        "lib = a.library(); n, kl, ku = 40, 17, 17; ldab = 2*kl+ku+1\n"
+        "ab = np.ones(ldab*n); b = np.zeros(n); piv = np.arange(1, n+1, dtype=np.int32)\n"
+        "I = [ctypes.c_int(v) for v in (n, kl, ku, 1, ldab, n)]; info = ctypes.c_int(0)\n"
+        "dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)\n"
+        "lib.adsg_dgbtrs_checked_(b'N', *[ctypes.byref(I[k]) for k in range(4)], ab.ctypes.data_as(dp),\n"
+        "    ctypes.byref(I[4]), piv.ctypes.data_as(ip), b.ctypes.data_as(dp), ctypes.byref(I[5]), ctypes.byref(info))\n"
+        "print('returned')\n" % os.path.join(ROOT, "iga-ads_gb300"))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "returned" not in r.stdout
+    assert "aborting" in r.stderr and "band wider" in r.stderr
 
 
 def test_ctx_create_rejects_bad_arguments_without_gpu():

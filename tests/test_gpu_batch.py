@@ -7,16 +7,12 @@ import pytest
 
 import ads_gb300 as ads
 import oracle
-from _tol import mass_condition, step_tol
+from _tol import STEP, check, oracle_self
 
 pytestmark = pytest.mark.gpu
 
 SMALL = [(2, 2, 17, 1e-5), (3, 4, 7, 1e-6), (2, 4, 40, 2e-6), (3, 2, 12, 1e-6), (3, 3, 9, 1e-6), (2, 3, 5, 1e-4),
          (3, 1, 6, 1e-5), (2, 1, 33, 1e-5)]
-
-
-def _cond(p, e):
-    return mass_condition(ads.Dimension(p, e).form_band(0).ravel(), p)
 
 
 def test_batch_against_oracle_and_loop(cuda):
@@ -28,9 +24,11 @@ def test_batch_against_oracle_and_loop(cuda):
     b.steps(3)
     b.synchronize()
     got = [b.get_state(i) for i in range(len(SMALL))]
+    selfd = []
     for i, (nd, p, e, dt) in enumerate(SMALL):
-        ref = oracle.Problem([p] * nd, [e] * nd).heat_steps(u0[i], dt, 3)
-        assert oracle.rel_l2(got[i], ref) <= 3 * step_tol([_cond(p, e)] * nd), (i, SMALL[i])
+        pr = oracle.Problem([p] * nd, [e] * nd)
+        selfd.append(oracle_self(pr, u0[i], dt, 3))
+        check(f"batch {SMALL[i]} 3 steps", oracle.rel_l2(got[i], pr.heat_steps(u0[i], dt, 3)), 3 * STEP, selfd[i])
     # the same three steps through the plain per-instance kernels (their
     # autotuned solves may use the two-ended sweep, which rounds differently
     # from the batched kernel's LAPACK-order sweep)
@@ -39,7 +37,7 @@ def test_batch_against_oracle_and_loop(cuda):
     b.steps_looped(3)
     b.synchronize()
     for i, (nd, p, e, dt) in enumerate(SMALL):
-        assert oracle.rel_l2(b.get_state(i), got[i]) <= 3 * step_tol([_cond(p, e)] * nd), (i, SMALL[i])
+        check(f"batch vs looped {SMALL[i]}", oracle.rel_l2(b.get_state(i), got[i]), 3 * STEP, selfd[i])
 
 
 @pytest.mark.parametrize("engine", ["0", "1"])
@@ -56,8 +54,9 @@ def test_batch_repeated_calls_and_parity(engine, cuda, monkeypatch):
         b.steps(n)
     b.synchronize()
     for i, (nd, p, e, dt) in enumerate(SMALL[:4]):
-        ref = oracle.Problem([p] * nd, [e] * nd).heat_steps(u0[i], dt, 7)
-        assert oracle.rel_l2(b.get_state(i), ref) <= 7 * step_tol([_cond(p, e)] * nd)
+        pr = oracle.Problem([p] * nd, [e] * nd)
+        check(f"batch engine {engine} {SMALL[i]} 7 steps", oracle.rel_l2(b.get_state(i), pr.heat_steps(u0[i], dt, 7)),
+              7 * STEP, oracle_self(pr, u0[i], dt, 7))
     t = b.tuning()
     assert t["blocks_per_sm"] >= 1
     assert t["engine"] == ("concurrent" if engine == "1" else "persistent")
@@ -79,9 +78,13 @@ def test_mixed_64_batch_matches_plain_kernels(cuda):
     b.steps_looped(2)
     b.synchronize()
     # the per-instance contexts may solve with the two-ended sweep, which
-    # rounds differently from the batched kernel's LAPACK-order sweep
+    # rounds differently from the batched kernel's LAPACK-order sweep; the
+    # bound is the oracle's own spread at that instance's shape
     for i, (nd, p, e, dt) in enumerate(specs):
-        assert oracle.rel_l2(b.get_state(i), got[i]) <= 2 * step_tol([_cond(p, e)] * nd), specs[i]
+        err = oracle.rel_l2(b.get_state(i), got[i])
+        if err > 2 * STEP:
+            pr = oracle.Problem([p] * nd, [e] * nd)
+            check(f"mixed-64 batch vs looped {specs[i]}", err, 2 * STEP, oracle_self(pr, u0[i], dt, 2))
 
 
 def test_batch_rejects_bad_specs():

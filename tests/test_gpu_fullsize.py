@@ -1,0 +1,147 @@
+"""Parity at the full sizes of the 3D heat configurations and of the mixed
+64-instance batch, through the C-ABI:
+
+- 130^3 dofs, p = 2, dt = 1e-6, 50 steps: the whole run against the
+  reference's own run of the same steps (planes and global statistics kept in
+  tests/golden/run_3d_p2_e128.npz, made by tests/golden/make_golden.py from the
+  reference sources) and the whole field against the multi-threaded oracle;
+- 260^3 dofs, p = 4, dt = 1e-6, 20 steps (unstable at this dt: the top modes
+  grow ~16.6x per step, so errors are relative L2 after scaling by the
+  largest entry): one whole step against the multi-threaded oracle, and the
+  first and last steps against the reference's own run;
+- the seeded mixed 64-instance batch (sides up to 512^2 and 96^3, p in
+  {2, 3, 4}), two steps under both batch engines, instance by instance against
+  the oracle.
+
+Bounds: the contract (1e-12 per step, 1e-10 per run), or twice the measured
+disagreement between two CPU forms of the reference's algorithm on the same
+input where that is larger (the reference's run against the oracle's, or the
+oracle's executor on two thread counts).  Each check prints both numbers."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+import ads_gb300 as ads
+import oracle
+from _tol import RUN, STEP, check
+from ads_gb300 import inputs
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+THREADS = max(1, min(64, os.cpu_count() or 1))
+
+
+def _fixture(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.fail(f"{name}.npz missing: made by tests/golden/make_golden.py --runs")
+    return np.load(path)
+
+
+def _mass_norm(ctx, u):
+    """sqrt(u^T (Mx (x) My (x) Mz) u) with the engine's own operator (the heat
+    right-hand side at dt = 0), scaled by max |u| against overflow."""
+    import torch
+
+    s = float(np.abs(u).max())
+    d = torch.from_numpy(u / s).cuda()
+    Mu = torch.empty_like(d)
+    ctx.heat_rhs(d, Mu, 0.0)
+    ctx.synchronize()
+    return float(torch.sqrt(torch.dot(d, Mu))) * s
+
+
+def _vs_run(u, g, prefix, n, ctx):
+    """Largest relative difference of u from the reference run's record:
+    whole planes (rel L2) and the global L2 and mass norms."""
+    t = u.reshape(n, n, n)
+    errs = [oracle.rel_l2(t[int(g["plane_z_index"])], g[prefix + "plane_z"])]
+    if prefix + "plane_y" in g.files:
+        errs.append(oracle.rel_l2(t[:, int(g["plane_y_index"]), :], g[prefix + "plane_y"]))
+    s = float(np.abs(u).max())
+    errs.append(abs(np.linalg.norm(u / s) * s - float(g[prefix + "norm"])) / float(g[prefix + "norm"]))
+    if ctx is not None:
+        errs.append(abs(_mass_norm(ctx, u) - float(g[prefix + "mass_norm"])) / float(g[prefix + "mass_norm"]))
+    return max(errs)
+
+
+def _initial(dims, g):
+    u0 = inputs.initial_field(dims, seed=int(g["seed"]))
+    # the field is recomputed here; it must be the one the reference started from
+    assert abs(np.linalg.norm(u0) - float(g["u0_norm"])) <= 1e-14 * float(g["u0_norm"])
+    assert abs(u0.sum() - float(g["u0_sum"])) <= 1e-12 * np.abs(u0).sum()
+    return u0
+
+
+def test_heat_130cubed_p2_full_run(cuda):
+    """The 3D p=2 configuration (128^3 elements, dt = 1e-6, 50 steps)."""
+    g = _fixture("run_3d_p2_e128")
+    p, E, dt, N = int(g["p"]), int(g["elements"]), float(g["dt"]), int(g["nsteps"])
+    n = E + p
+    dims = [ads.Dimension(p, E) for _ in range(3)]
+    ctx = ads.Context(dims)
+    u0 = _initial(dims, g)
+    u1 = u0.copy()
+    ctx.heat_steps_host(u1, dt, 1)
+    uN = u0.copy()
+    ctx.heat_steps_host(uN, dt, N)
+    check("130^3 p=2 1 step vs reference run", _vs_run(u1, g, "u1_", n, ctx), STEP)
+    check(f"130^3 p=2 {N} steps vs reference run", _vs_run(uN, g, "uN_", n, ctx), RUN)
+    pr = oracle.Problem([p] * 3, [E] * 3)
+    ref = pr.heat_steps(u0, dt, N, nthreads=THREADS)
+    d_cpu = _vs_run(ref, g, "uN_", n, None)  # oracle against the reference: two CPU forms
+    check(f"130^3 p=2 {N} steps vs oracle (whole field)", oracle.rel_l2(uN, ref), RUN, d_cpu)
+
+
+def test_heat_260cubed_p4_run(cuda):
+    """The 3D p=4 configuration (256^3 elements, dt = 1e-6, 20 steps)."""
+    g = _fixture("run_3d_p4_e256")
+    p, E, dt, N = int(g["p"]), int(g["elements"]), float(g["dt"]), int(g["nsteps"])
+    n = E + p
+    dims = [ads.Dimension(p, E) for _ in range(3)]
+    ctx = ads.Context(dims)
+    u0 = _initial(dims, g)
+    u1 = u0.copy()
+    ctx.heat_steps_host(u1, dt, 1)
+    uN = u0.copy()
+    ctx.heat_steps_host(uN, dt, N)
+    pr = oracle.Problem([p] * 3, [E] * 3)
+    ref1 = pr.heat_steps(u0, dt, 1, nthreads=THREADS)
+    d_cpu1 = _vs_run(ref1, g, "u1_", n, None)  # oracle against the reference after one step
+    check("260^3 p=4 1 step vs oracle (whole field)", oracle.rel_l2(u1, ref1), STEP, d_cpu1)
+    check("260^3 p=4 1 step vs reference run", _vs_run(u1, g, "u1_", n, ctx), STEP, d_cpu1)
+    check(f"260^3 p=4 {N} steps vs reference run", _vs_run(uN, g, "uN_", n, ctx), RUN, float(g["self_uN"])
+          if "self_uN" in g.files else 0.0)
+
+
+@pytest.mark.parametrize("engine", ["0", "1"])
+def test_mixed_64_batch_against_oracle(engine, cuda, monkeypatch):
+    """Both batch engines (persistent kernel, concurrent per-instance graph) on
+    the seeded 64-instance set, two steps, every instance against the
+    oracle.  The bound of a p >= 3 instance also admits twice the oracle's
+    own spread (its executor on two thread counts) at that instance."""
+    monkeypatch.setenv("ADSG_BATCH_ENGINE", engine)
+    specs = ads.batch_specs(seed=0)
+    b = ads.Batch(specs)
+    assert b.tuning()["engine"] == ("concurrent" if engine == "1" else "persistent")
+    u0 = []
+    for i, (nd, p, e, dt) in enumerate(specs):
+        u0.append(inputs.initial_field([ads.Dimension(p, e) for _ in range(nd)], seed=1000 + i))
+        b.set_state(i, u0[i])
+    b.steps(2)
+    b.synchronize()
+    worst = 0.0
+    for i, (nd, p, e, dt) in enumerate(specs):
+        pr = oracle.Problem([p] * nd, [e] * nd)
+        ref = pr.heat_steps(u0[i], dt, 2, nthreads=THREADS)
+        err = oracle.rel_l2(b.get_state(i), ref)
+        spread = 0.0
+        if err > 2 * STEP:
+            spread = oracle.rel_l2(pr.heat_steps(u0[i], dt, 2, nthreads=max(2, THREADS - 3)), ref)
+        check(f"engine {engine} instance {i} {nd}D p={p} {e} elements 2 steps", err, 2 * STEP, spread)
+        worst = max(worst, err)
+    print(f"[parity] engine {engine}: worst instance rel L2 {worst:.3e}")
