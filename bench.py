@@ -7,16 +7,22 @@ FP64).  Workload (default): the 3D heat problem with quadratic B-splines on
 is one explicit time step of the whole grid.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload heat3d_p2_128|heat2d_p2_32|heat3d_p4_256]
+                  [--workload heat3d_p2_128|heat2d_p2_32|heat3d_p4_256|batch64|adjoint_p2_96]
 
 Our arm: inputs resident in HBM, every timed step preceded by an L2 flush
-(a 512 MiB memset, outside the step's CUDA-event interval), the steps issued
-through the C-ABI's device entry points (adsg_heat_rhs + adsg_ads_solve) on
-one stream; `e2e` times the reference-facing host entry point
-(adsg_heat_steps_host: pinned host tensor in, one step, host tensor out).
+(a 512 MiB memset, outside the step's CUDA-event interval), each step one
+adsg_heat_step call (heat_3d::step: the three band passes of the RHS and the
+three line solves, 6 kernels, replayed from a cached single-step CUDA graph
+where the context's tuner found that faster) on one stream; `e2e` times the
+reference-facing host entry point (adsg_heat_steps_host: pinned host tensor
+in, one step, host tensor out).  `parity` holds the relative L2 error of the
+first step from the bench's initial field against the CPU oracle (whole
+field) and against the reference's own run of that step (planes and norms
+recorded in tests/golden/, where a record exists for the workload).
 The reference arm (--impl reference) times the CPU oracle (a C restatement
 of the reference's heat step: Galois-style element loop on all host threads,
-single-threaded ADS solve) on the same workload.
+single-threaded ADS solve) on the same workload, initial field, step count
+and warm-up.
 Multi-GPU: replicas only (the single-grid step does not shard); each rank
 runs its own copy and value is the sum over ranks.
 """
@@ -43,13 +49,17 @@ WORKLOADS = {
     "adjoint_p2_96": (3, 2, 96, 1e-6),  # kappa field, 200 steps, sqrt(N) checkpoints
 }
 METRIC = "DOF-updates/s per explicit step (RHS+ADS solve, FP64, <=1e-12 rel L2)"
+DATA = "synthetic: L2 projection of prod sin(pi x_d) + seeded SplitMix64 noise in [-1e-2, 1e-2]"
+# The reference's own record of the first and last steps of a workload
+# (tests/golden/make_golden.py --runs): planes of the state and its norms.
+RUN_RECORDS = {"heat3d_p2_128": "run_3d_p2_e128", "heat3d_p4_256": "run_3d_p4_e256"}
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="heat3d_p2_128", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -188,36 +198,56 @@ def cpu_baseline(cfg, seconds_budget=20.0):
                       f"locked scatter), ADS solve single-threaded", "s_per_step": per}
 
 
+class _OracleDim:
+    """One dimension of an oracle problem in the shape ads_gb300.inputs reads
+    (its tables are the oracle's, bit-identical to the reference's)."""
+
+    def __init__(self, pr, d):
+        self.p, self.elements = pr.p[d], pr.elements[d]
+        self.quad_order = self.p + 1
+        self._t = pr.dim(d)
+
+    def dofs(self):
+        return self.elements + self.p
+
+    def tables(self):
+        return self._t
+
+    def form_band(self, which):
+        assert which == 0
+        return self._t["mass"].reshape(self.dofs(), 3 * self.p + 1)
+
+
 def run_reference(args, cfg):
+    """The reference arm: the CPU oracle's heat step on all host threads, on
+    the same grid, initial field, warm-up and step count as our arm."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    budget = 60.0
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
     import oracle
+    from ads_gb300 import inputs  # host-side numpy only (the engine library is not loaded)
 
     nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
     threads = os.cpu_count() or 1
     pr = oracle.Problem([p] * nd, [E] * nd)
-    u = np.random.default_rng(0).uniform(-1, 1, pr.size)
-    # warm-up steps (bounded), then timed steps (bounded so the run stays within minutes)
-    t_start = time.perf_counter()
-    for _ in range(min(args.warmup, 3)):
-        u = pr.heat_steps(u, dt, 1, nthreads=threads)
-    per_warm = (time.perf_counter() - t_start) / max(1, min(args.warmup, 3))
-    k = max(1, min(args.steps, int(budget // max(per_warm, 1e-9))))
+    u = inputs.initial_field([_OracleDim(pr, d) for d in range(nd)], seed=0)
     t0 = time.perf_counter()
-    u = pr.heat_steps(u, dt, k, nthreads=threads)
+    if args.warmup:
+        u = pr.heat_steps(u, dt, args.warmup, nthreads=threads)
+    warm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u = pr.heat_steps(u, dt, args.steps, nthreads=threads)
     el = time.perf_counter() - t0
-    v = cfg["dofs"] * k / el
-    line = {"metric": METRIC, "value": v, "unit": "DOF-updates/s", "n_gpus": args.gpus, "steps": k,
-            "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * el / k, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform field)",
-            "config": {k2: v2 for k2, v2 in cfg.items()}, "impl": "reference",
+    v = cfg["dofs"] * args.steps / el
+    line = {"metric": METRIC, "value": v, "unit": "DOF-updates/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": dict(cfg), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
-                             "sample": f"{k} full steps of the benchmark grid (requested {args.steps}); the CPU "
-                                       f"oracle restating the reference step, RHS on {threads} threads"},
+                             "sample": f"{args.steps} full steps of the benchmark grid after {args.warmup} warm-up "
+                                       f"steps ({warm:.1f} s); the CPU oracle restating the reference step, RHS "
+                                       f"on {threads} threads, ADS solve single-threaded"},
             "e2e": {"value": v, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -254,23 +284,56 @@ def measured_peaks():
         return {}
 
 
+# DRAM bytes per dof of each step kernel, from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch over the workload's dofs); the captures,
+# their commands and the kernels are listed in profiles/traffic_per_dof.md.
+# A workload without its own figures takes those of the larger-than-L2
+# heat3d_p4_256 workload, where every stage streams whole tensors and the
+# traffic grows with the dofs.
+NCU_TRAFFIC_PER_DOF = {
+    "heat3d_p2_128": {"rhs_outer": 8.1, "rhs_middle": 16.8, "rhs_x": 16.0, "solve_x": 8.0, "solve_y": 8.0,
+                      "solve_z": 8.0},
+    "heat3d_p4_256": {"rhs_outer": 21.2, "rhs_middle": 29.8, "rhs_x": 22.3, "solve_x": 12.4, "solve_y": 17.2,
+                      "solve_z": 17.1},
+}
+
+
 def profiled_traffic(stage, dofs, workload):
-    """DRAM bytes per launch of a stage: the bytes per dof measured by ncu
-    (dram__bytes_read.sum + dram__bytes_write.sum, committed in
-    profiles/traffic_per_dof.md) for this workload -- or, for a workload
-    without its own row, the row of the larger-than-L2 p=4 workload -- times
-    this workload's dofs; None when neither exists."""
-    path = os.path.join(ROOT, "profiles", "traffic_per_dof.md")
-    rows = {}
-    try:
-        for ln in open(path):
-            cells = [c.strip() for c in ln.split("|")]
-            if len(cells) > 4 and cells[1] == stage:
-                rows[cells[2]] = float(cells[4])
-    except (OSError, ValueError):
-        return None
-    per_dof = rows.get(workload, rows.get("heat3d_p4_256"))
+    """DRAM bytes of one launch of a stage from the ncu figures above; None
+    when the stage has none."""
+    per_dof = NCU_TRAFFIC_PER_DOF.get(workload, NCU_TRAFFIC_PER_DOF["heat3d_p4_256"]).get(stage)
     return None if per_dof is None else per_dof * dofs
+
+
+def step_parity(ctx, u0, cfg, workload, threads):
+    """Relative L2 error of one step from u0 (the bench's initial field)
+    against the CPU oracle's step (whole field; skipped where one oracle step
+    would take minutes) and against the reference's own run of that step
+    (planes and norms of its record), scaled by the largest entry."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
+    got = u0.copy()
+    ctx.heat_steps_host(got, dt, 1)
+    out = {"steps": 1, "tol": 1e-12, "initial_field": "the bench's (seed 0)"}
+    if (p + 1) ** (2 * nd) * E ** nd <= 4e9:  # element-loop work of one oracle step
+        t0 = time.perf_counter()
+        ref = oracle.Problem([p] * nd, [E] * nd).heat_steps(u0, dt, 1, nthreads=threads)
+        out["rel_l2_vs_oracle"] = oracle.rel_l2(got, ref)
+        out["oracle_s"] = time.perf_counter() - t0
+    rec = RUN_RECORDS.get(workload)
+    path = os.path.join(ROOT, "tests", "golden", f"{rec}.npz") if rec else None
+    if path and os.path.exists(path):
+        g = np.load(path)
+        n = E + p
+        if abs(np.linalg.norm(u0) - float(g["u0_norm"])) <= 1e-14 * float(g["u0_norm"]):
+            t = got.reshape(n, n, n)
+            out["rel_l2_vs_reference_plane"] = oracle.rel_l2(t[int(g["plane_z_index"])], g["u1_plane_z"])
+            out["reference_record"] = f"tests/golden/{rec}.npz (z-plane {int(g['plane_z_index'])})"
+    return out
 
 
 def run_ours(args, cfg):
@@ -394,7 +457,8 @@ def run_ours(args, cfg):
             fl, by = work[name]
             avg = ms / n
             per_stage[name] = {"launches": n, "avg_us": 1e3 * avg, "share": 0.0,
-                               "gflop_per_launch": fl / 1e9, "tflops": fl / (avg * 1e-3) / 1e12,
+                               "fp64_slot_gflop_per_launch": fl / 1e9,
+                               "fp64_slot_tflops": fl / (avg * 1e-3) / 1e12,
                                "gbs": by / (avg * 1e-3) / 1e9}
     tot = sum(v["avg_us"] * v["launches"] for v in per_stage.values())
     for v in per_stage.values():
@@ -402,8 +466,10 @@ def run_ours(args, cfg):
     dom = max(per_stage, key=lambda k: per_stage[k]["share"])
     d = per_stage[dom]
     peaks = measured_peaks()
-    roof = {"bound": "fp64", "kernel": dom, "achieved": d["tflops"], "peak": peak_fp64, "unit": "TFLOP/s",
-            "frac": d["tflops"] / peak_fp64,
+    roof = {"bound": "fp64", "kernel": dom, "achieved": d["fp64_slot_tflops"], "peak": peak_fp64, "unit": "TFLOP/s",
+            "frac": d["fp64_slot_tflops"] / peak_fp64,
+            "achieved_counts": "FP64 issue slots x 2 per second (an FMA, multiply or add each takes one DFMA slot), "
+                               "not an IEEE flop count",
             "traffic": profiled_traffic(dom, size, args.workload),
             "peak_source": "cuBLAS DGEMM 4096^3 measured live in bench.py (GB300 FP64 is not in "
                            "MEASURED_PEAKS.json)",
@@ -418,12 +484,13 @@ def run_ours(args, cfg):
         "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": step_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: L2 projection of prod sin(pi x_d) + seeded SplitMix64 noise in [-1e-2, 1e-2]",
-        "config": {**cfg, "l2": "flushed before every timed step (512 MiB memset outside the step interval)",
-                   "solve_variants": ctx.solve_variants(), "step_solve_variants": ctx.step_solve_variants(), "launch_pdl": ctx.launch_pdl(),
-                   "fused_x": ctx.fused_x(), "step_1block": ctx.step_1block(),
-                   "step_graphs": ctx.step_graphs(),
-                   "parallelism": f"replicas x{world}", "rhs": "factored quadrature (1D Gauss-assembled bands)"},
+        "data": DATA,
+        "config": dict(cfg),
+        "timing": {"l2": "flushed before every timed step (512 MiB memset outside the step interval)",
+                   "parallelism": f"replicas x{world}"},
+        "tuning": {"solve_variants": ctx.solve_variants(), "step_solve_variants": ctx.step_solve_variants(),
+                   "launch_pdl": ctx.launch_pdl(), "fused_x": ctx.fused_x(), "step_1block": ctx.step_1block(),
+                   "step_graphs": ctx.step_graphs(), "rhs": "factored quadrature (1D Gauss-assembled bands)"},
         "e2e": {"value": e2e, "unit": "DOF-updates/s", "h2d_bytes_per_step": 8 * size, "d2h_bytes_per_step": 8 * size,
                 "steps": ke, "entry": "adsg_heat_steps_host"},
         "gpu_launches": sum(v["launches"] for v in per_stage.values()),
@@ -432,11 +499,12 @@ def run_ours(args, cfg):
         "stage_pass": {"note": "per-kernel CUDA events, a second pass of the same K steps right after the timed one",
                        "ms_per_step": staged_ms / args.steps},
         "element_rhs": elem,
-        "step_tflops": step_flops / (step_ms / args.steps * 1e-3) / 1e12,
+        "step_fp64_slot_tflops": step_flops / (step_ms / args.steps * 1e-3) / 1e12,
         "clocks": clocks,
         "wall_s": wall,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["parity"] = step_parity(ctx, u0, cfg, args.workload, os.cpu_count() or 1)
         line["cpu_baseline"] = cpu_baseline(cfg)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -21,7 +21,10 @@ from typing import Optional, Sequence
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libads_gb300.so")
+# ADSG_LIBRARY=checked loads the debug build with device-side bounds checks
+# (python iga-ads_gb300/build.py --checked) in place of the release engine.
+LIB_PATH = os.path.join(_HERE, "libads_gb300_checked.so" if os.environ.get("ADSG_LIBRARY") == "checked"
+                        else "libads_gb300.so")
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_double_p = ctypes.POINTER(ctypes.c_double)
@@ -141,6 +144,8 @@ def library() -> ctypes.CDLL:
         "adsg_batch_synchronize": (i, [vp]),
         "adsg_batch_tuning": (i, [vp, _c_int_p, _c_int_p]),
         "adsg_batch_engine": (i, [vp]),
+        "adsg_batch_test_barrier": (i, [vp, i, ll]),
+        "adsg_debug_bounds": (i, [ctypes.POINTER(ll), _c_int_p, _c_int_p, ctypes.POINTER(ll), ctypes.POINTER(ll), i]),
         "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
         "adsg_dgbtrs_checked_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
@@ -152,6 +157,20 @@ def library() -> ctypes.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def debug_bounds(reset: bool = False) -> dict:
+    """Out-of-bounds accesses the bounds-checked build's kernels caught (and
+    skipped) since the last reset: {"violations", "file", "line", "index",
+    "extent"} of the first one.  Raises AdsError in the release build."""
+    ll = ctypes.c_longlong
+    v, idx, ext = ll(0), ll(0), ll(0)
+    f, line = ctypes.c_int(0), ctypes.c_int(0)
+    _check(library().adsg_debug_bounds(ctypes.byref(v), ctypes.byref(f), ctypes.byref(line), ctypes.byref(idx),
+                                       ctypes.byref(ext), int(reset)))
+    files = ("adsg_kernels.cu", "adsg_elem.cu", "adsg_quad.cu")
+    return {"violations": v.value, "file": files[f.value] if 0 <= f.value < 3 else None, "line": line.value,
+            "index": idx.value, "extent": ext.value}
 
 
 def _check(code: int) -> None:

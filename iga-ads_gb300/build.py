@@ -1,6 +1,6 @@
 """Builds libads_gb300.so (the sm_103a engine and its C-ABI) in-tree.
 
-Usage: python iga-ads_gb300/build.py [--force]
+Usage: python iga-ads_gb300/build.py [--force] [--checked]
 
 Every CUDA translation unit is compiled for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a), in parallel, then linked with a
@@ -20,6 +20,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "ads_gb300", "libads_gb300.so")
+# the debug build with device-side bounds checks (-DADSG_BOUNDS_CHECK=1)
+BUILD_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(HERE, "ads_gb300", "libads_gb300_checked.so")
 
 CUDA_SOURCES = ["adsg_kernels.cu", "adsg_elem.cu", "adsg_capi.cu", "adsg_adjoint.cu", "adsg_points.cu", "adsg_general.cu",
                 "adsg_batch.cu", "adsg_noalloc.cu", "adsg_quad.cu"]
@@ -51,8 +54,12 @@ def _compile(cmd: list[str]) -> None:
         raise RuntimeError("compile failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    """Compile and link the engine; checked=True builds the bounds-checked
+    debug library instead (its own objects, libads_gb300_checked.so)."""
+    build_dir, lib = (BUILD_CHECKED, LIB_CHECKED) if checked else (BUILD, LIB)
+    defs = ["-DADSG_BOUNDS_CHECK=1"] if checked else []
+    os.makedirs(build_dir, exist_ok=True)
     cu, cxx = _sources()
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".hpp", ".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "ads_gb300.h"))
@@ -61,33 +68,35 @@ def build(force: bool = False, verbose: bool = False) -> str:
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
     for s in cu:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(BUILD, s + ".o")
+        obj = os.path.join(build_dir, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nv, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xptxas", "-warn-spills", *inc, "-c", src, "-o", obj])
+                         "-Xptxas", "-warn-spills", *defs, *inc, "-c", src, "-o", obj])
     for s in cxx:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(BUILD, s + ".o")
+        obj = os.path.join(build_dir, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nv, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", obj])
+            jobs.append([nv, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", *defs, *inc, "-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             list(ex.map(_compile, jobs))
-    if force or jobs or _stale(LIB, objs):
-        _compile([nv, *ARCH, "-shared", "-cudart", "static", "-Xlinker", "-soname=libads_gb300.so", "-o", LIB, *objs])
+    if force or jobs or _stale(lib, objs):
+        _compile([nv, *ARCH, "-shared", "-cudart", "static", "-Xlinker", f"-soname={os.path.basename(lib)}", "-o", lib,
+                  *objs])
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
+    ap.add_argument("--checked", action="store_true", help="the bounds-checked debug library")
     a = ap.parse_args()
     try:
-        build(force=a.force, verbose=True)
+        build(force=a.force, verbose=True, checked=a.checked)
     except RuntimeError as e:
         print(e, file=sys.stderr)
         sys.exit(1)

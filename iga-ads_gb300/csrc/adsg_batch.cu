@@ -511,4 +511,23 @@ int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captur
 
 int adsg_batch_engine(const adsg_batch* b) { return b ? b->engine : -1; }
 
+int adsg_batch_test_barrier(adsg_batch* b, int extra_arrivals, long long spin_limit) {
+    if (!b) return fail(-1, "batch is NULL");
+    if (extra_arrivals < 0) return fail(-2, "extra_arrivals < 0");
+    if (spin_limit < 1) return fail(-3, "spin_limit < 1");
+    if (b->stream) {
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) return fail_cuda(e, "batch synchronize");
+    }
+    // the launch arguments are baked into a captured graph: drop it
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->graph_steps = b->graph_par = -1;
+    b->B.barrier_extra = static_cast<unsigned>(extra_arrivals);
+    b->B.spin_limit = spin_limit;
+    return 0;
+}
+
 }  // extern "C"

@@ -34,6 +34,7 @@ int fail_cuda(int err, const char* where) {
 
 using namespace adsg;
 
+#include "adsg_check.cuh"
 #include "adsg_context.cuh"
 
 namespace {
@@ -713,6 +714,12 @@ int adsg_ctx_create(int ndim, const adsg_dim_desc* dims, adsg_ctx** out) {
         const std::vector<double> m = row_band(h, 0);
         const std::vector<double> k = row_band(h, 1);
         symmetric_row_range(m, k, h.n, h.p, D.sym_lo, D.sym_hi);
+        {
+            // ADSG_PAIR_SUMS=0: full-band passes on every row (no symmetric
+            // range), to measure what the pair sums change
+            const char* ps = std::getenv("ADSG_PAIR_SUMS");
+            if (ps && *ps == '0') D.sym_lo = D.sym_hi = 0;
+        }
         const size_t nb = static_cast<size_t>(h.elements) * h.quad_order * 2 * (h.p + 1);
         double *mrow = nullptr, *krow = nullptr, *lmul = nullptr, *ucol = nullptr, *rdiag = nullptr;
         double *btab = nullptr, *wq = nullptr, *jac = nullptr;
@@ -1216,6 +1223,7 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
         L.a = L.nlines;
         L.sa = nn;
         L.contiguous = 1;
+        L.total = L.nlines * nn;
         e = launch_line_solve(x, D, L, tr ? 1 : 0, s);
     }
     if (e == cudaSuccess)
@@ -1227,6 +1235,38 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
         if (info) *info = n_unsolved;
         std::fprintf(stderr, "adsg_dgbtrs_: CUDA failure: %s (info %d)\n", cudaGetErrorString(e), n_unsolved);
         return fail_cuda(e, "dgbtrs");
+    }
+    return 0;
+}
+
+int adsg_debug_bounds(long long* violations, int* file, int* line, long long* index, long long* extent, int reset) {
+    if (!violations) return fail(-1, "violations is NULL");
+    if (!ADSG_BOUNDS_CHECK) return fail(ADSG_ERR_UNSUPPORTED, "not the bounds-checked build (ADSG_BOUNDS_CHECK)");
+    {
+        const cudaError_t e = cudaDeviceSynchronize();  // every kernel's records are complete
+        if (e != cudaSuccess) return fail_cuda(e, "synchronize before reading the bounds records");
+    }
+    bounds_record r[3] = {};
+    const int st[3] = {bounds_read_kernels(&r[0], 0), bounds_read_elem(&r[1], 0), bounds_read_quad(&r[2], 0)};
+    for (int k = 0; k < 3; ++k) {
+        if (st[k] == 0) return fail(ADSG_ERR_UNSUPPORTED, "not the bounds-checked build (ADSG_BOUNDS_CHECK)");
+        if (st[k] < 0) return fail_cuda(static_cast<cudaError_t>(-st[k]), "read the bounds records");
+    }
+    *violations = 0;
+    int first = -1;
+    for (int k = 0; k < 3; ++k) {
+        *violations += static_cast<long long>(r[k].count);
+        if (first < 0 && r[k].count) first = k;
+    }
+    if (file) *file = first;
+    if (line) *line = first >= 0 ? r[first].line : 0;
+    if (index) *index = first >= 0 ? r[first].index : 0;
+    if (extent) *extent = first >= 0 ? r[first].extent : 0;
+    if (reset) {
+        bounds_record tmp;
+        bounds_read_kernels(&tmp, 1);
+        bounds_read_elem(&tmp, 1);
+        bounds_read_quad(&tmp, 1);
     }
     return 0;
 }

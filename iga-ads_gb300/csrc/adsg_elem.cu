@@ -12,9 +12,19 @@
 // global RHS is a plain read-modify-write, with no atomics, in a fixed order.
 #include <cuda_runtime.h>
 
+#include "adsg_check.cuh"
 #include "adsg_kernels.cuh"
 
 namespace adsg {
+
+ADSG_BOUNDS_TU(elem)
+
+// Bounds-checked build: element e[d] inside the grid and its dof box
+// first[e] .. first[e] + N - 1 inside the tensor along direction d; every
+// gather and scatter of a valid element then stays inside the tensor.
+#define ADSG_ELEM_OK(S, X, d)                                                             \
+    (ADSG_IN((S).e[d], (X).elements) && ADSG_IN((X).first[(S).e[d]], (X).n) &&           \
+     ADSG_IN((X).first[(S).e[d]] + N - 1, (X).n))
 
 namespace {
 
@@ -134,6 +144,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.e[0] = cx + ix * N;
             S.e[1] = cy + iy * N;
             S.e[2] = cz + iz * N;
+            S.valid = ADSG_ELEM_OK(S, X, 0) && ADSG_ELEM_OK(S, Y, 1) && ADSG_ELEM_OK(S, Z, 2);
+        }
+        if (S.valid) {
             S.f0[0] = X.first[S.e[0]];
             S.f0[1] = Y.first[S.e[1]];
             S.f0[2] = Z.first[S.e[2]];
@@ -324,6 +337,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         if (S.valid) {
             S.e[0] = cx + static_cast<int>(id / my) * N;
             S.e[1] = cy + static_cast<int>(id % my) * N;
+            S.valid = ADSG_ELEM_OK(S, X, 0) && ADSG_ELEM_OK(S, Y, 1);
+        }
+        if (S.valid) {
             S.f0[0] = X.first[S.e[0]];
             S.f0[1] = Y.first[S.e[1]];
             S.J = X.jac[S.e[0]] * Y.jac[S.e[1]];
@@ -499,6 +515,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.e[0] = cx + ix * N;
             S.e[1] = cy + iy * N;
             S.e[2] = cz + iz * N;
+            S.valid = ADSG_ELEM_OK(S, X, 0) && ADSG_ELEM_OK(S, Y, 1) && ADSG_ELEM_OK(S, Z, 2);
+        }
+        if (S.valid) {
             S.f0[0] = X.first[S.e[0]];
             S.f0[1] = Y.first[S.e[1]];
             S.f0[2] = Z.first[S.e[2]];
@@ -694,6 +713,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         if (S.valid) {
             S.e[0] = cx + static_cast<int>(id / my) * N;
             S.e[1] = cy + static_cast<int>(id % my) * N;
+            S.valid = ADSG_ELEM_OK(S, X, 0) && ADSG_ELEM_OK(S, Y, 1);
+        }
+        if (S.valid) {
             S.f0[0] = X.first[S.e[0]];
             S.f0[1] = Y.first[S.e[1]];
             S.J = X.jac[S.e[0]] * Y.jac[S.e[1]];

@@ -14,9 +14,19 @@
 #include <mutex>
 #include <vector>
 
+#include "adsg_check.cuh"
 #include "adsg_kernels.cuh"
 
 namespace adsg {
+
+ADSG_BOUNDS_TU(kernels)
+
+// Bounds-checked build: whether the rows 0 .. n-1 of a line, x[r * es],
+// lie inside the buffer of `total` doubles at base (a line's accesses are
+// all of that form, with the row index kept in [0, n) by the sweeps' loops).
+#define ADSG_LINE_OK(base, x, n, es, total)                                                               \
+    (!ADSG_BOUNDS_CHECK || (ADSG_IN((x) - (base), (total)) &&                                            \
+                            ADSG_IN(((x) - (base)) + static_cast<long long>((n) - 1) * (es), (total))))
 
 // ---------------------------------------------------------------------------
 // Programmatic dependent launch.  The step's kernels are launched with
@@ -92,9 +102,14 @@ template <int P, bool IN1, bool OUT1, bool SYM, bool GIN>
 __device__ __forceinline__ void band_out(long long g, const double* in0, const double* in1, double* out0,
                                          double* out1, const double* __restrict__ A0,
                                          const double* __restrict__ A1, const double* __restrict__ B0, int n_axis,
-                                         long long stride, int sym_lo, int sym_hi) {
+                                         long long stride, int sym_lo, int sym_hi, long long total) {
     constexpr int BW = 2 * P + 1;
     const int r = static_cast<int>((g / stride) % n_axis);
+    // bounds-checked build: the output, and the rows r-P .. r+P the band
+    // reaches (those inside the axis), inside the tensors of `total` doubles
+    if (!(ADSG_IN(g, total) && ADSG_IN(g - static_cast<long long>(min(r, P)) * stride, total) &&
+          ADSG_IN(g + static_cast<long long>(min(n_axis - 1 - r, P)) * stride, total)))
+        return;
     const double* a0 = A0 + static_cast<long long>(r) * BW;
     const double* a1 = IN1 ? A1 + static_cast<long long>(r) * BW : nullptr;
     const double* b0 = OUT1 ? B0 + static_cast<long long>(r) * BW : nullptr;
@@ -143,7 +158,7 @@ __global__ void __launch_bounds__(256) band_pass_kernel(const double* __restrict
     long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (g >= total) return;
     pdl_wait_and_release();
-    band_out<P, IN1, OUT1, SYM, true>(g, in0, in1, out0, out1, A0, A1, B0, n_axis, stride, sym_lo, sym_hi);
+    band_out<P, IN1, OUT1, SYM, true>(g, in0, in1, out0, out1, A0, A1, B0, n_axis, stride, sym_lo, sym_hi, total);
 }
 
 template <int P>
@@ -220,6 +235,8 @@ __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __rest
     const long long col = t % so;
     const int r0 = static_cast<int>(t / so) * seg, r1 = min(n, r0 + seg);
     const double* src = in + col;
+    if (!(ADSG_IN(col, so) && ADSG_IN(col + static_cast<long long>(n - 1) * so, static_cast<long long>(n) * so)))
+        return;  // bounds-checked build: the column inside the n x so tensor
     auto ld = [&](int r) -> double { return (r >= 0 && r < n) ? src[r * so] : 0.0; };
     double w[BW];
 #pragma unroll
@@ -324,6 +341,10 @@ cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* k
 // direction's lines where they lie.
 // ---------------------------------------------------------------------------
 constexpr int kPitch = 33;
+// Shared-memory rows reserved above and below each staged line (zeros): the
+// register sweeps read up to UNR + KL + 1 rows past the end and UNR + KL + KU
+// + 1 rows before the start (at most 8 + 2 + 1 and 4 + 8 + 1 for p <= 4).
+constexpr int kPadLo = 16, kPadHi = 16;
 
 // Raise a kernel's dynamic shared-memory limit on the current device once
 // (the attribute is per device; a small table remembers what was set).
@@ -350,6 +371,7 @@ cudaError_t ensure_smem_attribute(const void* func, size_t bytes) {
 line_layout make_line_layout(const int* n, int ndim, int d) {
     long long nx = n[0], ny = ndim > 1 ? n[1] : 1, nz = ndim > 2 ? n[2] : 1;
     line_layout L;
+    L.total = nx * ny * nz;
     if (d == 0) {
         L.nlines = ny * nz;
         L.a = L.nlines;
@@ -385,7 +407,10 @@ __device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_a
 
 __device__ __forceinline__ void stage_in(const double* __restrict__ data, double* s, const line_layout& L,
                                          int n, long long line0, int nvalid, int lane) {
+    // bounds-checked build: the lines inside the tensor (the kernels check
+    // their tiles against the launch's shared memory)
     if (L.contiguous) {
+        if (!(ADSG_IN(line0 * n, L.total) && ADSG_IN((line0 + nvalid) * n - 1, L.total))) return;
         const double* src = data + line0 * n;
         for (int l = 0; l < 32; ++l) {
             if (l < nvalid) {
@@ -398,6 +423,7 @@ __device__ __forceinline__ void stage_in(const double* __restrict__ data, double
         const long long g = line0 + lane;
         if (lane < nvalid) {
             const double* src = data + (g % L.a) * L.sa + (g / L.a) * L.sb;
+            if (!ADSG_LINE_OK(data, src, n, L.elem_stride, L.total)) return;
             for (int j = 0; j < n; ++j) async_copy8(s + j * kPitch + lane, src + j * L.elem_stride);
         } else {
             for (int j = 0; j < n; ++j) s[j * kPitch + lane] = 0.0;
@@ -410,12 +436,14 @@ __device__ __forceinline__ void stage_out(double* __restrict__ data, const doubl
                                           int n, long long line0, int nvalid, int lane) {
     if (L.contiguous) {
         double* dst = data + line0 * n;
+        if (!(ADSG_IN(line0 * n, L.total) && ADSG_IN((line0 + nvalid) * n - 1, L.total))) return;
         for (int l = 0; l < nvalid; ++l)
             for (int j = lane; j < n; j += 32) dst[static_cast<long long>(l) * n + j] = s[j * kPitch + l];
     } else {
         if (lane < nvalid) {
             const long long g = line0 + lane;
             double* dst = data + (g % L.a) * L.sa + (g / L.a) * L.sb;
+            if (!ADSG_LINE_OK(data, dst, n, L.elem_stride, L.total)) return;
 #pragma unroll 8
             for (int j = 0; j < n; ++j) dst[j * L.elem_stride] = s[j * kPitch + lane];
         }
@@ -464,6 +492,8 @@ __device__ __forceinline__ void sweep_n_generic(double* x, const dim_dev& D, con
 template <int KL, int KU, int UNR>
 __device__ __forceinline__ void sweep_n_reg(double* x, const dim_dev& D) {
     constexpr int WW = KL + KU;
+    // every row the sweep touches lies in [-kPadLo, n + kPadHi): the tile
+    static_assert(UNR + KL + 1 <= kPadHi && UNR + WW + 1 <= kPadLo, "staged tile padding too small");
     const int n = D.n;
     const int w = D.w;  // U table stride (>= KU); the L table stride equals KL
     // ---- forward: window f[t] = x[j+t] ----
@@ -619,8 +649,6 @@ __device__ __forceinline__ void sweep_t(double* x, const dim_dev& D, const long 
     }
 }
 
-// Shared-memory rows reserved above and below each staged line (zeros).
-constexpr int kPadLo = 16, kPadHi = 16;
 
 // KL/KU > 0: register sweeps for bands with kl <= KL, regular U extent <= KU;
 // KL == 0: generic shared-memory sweeps.
@@ -634,6 +662,7 @@ __global__ void __launch_bounds__(32) line_solve_kernel(double* __restrict__ dat
     pdl_wait();
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
     double* s = smem + kPadLo * kPitch;
+    if (!ADSG_SMEM_RANGE(smem, static_cast<long long>(D.n + kPadLo + kPadHi) * kPitch)) return;
     for (int r = 0; r < kPadLo; ++r) smem[r * kPitch + lane] = 0.0;
     for (int r = 0; r < kPadHi; ++r) s[(D.n + r) * kPitch + lane] = 0.0;
     stage_in(data, s, L, D.n, line0, nvalid, lane);
@@ -660,6 +689,7 @@ __global__ void __launch_bounds__(128) line_solve_long_kernel(double* __restrict
     if (g >= L.nlines) return;
     pdl_wait();
     double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    if (!ADSG_LINE_OK(data, x, D.n, L.elem_stride, L.total)) return;
     if (trans)
         sweep_t(x, D, L.elem_stride);
     else
@@ -825,6 +855,7 @@ __global__ void __launch_bounds__(128) line_solve_global_kernel(double* __restri
     if (g >= L.nlines) return;
     pdl_wait();
     double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    if (!ADSG_LINE_OK(data, x, D.n, L.elem_stride, L.total)) return;
     sweep_global<KL, KU, UNR>(x, L.elem_stride, D);
 }
 
@@ -1015,12 +1046,14 @@ template <int K, int UNR, bool UNIT>
 __global__ void __launch_bounds__(128) line_solve_twisted_kernel(double* __restrict__ data, dim_dev D, line_layout L) {
     const int lane = threadIdx.x & 31, chain = lane >> 4;
     const long long g = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 16 + (lane & 15);
-    const bool active = g < L.nlines;
+    double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
+    const long long es = L.elem_stride;
+    // bounds-checked build: the line inside the tensor (both chains of a line
+    // decide alike, so a skipped line leaves no partner waiting in the shuffle)
+    const bool active = g < L.nlines && ADSG_LINE_OK(data, x, D.n, es, L.total);
     const unsigned mask = __ballot_sync(0xffffffffu, active);  // lanes g and g^16 share a line
     if (!active) return;
     pdl_wait();
-    double* x = data + (L.contiguous ? g * D.n : (g % L.a) * L.sa + (g / L.a) * L.sb);
-    const long long es = L.elem_stride;
     const long long off = static_cast<long long>(chain) * D.tw_rows;
     if (chain) x += static_cast<long long>(D.n - 1) * es;
     twisted_chain<K, UNR, UNIT>(x, x, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K, D.tw_ucol + off * K,
@@ -1050,6 +1083,9 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(const do
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const double* src = data + g0 * n;
     const int count = nv * n;
+    // bounds-checked build: the warp's tile and its 16 lines (warp-uniform)
+    if (!(ADSG_SMEM_RANGE(tile, 16LL * pitch) && ADSG_IN(g0 * n, L.total) && ADSG_IN(g0 * n + count - 1, L.total)))
+        return;
 #pragma unroll 4
     for (int e = lane; e < count; e += 32) {
         const int line = e / n;
@@ -1159,6 +1195,10 @@ __global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double*
     W.n2 = D.tw_n2;
     W.nv = static_cast<int>(min(16LL, L.nlines - g0));
     double* buf = smem + static_cast<size_t>(warp) * 2 * 16 * kChunkPitch;
+    // bounds-checked build: the warp's buffer and its 16 lines (warp-uniform)
+    if (!(ADSG_SMEM_RANGE(buf, 2LL * 16 * kChunkPitch) && ADSG_IN(g0 * D.n, L.total) &&
+          ADSG_IN((g0 + W.nv) * D.n - 1, L.total)))
+        return;
     double* mine = buf + (chain * 16 + line) * kChunkPitch;  // this lane's slots
     const bool active = line < W.nv;  // every lane stays to the end: the staging is warp-wide
     const int nc = chain ? W.n2 : W.n1, nmax = max(W.n1, W.n2);
@@ -1291,6 +1331,8 @@ __global__ void __launch_bounds__(128) rhs_x_solve_kernel(const double* __restri
     double* tile = smem + static_cast<size_t>(warp) * 16 * pitch;
     const long long base = g0 * n;
     const int count = nv * n;
+    // bounds-checked build: the warp's tile and its 16 lines (warp-uniform)
+    if (!(ADSG_SMEM_RANGE(tile, 16LL * pitch) && ADSG_IN(base, L.total) && ADSG_IN(base + count - 1, L.total))) return;
     // unrolled so that several outputs' loads are in flight at once: few warps
     // per SM hold these tiles
 #pragma unroll 4
@@ -1402,6 +1444,7 @@ __global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restr
     double* A = sm + N;
     double* C = sm + 2 * N;
     double* R = sm + 3 * N;
+    if (!ADSG_SMEM_RANGE(sm, 4LL * N)) return;
     pdl_wait_and_release();  // the tables may come from the previous launch (the dt bands)
     prefetch_step_tables<K>(X, true);
     prefetch_step_tables<K>(Y, false);
@@ -1411,14 +1454,14 @@ __global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restr
     const int ylo = max(Y.sym_lo, K), yhi = min(Y.sym_hi, ny - K);
     for (int g = threadIdx.x; g < N; g += blockDim.x) {
         if (yhi > ylo)
-            band_out<K, false, true, true, false>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, ylo, yhi);
+            band_out<K, false, true, true, false>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, ylo, yhi, N);
         else
-            band_out<K, false, true, false, false>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, 0, 0);
+            band_out<K, false, true, false, false>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, 0, 0, N);
     }
     __syncthreads();
     // x pass: R = (-dt Kx) A + Mx C
     for (int g = threadIdx.x; g < N; g += blockDim.x)
-        band_out<K, true, false, false, false>(g, A, C, R, nullptr, X.kdt, X.mrow, nullptr, nx, 1, 0, 0);
+        band_out<K, true, false, false, false>(g, A, C, R, nullptr, X.kdt, X.mrow, nullptr, nx, 1, 0, 0, N);
     __syncthreads();
     // the step's solve order: the outer direction first, x last
     small_sweeps<K, UNR>(R, Y, nx, 1, nx);  // y-lines: columns of R
@@ -1538,6 +1581,7 @@ __global__ void __launch_bounds__(32 * WPB) line_solve_staged_kernel(double* __r
     const int nvalid = static_cast<int>(min(32LL, L.nlines - line0));
     double* base = smem + static_cast<size_t>(warp) * (D.n + kPadLo + kPadHi) * kPitch;
     double* s = base + kPadLo * kPitch;
+    if (!ADSG_SMEM_RANGE(base, static_cast<long long>(D.n + kPadLo + kPadHi) * kPitch)) return;
     for (int r = 0; r < kPadLo; ++r) base[r * kPitch + lane] = 0.0;
     for (int r = 0; r < kPadHi; ++r) s[(D.n + r) * kPitch + lane] = 0.0;
     stage_in(data, s, L, D.n, line0, nvalid, lane);
@@ -1684,6 +1728,7 @@ __global__ void __launch_bounds__(128) line_solve_permat_kernel(double* __restri
     const int* uext = T.uext + m * static_cast<long long>(n);
     double* x = data + (L.contiguous ? g * n : (g % L.a) * L.sa + (g / L.a) * L.sb);
     const long long es = L.elem_stride;
+    if (!ADSG_LINE_OK(data, x, n, es, L.total)) return;
     for (int j = 0; j < n - 1; ++j) {
         const int l = __ldg(piv + j);
         if (l != j) {
@@ -1795,9 +1840,14 @@ namespace {
 template <int P>
 __device__ __forceinline__ void band_one_cg(long long g, const double* in0, const double* in1, double* out0, double* out1,
                                             const double* A0, const double* A1, const double* B0, int n_axis,
-                                            long long stride) {
+                                            long long stride, long long total) {
     constexpr int BW = 2 * P + 1;
     const int r = static_cast<int>((g / stride) % n_axis);
+    // bounds-checked build: the output and the rows the band reaches inside
+    // the instance's tensors of `total` doubles
+    if (!(ADSG_IN(g, total) && ADSG_IN(g - static_cast<long long>(min(r, P)) * stride, total) &&
+          ADSG_IN(g + static_cast<long long>(min(n_axis - 1 - r, P)) * stride, total)))
+        return;
     const double* a0 = A0 + static_cast<long long>(r) * BW;
     double acc0 = 0.0, acc1 = 0.0;
 #pragma unroll
@@ -1824,19 +1874,31 @@ __device__ __forceinline__ void batch_unit(const batch_inst& I, int stage, long 
     const long long nn = static_cast<long long>(n) * n;
     if (I.ndim == 3) {
         switch (stage) {
-            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn); return;
-            case 1: band_one_cg<P>(u, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n); return;
-            case 2: band_one_cg<P>(u, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1); return;
-            case 3: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D); return;
-            case 4: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + (u % n) + (u / n) * nn, n, D); return;
-            default: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, nn, D); return;
+            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn, I.size); return;
+            case 1: band_one_cg<P>(u, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n, I.size); return;
+            case 2: band_one_cg<P>(u, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, I.size); return;
+            case 3:
+                if (ADSG_LINE_OK(nxt, nxt + u * n, n, 1, I.size))
+                    sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D);
+                return;
+            case 4:
+                if (ADSG_LINE_OK(nxt, nxt + (u % n) + (u / n) * nn, n, n, I.size))
+                    sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + (u % n) + (u / n) * nn, n, D);
+                return;
+            default:
+                if (ADSG_LINE_OK(nxt, nxt + u, n, nn, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, nn, D);
+                return;
         }
     } else {
         switch (stage) {
-            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n); return;
-            case 2: band_one_cg<P>(u, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1); return;
-            case 3: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D); return;
-            case 4: sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, n, D); return;
+            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n, I.size); return;
+            case 2: band_one_cg<P>(u, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, I.size); return;
+            case 3:
+                if (ADSG_LINE_OK(nxt, nxt + u * n, n, 1, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D);
+                return;
+            case 4:
+                if (ADSG_LINE_OK(nxt, nxt + u, n, n, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, n, D);
+                return;
             default: return;
         }
     }
@@ -1846,7 +1908,8 @@ __device__ __forceinline__ void batch_unit(const batch_inst& I, int stage, long 
 // counter; the last arrival resets it and advances the generation; the
 // others poll the generation with a spin limit, after which they set the
 // error word and the kernel winds down instead of waiting forever.
-__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err, unsigned nblocks) {
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err, unsigned nblocks,
+                                             long long spin_limit) {
     __syncthreads();
     __shared__ int ok;
     if (threadIdx.x == 0) {
@@ -1861,7 +1924,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int
         } else {
             long long spins = 0;
             while (atomicAdd(gen, 0u) == g) {
-                if (++spins > (1LL << 26) || atomicAdd(reinterpret_cast<unsigned*>(err), 0u) != 0u) {
+                if (++spins > spin_limit || atomicAdd(reinterpret_cast<unsigned*>(err), 0u) != 0u) {
                     atomicExch(err, 1);
                     ok = 0;
                     break;
@@ -1899,7 +1962,7 @@ __global__ void __launch_bounds__(256) batch_steps_kernel(batch_dev B, int nstep
                     }
                 }
             }
-            if (!grid_barrier(B.bar_count, B.bar_gen, B.err, nblocks)) return;
+            if (!grid_barrier(B.bar_count, B.bar_gen, B.err, nblocks + B.barrier_extra, B.spin_limit)) return;
         }
     }
 }

@@ -68,6 +68,7 @@ struct line_layout {
     long long nlines = 0;
     long long a = 1, sa = 0, sb = 0, elem_stride = 1;
     int contiguous = 0;  // lines are consecutive blocks of n doubles
+    long long total = 0;  // doubles in the tensor the lines belong to (bounds-checked build)
 };
 
 line_layout make_line_layout(const int* n, int ndim, int d);
@@ -112,6 +113,12 @@ struct batch_dev {
     unsigned* bar_count = nullptr;
     unsigned* bar_gen = nullptr;
     int* err = nullptr;
+    // bounded wait of the grid barrier: polls of the generation before a
+    // waiting block gives up (sets *err and winds down)
+    long long spin_limit = 1LL << 26;
+    // test hook (failure detection): arrivals the barrier expects beyond the
+    // blocks launched; nonzero makes every wait run out
+    unsigned barrier_extra = 0;
 };
 
 const void* batch_kernel_symbol();

@@ -7,9 +7,12 @@
 // (p+1)- or (p+1)q-term sum.
 #include <cuda_runtime.h>
 
+#include "adsg_check.cuh"
 #include "adsg_kernels.cuh"
 
 namespace adsg {
+
+ADSG_BOUNDS_TU(quad)
 
 namespace {
 
@@ -27,6 +30,10 @@ __global__ void quad_interp_kernel(const double* __restrict__ in, double* __rest
         const int e = static_cast<int>(r / q), qq = static_cast<int>(r % q);
         const double* row = btab + (static_cast<long long>(e) * q + qq) * 2 * (p + 1);
         const long long base = ii + inner * (static_cast<long long>(__ldg(first + e)) + n_axis * oo);
+        // bounds-checked build: the element, and its p+1 input rows inside the tensor
+        if (!(ADSG_IN(e, E) && ADSG_IN(base, inner * n_axis * outer) &&
+              ADSG_IN(base + inner * p, inner * n_axis * outer)))
+            continue;
         double a0 = 0.0, a1 = 0.0;
         for (int a = 0; a <= p; ++a) {
             const double v = in[base + inner * a];
@@ -53,6 +60,10 @@ __global__ void quad_project_kernel(const double* __restrict__ in, double* __res
         const long long oo = g / (inner * n_axis);
         double acc = 0.0;
         const int lo = __ldg(erange + 2 * a), hi = __ldg(erange + 2 * a + 1);
+        // bounds-checked build: the supporting elements, and the point rows they read
+        if (!(ADSG_IN(lo, E) && ADSG_IN(hi, E) && ADSG_IN(ii + inner * (static_cast<long long>(lo) * q + Qa * oo), inner * Qa * outer) &&
+              ADSG_IN(ii + inner * (static_cast<long long>(hi) * q + q - 1 + Qa * oo), inner * Qa * outer)))
+            continue;
         for (int e = lo; e <= hi; ++e) {
             const int loc = a - __ldg(first + e);
             const double je = __ldg(J + e);

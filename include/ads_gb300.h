@@ -370,6 +370,27 @@ int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captur
  * kernels, run side by side); -1 for a NULL batch.  ADSG_BATCH_ENGINE=0/1
  * forces it. */
 int adsg_batch_engine(const adsg_batch* b);
+/* Test hook for failure detection (no reference counterpart): the persistent
+ * kernel's grid barriers expect extra_arrivals blocks beyond those launched
+ * (nonzero: no barrier can complete) and a waiting block gives up after
+ * spin_limit polls, sets the batch's error word and the kernel winds down.
+ * The next adsg_batch_synchronize returns ADSG_ERR_DEVICE and clears the
+ * word; adsg_batch_test_barrier(b, 0, 1 << 26) restores the defaults. */
+int adsg_batch_test_barrier(adsg_batch* b, int extra_arrivals, long long spin_limit);
+
+/* ---- debug build: device-side bounds checks ----------------------------------
+ * No reference counterpart (the reference's debug builds assert in
+ * band_matrix::operator(), lin/band_matrix.hpp:43).  In the library built
+ * with -DADSG_BOUNDS_CHECK=1 (libads_gb300_checked.so: python
+ * iga-ads_gb300/build.py --checked) the step, solve, batch, element and
+ * Gauss-point kernels compare every global index with the extent of the
+ * buffer it addresses, and every shared-memory tile with the launch's
+ * dynamic shared memory; a violation skips the access (never traps) and is
+ * counted.  This returns the count since the last reset and the first
+ * violation's file (0 adsg_kernels.cu, 1 adsg_elem.cu, 2 adsg_quad.cu), source
+ * line, index and extent; reset != 0 clears them.  Synchronises the device.
+ * ADSG_ERR_UNSUPPORTED in the release build. */
+int adsg_debug_bounds(long long* violations, int* file, int* line, long long* index, long long* extent, int reset);
 
 /* ---- the heat RHS without any allocation --------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

@@ -24,9 +24,25 @@ def pytest_sessionstart(session):
     import build as engine_build  # iga-ads_gb300/build.py
 
     engine_build.build()
+    if os.environ.get("ADSG_LIBRARY") == "checked":  # the bounds-checked debug library
+        engine_build.build(checked=True)
     import oracle
 
     oracle.build()
+
+
+def pytest_sessionfinish(session, exitstatus):
+    """Under the bounds-checked library, write what its kernels' checks
+    caught to the file ADSG_BOUNDS_REPORT names (read by the test that runs
+    the parity cases under the checks)."""
+    path = os.environ.get("ADSG_BOUNDS_REPORT")
+    if path and os.environ.get("ADSG_LIBRARY") == "checked" and gpu_available():
+        import json
+
+        import ads_gb300
+
+        with open(path, "w") as f:
+            json.dump(ads_gb300.debug_bounds(), f)
 
 
 def gpu_available() -> bool:

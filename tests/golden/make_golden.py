@@ -308,11 +308,11 @@ def snapshot(u, n, mass_ab, p, prefix, planes):
     out = {prefix + "max": np.float64(s), prefix + "norm": np.float64(np.linalg.norm(u / s) * s)}
     Mu = mass_apply(u / s, (n, n, n), [(mass_ab, p)] * 3)
     out[prefix + "mass_norm"] = np.float64(np.sqrt(np.dot(u / s, Mu)) * s)
-    t = u.reshape(n, n, n)  # [k][j][i]
+    t = u.reshape(n, n, n)  # [k][j][i]; copies, since u goes on changing in place
     if "z" in planes:
-        out[prefix + "plane_z"] = np.ascontiguousarray(t[n // 2])
+        out[prefix + "plane_z"] = t[n // 2].copy()
     if "y" in planes:
-        out[prefix + "plane_y"] = np.ascontiguousarray(t[:, n // 3, :])
+        out[prefix + "plane_y"] = t[:, n // 3, :].copy()
     return out
 
 

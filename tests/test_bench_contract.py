@@ -1,6 +1,7 @@
 """bench.py's host-side pieces, on the CPU: the workload descriptions, the
-DRAM-traffic lookup in the committed profile table, the clock-record parser
-and the reference arm's JSON line (the CPU oracle on a small grid)."""
+DRAM-traffic figures from ncu, the clock-record parser and the reference
+arm's JSON line (the CPU oracle on a small grid, with the same warm-up, step
+count, initial field and config as our arm)."""
 from __future__ import annotations
 
 import importlib.util
@@ -94,3 +95,22 @@ def test_reference_arm_line(capsys):
     assert line["e2e"] == {"value": line["value"], "unit": "DOF-updates/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["dofs"] == 34 * 34
+    assert line["warmup"] == 1 and line["data"] == b.DATA
+    assert line["config"] == b.workload_config("heat2d_p2_32")
+
+
+def test_reference_arm_initial_field_matches_ours():
+    """The reference arm builds the initial field from the oracle's tables
+    (bit-identical to the reference's); it equals the engine's host-side
+    field to rounding."""
+    import numpy as np
+
+    import ads_gb300 as ads
+    import oracle
+    from ads_gb300 import inputs
+
+    b = _bench()
+    pr = oracle.Problem([2, 2], [32, 32])
+    mine = inputs.initial_field([b._OracleDim(pr, d) for d in range(2)], seed=0)
+    ours = inputs.initial_field([ads.Dimension(2, 32) for _ in range(2)], seed=0)
+    assert np.abs(mine - ours).max() <= 1e-15

@@ -122,8 +122,9 @@ def test_heat_260cubed_p4_run(cuda):
 def test_mixed_64_batch_against_oracle(engine, cuda, monkeypatch):
     """Both batch engines (persistent kernel, concurrent per-instance graph) on
     the seeded 64-instance set, two steps, every instance against the
-    oracle.  The bound of a p >= 3 instance also admits twice the oracle's
-    own spread (its executor on two thread counts) at that instance."""
+    oracle.  Where an instance's error is above the contract (p = 4), the
+    bound also admits twice the oracle's own spread at that instance: its
+    executor on other thread counts against the run compared with."""
     monkeypatch.setenv("ADSG_BATCH_ENGINE", engine)
     specs = ads.batch_specs(seed=0)
     b = ads.Batch(specs)
@@ -141,7 +142,35 @@ def test_mixed_64_batch_against_oracle(engine, cuda, monkeypatch):
         err = oracle.rel_l2(b.get_state(i), ref)
         spread = 0.0
         if err > 2 * STEP:
-            spread = oracle.rel_l2(pr.heat_steps(u0[i], dt, 2, nthreads=max(2, THREADS - 3)), ref)
+            for t in {max(2, THREADS - 3), max(2, THREADS - 5), max(2, THREADS // 2)}:
+                spread = max(spread, oracle.rel_l2(pr.heat_steps(u0[i], dt, 2, nthreads=t), ref))
         check(f"engine {engine} instance {i} {nd}D p={p} {e} elements 2 steps", err, 2 * STEP, spread)
         worst = max(worst, err)
     print(f"[parity] engine {engine}: worst instance rel L2 {worst:.3e}")
+
+
+@pytest.mark.parametrize("p,E,nsteps", [(2, 128, 50), (4, 256, 20)])
+def test_pair_sums_stay_inside_the_bounds_at_full_size(p, E, nsteps, cuda, monkeypatch):
+    """On the symmetric interior rows the RHS passes add u[r-t] + u[r+t] once
+    and multiply by the left coefficient of the pair; the quadrature leaves
+    the right one 14-220 ulp of the row's largest entry away.  Against the
+    same passes on full band rows (ADSG_PAIR_SUMS=0): the RHS stays within
+    its 1e-13 bound and the whole run within 1e-10."""
+    import torch
+
+    monkeypatch.setenv("ADSG_FUSE_X", "0")  # both contexts solve x last
+    dims = [ads.Dimension(p, E) for _ in range(3)]
+    u0 = torch.from_numpy(inputs.initial_field(dims, seed=0)).to(cuda)
+    out = []
+    for pair in ("1", "0"):
+        monkeypatch.setenv("ADSG_PAIR_SUMS", pair)
+        ctx = ads.Context(dims)
+        r = torch.empty_like(u0)
+        ctx.heat_rhs(u0, r, 1e-6)
+        u = u0.clone()
+        ctx.heat_steps(u, 1e-6, nsteps)
+        ctx.synchronize()
+        out.append((r.cpu().numpy(), u.cpu().numpy()))
+        ctx.close()
+    check(f"{E + p}^3 p={p} rhs, pair sums vs full band", oracle.rel_l2(out[0][0], out[1][0]), 1e-13)
+    check(f"{E + p}^3 p={p} {nsteps} steps, pair sums vs full band", oracle.rel_l2(out[0][1], out[1][1]), RUN)
