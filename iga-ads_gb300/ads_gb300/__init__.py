@@ -75,6 +75,24 @@ class PointForm(ctypes.Structure):
     ]
 
 
+class Plane(ctypes.Structure):
+    """adsg_plane: the dofs whose index along direction `dim` is `index`;
+    `values` a device address (x-fastest over the other directions) or None
+    for zeros."""
+
+    _fields_ = [("dim", ctypes.c_int), ("index", ctypes.c_int), ("values", ctypes.c_void_p)]
+
+
+def _planes(planes):
+    """[(dim, index, values or None), ...] -> a ctypes array of Plane."""
+    planes = list(planes)
+    arr = (Plane * max(1, len(planes)))()
+    for k, (d, idx, vals) in enumerate(planes):
+        arr[k].dim, arr[k].index = int(d), int(idx)
+        arr[k].values = None if vals is None else _devptr(vals)
+    return arr, len(planes)
+
+
 _lib = None
 
 
@@ -106,6 +124,8 @@ def library() -> ctypes.CDLL:
         "adsg_ads_solve": (i, [vp, vp, vp]),
         "adsg_ads_solve_t": (i, [vp, vp]),
         "adsg_heat_step": (i, [vp, vp, vp, d]),
+        "adsg_set_planes": (i, [vp, vp, i, ctypes.POINTER(Plane)]),
+        "adsg_heat_step_dirichlet": (i, [vp, vp, vp, d, i, ctypes.POINTER(Plane)]),
         "adsg_form_rhs": (i, [vp, vp, ctypes.POINTER(PointForm), vp]),
         "adsg_heat_steps": (i, [vp, vp, d, i]),
         "adsg_heat_steps_host": (i, [vp, _c_double_p, d, i]),
@@ -395,6 +415,19 @@ class Context:
     def heat_steps(self, u, dt: float, nsteps: int) -> None:
         _check(library().adsg_heat_steps(self._h, _devptr(u), float(dt), int(nsteps)))
 
+    def set_planes(self, u, planes) -> None:
+        """Overwrite planes [(dim, index, values or None)] of a device tensor:
+        the Dirichlet rows of the reference's heat_2d / validation solves."""
+        arr, n = _planes(planes)
+        _check(library().adsg_set_planes(self._h, _devptr(u), n, arr))
+
+    def heat_step_dirichlet(self, u_prev, u_next, dt: float, planes) -> None:
+        """heat_2d::step / validation::step: compute_rhs, the Dirichlet planes
+        [(dim, index, values or None)] written into the right-hand side, then
+        ads_solve with the fixed-row factorisations."""
+        arr, n = _planes(planes)
+        _check(library().adsg_heat_step_dirichlet(self._h, _devptr(u_prev), _devptr(u_next), float(dt), n, arr))
+
     def count_nonfinite(self, u) -> int:
         """Number of NaN / Inf entries of a device tensor (failure detection)."""
         c = ctypes.c_longlong()
@@ -589,4 +622,5 @@ def dgbtrs(trans: str, n: int, kl: int, ku: int, nrhs: int, ab: np.ndarray, ldab
     return info.value
 
 
-__all__ = ["AdsError", "Adjoint", "mass_loss", "Batch", "batch_specs", "Context", "DimDesc", "Dimension", "Heat", "ads_solve", "dgbtrs", "library", "LIB_PATH"]
+__all__ = ["AdsError", "Adjoint", "mass_loss", "Batch", "batch_specs", "Context", "DimDesc", "Dimension", "Heat", "Plane",
+           "ads_solve", "debug_bounds", "dgbtrs", "library", "LIB_PATH"]

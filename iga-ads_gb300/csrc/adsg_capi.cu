@@ -919,6 +919,43 @@ int adsg_heat_step(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, 
     return step_via_graph(ctx, u_prev_dev, u_next_dev, dt);
 }
 
+int adsg_set_planes(adsg_ctx* ctx, double* u_dev, int nplanes, const adsg_plane* planes) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_dev) return fail(-2, "u is NULL");
+    if (nplanes < 0) return fail(-3, "nplanes < 0");
+    if (nplanes > 0 && !planes) return fail(-4, "planes is NULL");
+    for (int i = 0; i < nplanes; ++i)
+        if (planes[i].dim < 0 || planes[i].dim >= ctx->ndim || planes[i].index < 0 ||
+            planes[i].index >= ctx->n[planes[i].dim])
+            return fail(-4, "a plane's direction or index is outside the tensor");
+    for (int i = 0; i < nplanes; ++i)
+        ADSG_CUDA_TRY(launch_set_plane(u_dev, planes[i].values, ctx->n, ctx->ndim, planes[i].dim, planes[i].index,
+                                       ctx->stream),
+                      "set plane");
+    return 0;
+}
+
+int adsg_heat_step_dirichlet(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, double dt, int nplanes,
+                             const adsg_plane* planes) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_prev_dev) return fail(-2, "u_prev is NULL");
+    if (!u_next_dev) return fail(-3, "u_next is NULL");
+    if (!std::isfinite(dt)) return fail(-4, "dt must be finite");
+    if (nplanes < 0) return fail(-5, "nplanes < 0");
+    if (nplanes > 0 && !planes) return fail(-6, "planes is NULL");
+    const char* a = reinterpret_cast<const char*>(u_prev_dev);
+    const char* b = reinterpret_cast<const char*>(u_next_dev);
+    const size_t bytes = sizeof(double) * static_cast<size_t>(ctx->size);
+    if (a < b + bytes && b < a + bytes) return fail(-3, "u_prev and u_next overlap");
+    for (int i = 0; i < nplanes; ++i)
+        if (planes[i].dim < 0 || planes[i].dim >= ctx->ndim || planes[i].index < 0 ||
+            planes[i].index >= ctx->n[planes[i].dim])
+            return fail(-6, "a plane's direction or index is outside the tensor");
+    if (int st = enqueue_rhs(ctx, u_prev_dev, u_next_dev, dt)) return st;
+    if (int st = adsg_set_planes(ctx, u_next_dev, nplanes, planes)) return st;
+    return enqueue_solve(ctx, u_next_dev, 0);
+}
+
 int adsg_heat_steps(adsg_ctx* ctx, double* u_dev, double dt, int nsteps) {
     if (!ctx) return fail(-1, "ctx is NULL");
     if (!u_dev) return fail(-2, "u is NULL");

@@ -1807,6 +1807,39 @@ __global__ void count_nonfinite_kernel(const double* __restrict__ x, long long n
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
+// Dirichlet planes: the dofs of an x-fastest nx x ny x nz tensor whose index
+// along direction d is k, set to values[t] (t over the plane's dofs, x-fastest
+// over the other directions) or to 0 when values is NULL.
+__global__ void set_plane_kernel(double* __restrict__ u, const double* __restrict__ values, long long nx, long long ny,
+                                 long long nz, int d, long long k, long long count) {
+    const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    long long i, j, l;
+    if (d == 0) {
+        i = k;
+        j = t % ny;
+        l = t / ny;
+    } else if (d == 1) {
+        j = k;
+        i = t % nx;
+        l = t / nx;
+    } else {
+        l = k;
+        i = t % nx;
+        j = t / nx;
+    }
+    const long long g = i + nx * (j + ny * l);
+    if (ADSG_IN(g, nx * ny * nz)) u[g] = values ? values[t] : 0.0;
+}
+
+cudaError_t launch_set_plane(double* u, const double* values, const int* n, int ndim, int d, int k, cudaStream_t s) {
+    const long long nx = n[0], ny = ndim > 1 ? n[1] : 1, nz = ndim > 2 ? n[2] : 1;
+    const long long count = nx * ny * nz / n[d];
+    if (count <= 0) return cudaSuccess;
+    set_plane_kernel<<<static_cast<unsigned>((count + 255) / 256), 256, 0, s>>>(u, values, nx, ny, nz, d, k, count);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_count_nonfinite(const double* x, long long n, unsigned long long* count, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;

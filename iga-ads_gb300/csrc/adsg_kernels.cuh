@@ -141,6 +141,10 @@ cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, dou
                                       const double* B0, int n_axis, long long stride, cudaStream_t s, int sym_lo,
                                       int sym_hi);
 
+// Set the plane {index along d == k} of an x-fastest tensor with dofs n[0..ndim)
+// to values (device, x-fastest over the other directions) or to 0 (NULL).
+cudaError_t launch_set_plane(double* u, const double* values, const int* n, int ndim, int d, int k, cudaStream_t s);
+
 // nrow = mrow - dt*krow, kdt = -dt*krow for one dimension
 cudaError_t launch_dt_bands(const dim_dev& d, double dt, double* nrow, double* kdt, cudaStream_t s);
 

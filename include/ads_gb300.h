@@ -206,6 +206,30 @@ int adsg_ctx_step_1block(const adsg_ctx* ctx);
  * depend on it. */
 int adsg_ctx_step_graphs(const adsg_ctx* ctx);
 
+/* ---- Dirichlet rows -----------------------------------------------------------
+ * The reference imposes Dirichlet data in two steps: the dimension's mass
+ * matrix gets identity rows (dimension::fix_dof, adsg_dim_fix_dof here) and,
+ * before every solve, those rows of the right-hand side are overwritten with
+ * the boundary values -- examples/heat/heat_2d.hpp:40-45 sets row x = 0 to the
+ * load vector of sin(pi y); examples/validation/validation.hpp:31-41 zeroes
+ * all four sides.  A plane is the set of dofs whose index along direction dim
+ * equals index; values (device) holds its dofs x-fastest over the other
+ * directions, or is NULL for zeros. */
+typedef struct adsg_plane {
+    int dim;
+    int index;
+    const double* values;
+} adsg_plane;
+/* Overwrite planes of a device tensor (asynchronous). */
+int adsg_set_planes(adsg_ctx* ctx, double* u_dev, int nplanes, const adsg_plane* planes);
+/* One step of those examples: compute_rhs (the heat form, as adsg_heat_rhs),
+ * the planes overwritten in the right-hand side, then ads_solve with the
+ * context's (fixed-row) factorisations: heat_2d::step / validation::step
+ * (heat_2d.hpp:66-69 with its solve at :40-45).  u_prev and u_next must not
+ * overlap.  Asynchronous. */
+int adsg_heat_step_dirichlet(adsg_ctx* ctx, const double* u_prev_dev, double* u_next_dev, double dt, int nplanes,
+                             const adsg_plane* planes);
+
 /* ---- host-buffer entry points (the reference-facing boundary) ------------- */
 
 /* adsg_heat_steps on a host tensor: copies u_host to the device, runs nsteps,

@@ -74,6 +74,29 @@ public:
 #include "heat/heat_3d.hpp"
 #undef private
 
+// The reference's heat_2d (Dirichlet row at x = 0, heat_2d.hpp:40-52) and
+// validation (Dirichlet on every side, exact solution, validation.hpp) examples
+// write files through ads::output_manager, whose headers need boost::format;
+// this stand-in of output_manager<2> (constructor and to_file, the interface
+// those examples use) writes nothing, and its header is skipped.  Their
+// galois_executor is the stand-in above; galois/Timer.h comes from refshim/.
+#define ADS_OUTPUT_MANAGER_HPP
+namespace ads {
+template <std::size_t Dim>
+struct output_manager;
+template <>
+struct output_manager<2> {
+    template <typename... A>
+    explicit output_manager(const A&...) { }
+    template <typename... A>
+    void to_file(const A&...) { }
+};
+}  // namespace ads
+#define private public
+#include "heat/heat_2d.hpp"
+#include "validation/validation.hpp"
+#undef private
+
 // The reference's flow environment (random channel paths, mt19937-seeded) is
 // header-only; its flow.hpp include is skipped (the flow class needs Galois).
 #define FLOW_FLOW_HPP
@@ -405,6 +428,120 @@ int ref_heat_steps_mt(int ndim, int p, int elements, double dt, int nsteps, doub
     } else {
         return -1;
     }
+    return 0;
+}
+
+// normL2 / normH1 of a spline and errorL2 / errorH1 against
+// f = prod_d sin(pi x_d) (with its gradient), and normL2 / normH1 of f itself,
+// by basic_simulation_2d/3d's own quadrature loops
+// (basic_simulation_3d.hpp:281-397): out = {normL2(u), normH1(u),
+// errorL2(u, f), errorH1(u, f), normL2(f), normH1(f)}.
+class norms3_driver : public ads::simulation_3d {
+public:
+    using simulation_3d::simulation_3d;
+    void norms(const double* uin, double* out) {
+        vector_type u{shape()};
+        load(u, uin);
+        auto f = [](point_type p) {
+            const double sx = std::sin(M_PI * p[0]), sy = std::sin(M_PI * p[1]), sz = std::sin(M_PI * p[2]);
+            const double cx = M_PI * std::cos(M_PI * p[0]), cy = M_PI * std::cos(M_PI * p[1]),
+                         cz = M_PI * std::cos(M_PI * p[2]);
+            return value_type{sx * sy * sz, cx * sy * sz, sx * cy * sz, sx * sy * cz};
+        };
+        out[0] = normL2(u, x, y, z);
+        out[1] = normH1(u, x, y, z);
+        out[2] = errorL2(u, x, y, z, f);
+        out[3] = errorH1(u, x, y, z, f);
+        out[4] = normL2(x, y, z, f);
+        out[5] = normH1(x, y, z, f);
+    }
+    void step() { }
+};
+
+class norms2_driver : public ads::simulation_2d {
+public:
+    using simulation_2d::simulation_2d;
+    void norms(const double* uin, double* out) {
+        vector_type u{shape()};
+        load(u, uin);
+        auto f = [](point_type p) {
+            const double sx = std::sin(M_PI * p[0]), sy = std::sin(M_PI * p[1]);
+            return value_type{sx * sy, M_PI * std::cos(M_PI * p[0]) * sy, sx * M_PI * std::cos(M_PI * p[1])};
+        };
+        out[0] = normL2(u, x, y);
+        out[1] = normH1(u, x, y);
+        out[2] = errorL2(u, x, y, f);
+        out[3] = errorH1(u, x, y, f);
+        out[4] = normL2(x, y, f);
+        out[5] = normH1(x, y, f);
+    }
+    void step() { }
+};
+
+int ref_norms(int ndim, int p, int elements, const double* u, double* out) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{1, 0.0};
+    if (ndim == 3) {
+        norms3_driver s{ads::config_3d{dim, dim, dim, steps, 1}};
+        s.norms(u, out);
+    } else if (ndim == 2) {
+        norms2_driver s{ads::config_2d{dim, dim, steps, 1}};
+        s.norms(u, out);
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+// examples/validation: the 2D heat problem with Dirichlet rows on all four
+// sides (fix_left/fix_right in x and y, boundary rows of the right-hand side
+// zeroed before every solve) from the projection of sin(pi x) sin(pi y),
+// against its exact solution e^{-2 pi^2 t} sin(pi x) sin(pi y).  Runs the
+// reference's own class: before(), then nsteps x (before_step, step); writes
+// the state and errorL2(T), errorH1(T) in percent of the exact solution's
+// norms (validation.hpp:121-129), T = nsteps dt.
+int ref_validation(int p, int elements, double dt, int nsteps, double* u_out, double* err_out) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{nsteps, dt};
+    ads::problems::validation s{ads::config_2d{dim, dim, steps, 1}};
+    s.before();
+    for (int i = 0; i < nsteps; ++i) {
+        s.before_step(i, i * dt);
+        s.step(i, i * dt);
+    }
+    store(s.u, u_out);
+    err_out[0] = s.errorL2(nsteps * dt);
+    err_out[1] = s.errorH1(nsteps * dt);
+    return 0;
+}
+
+// examples/heat/heat_2d: x.fix_left(), and before every solve row x = 0 of
+// the right-hand side replaced by the load vector of sin(pi y) on the y basis
+// (heat_2d.hpp:40-52).  Runs the reference's own class from its before()
+// state (the projection of init_state = 0, then that solve) through nsteps
+// steps; writes the state and the load vector it imposes (ny values).
+struct heat2d_open : ads::problems::heat_2d {
+    using heat_2d::heat_2d;
+    using simulation_2d::projection;
+    const ads::dimension& ydim() const { return y; }
+};
+
+int ref_heat2d_dirichlet(int p, int elements, double dt, int nsteps, double* u_out, double* row_out) {
+    ads::dim_config dim{p, elements};
+    ads::timesteps_config steps{nsteps, dt};
+    heat2d_open s{ads::config_2d{dim, dim, steps, 1}};
+    s.prepare_matrices();
+    s.projection(s.u, [&s](double x, double y) { return s.init_state(x, y); });
+    s.solve(s.u);
+    for (int i = 0; i < nsteps; ++i) {
+        s.before_step(i, i * dt);
+        s.step(i, i * dt);
+    }
+    store(s.u, u_out);
+    const ads::dimension& y = s.ydim();
+    ads::lin::vector buf{{y.dofs()}};
+    ads::compute_projection(buf, y.basis, [](double t) { return std::sin(t * M_PI); });
+    for (int i = 0; i < y.dofs(); ++i) row_out[i] = buf(i);
     return 0;
 }
 

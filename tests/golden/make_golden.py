@@ -12,6 +12,13 @@ ads_solve, lin::factorize/solve_with_factorized).  Initial fields are the
 reference's projection of prod sin(pi x_d) solved by its ads_solve, plus
 SplitMix64 noise (the same generator as ads_gb300.inputs.splitmix_uniform).
 
+The norms_* fixtures come from basic_simulation_2d/3d's normL2 / normH1 /
+errorL2 / errorH1 (include/ads/simulation/basic_simulation_3d.hpp:281-397);
+validation_2d_p2_e16 from the reference's examples/validation class (Dirichlet
+on every side, exact solution) and heat2d_dirichlet_p2_e32 from its
+examples/heat/heat_2d class (the Dirichlet row at x = 0), both run as they
+are (their file output stubbed out).
+
 The form_* fixtures come from the reference's scalability_3d::compute_rhs
 (examples/scalability/test3d.hpp:66-95) and flow::compute_rhs
 (examples/flow/flow.hpp:77-98, permeability from its own environment class),
@@ -345,6 +352,45 @@ def run_case(L, name, p, E, dt, nsteps, seed, nthreads):
     print("wrote", name, flush=True)
 
 
+def norms_case(L, nd, p, E, seed):
+    """The reference's normL2 / normH1 of a seeded spline and its errorL2 /
+    errorH1 against prod sin(pi x_d), plus the norms of that function
+    (basic_simulation_2d/3d's quadrature loops)."""
+    L.ref_norms.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
+    size = (E + p) ** nd
+    u = (2.0 * splitmix_uniform(seed, size) - 1.0)
+    out = np.zeros(6)
+    assert L.ref_norms(nd, p, E, dp(u), dp(out)) == 0
+    return dict(ndim=np.int32(nd), p=np.int32(p), elements=np.int32(E), seed=np.int64(seed), u=u, normL2=out[0],
+                normH1=out[1], errorL2=out[2], errorH1=out[3], f_normL2=out[4], f_normH1=out[5])
+
+
+NORM_CASES = [(2, 2, 9, 21), (3, 2, 6, 22), (3, 4, 5, 23), (2, 3, 11, 24)]
+
+
+def validation_case(L, p, E, dt, nsteps):
+    """The reference's validation example (Dirichlet on every side, exact
+    solution e^{-2 pi^2 t} sin(pi x) sin(pi y)) run for nsteps."""
+    L.ref_validation.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp]
+    u = np.zeros((E + p) ** 2)
+    err = np.zeros(2)
+    assert L.ref_validation(p, E, dt, nsteps, dp(u), dp(err)) == 0
+    return dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps), uN=u,
+                errorL2_percent=err[0], errorH1_percent=err[1])
+
+
+def heat2d_dirichlet_case(L, p, E, dt, nsteps):
+    """The reference's heat_2d example (row x = 0 held at the load vector of
+    sin(pi y), x.fix_left()) from its initial state through nsteps."""
+    L.ref_heat2d_dirichlet.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp]
+    u = np.zeros((E + p) ** 2)
+    row = np.zeros(E + p)
+    assert L.ref_heat2d_dirichlet(p, E, dt, nsteps, dp(u), dp(row)) == 0
+    u1 = np.zeros_like(u)
+    assert L.ref_heat2d_dirichlet(p, E, dt, 1, dp(u1), dp(row)) == 0
+    return dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps), u1=u1, uN=u, row=row)
+
+
 def main_runs(names, nthreads):
     L = load_ref()
     for name, p, E, dt, nsteps, seed in RUNS:
@@ -359,6 +405,11 @@ def main():
     for name, which, p, E, dt, seed in FORM_CASES:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **form_case(L, which, p, E, dt, seed))
         print("wrote", name)
+    for nd, p, E, seed in NORM_CASES:
+        np.savez_compressed(os.path.join(HERE, f"norms_{nd}d_p{p}_e{E}.npz"), **norms_case(L, nd, p, E, seed))
+    np.savez_compressed(os.path.join(HERE, "validation_2d_p2_e16.npz"), **validation_case(L, 2, 16, 1e-4, 500))
+    np.savez_compressed(os.path.join(HERE, "heat2d_dirichlet_p2_e32.npz"),
+                        **heat2d_dirichlet_case(L, 2, 32, 1e-5, 100))
     for p, E in [(2, 8), (3, 7), (4, 12), (2, 32), (4, 36)]:
         np.savez_compressed(os.path.join(HERE, f"tables_p{p}_e{E}.npz"), **tables(L, p, E))
     np.savez_compressed(os.path.join(HERE, "solver_known_answers.npz"), **known_answers(L))

@@ -1,10 +1,13 @@
 """Gauss-point utilities through the C-ABI: the L2 projection (load vector of
 reference include/ads/projection.hpp and projection + ads_solve), spline
 evaluation at the Gauss points, normL2 / normH1 and errorL2 / errorH1
-(reference include/ads/simulation/basic_simulation_3d.hpp:281-397)."""
+(reference include/ads/simulation/basic_simulation_3d.hpp:281-397), the last
+pinned to the reference's own loops through tests/golden/norms_*.npz."""
 from __future__ import annotations
 
+import glob
 import itertools
+import os
 
 import numpy as np
 import pytest
@@ -12,6 +15,7 @@ import pytest
 import ads_gb300 as ads
 import oracle
 from _tol import mass_condition
+from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
@@ -148,3 +152,27 @@ def test_projection_converges_to_the_function(cuda):
         errs.append(ctx.errors(u, f)[0])
     rates = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
     assert all(2.7 < r < 3.3 for r in rates), rates
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "norms_*.npz"))), ids=os.path.basename)
+def test_norms_and_errors_match_the_reference_loops(path, cuda):
+    """adsg_norms / adsg_errors against the reference's own normL2, normH1,
+    errorL2 and errorH1 (basic_simulation_2d/3d.hpp quadrature loops, run by
+    tests/golden/make_golden.py) on a seeded spline and prod sin(pi x_d)."""
+    import torch
+
+    g = np.load(path)
+    nd, p, E = int(g["ndim"]), int(g["p"]), int(g["elements"])
+    dims = [ads.Dimension(p, E) for _ in range(nd)]
+    ctx = ads.Context(dims)
+    u = torch.from_numpy(np.ascontiguousarray(g["u"])).cuda()
+    l2, h1 = ctx.norms(u)
+    fq, fg = _grid_values(ctx, _sin)
+    el2, eh1 = ctx.errors(u, torch.from_numpy(fq).cuda(), torch.from_numpy(fg).cuda())
+    nl2, nh1 = ctx.errors(torch.zeros_like(u), torch.from_numpy(fq).cuda(), torch.from_numpy(fg).cuda())
+    for name, got, ref in (("normL2", l2, g["normL2"]), ("normH1", h1, g["normH1"]), ("errorL2", el2, g["errorL2"]),
+                           ("errorH1", eh1, g["errorH1"]), ("f normL2", nl2, g["f_normL2"]),
+                           ("f normH1", nh1, g["f_normH1"])):
+        rel = abs(got - float(ref)) / float(ref)
+        print(f"[parity] {os.path.basename(path)} {name}: {got:.15e} vs reference {float(ref):.15e} (rel {rel:.1e})")
+        assert rel <= 1e-13, (name, got, float(ref))
