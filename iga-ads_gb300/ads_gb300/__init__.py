@@ -164,7 +164,7 @@ def library() -> ctypes.CDLL:
         "adsg_batch_synchronize": (i, [vp]),
         "adsg_batch_tuning": (i, [vp, _c_int_p, _c_int_p]),
         "adsg_batch_engine": (i, [vp]),
-        "adsg_batch_test_barrier": (i, [vp, i, ll]),
+        "adsg_batch_test_waits": (i, [vp, i, ll]),
         "adsg_debug_bounds": (i, [ctypes.POINTER(ll), _c_int_p, _c_int_p, ctypes.POINTER(ll), ctypes.POINTER(ll), i]),
         "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]),

@@ -2,8 +2,9 @@
 // degrees advanced together, by one of two engines chosen at creation by
 // timing both on the batch itself:
 //  - persistent: ONE cooperative launch per run of steps (all stages of all
-//    instances, grid barriers between stages), replayed from a CUDA graph,
-//    its grid size autotuned;
+//    instances as one sequence of work items taken from a counter, each
+//    instance's stages ordered by per-instance completion counts), replayed
+//    from a CUDA graph, its grid size autotuned;
 //  - concurrent: every instance has a plain context (its own tuned kernels:
 //    two-ended sweeps, pair sums, row-scaled step) on its own stream, and one
 //    step of all instances is a CUDA graph of independent per-instance
@@ -48,8 +49,6 @@ struct arena {
     }
 };
 
-constexpr int kUnitsPerItem = 256;
-
 }  // namespace
 
 struct adsg_batch {
@@ -91,9 +90,13 @@ struct adsg_batch {
 namespace {
 
 int launch_steps(adsg_batch* b, int nsteps, int blocks_per_sm) {
+    // completion counts and the work counter start at zero in every launch
+    cudaError_t e = cudaMemsetAsync(b->B.done, 0, sizeof(unsigned) * 6 * b->count, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->B.next, 0, sizeof(unsigned long long), b->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "reset the work counters");
     void* args[] = {&b->B, &nsteps, &b->par};
     const dim3 grid(b->sms * blocks_per_sm), block(256);
-    cudaError_t e = cudaLaunchCooperativeKernel(batch_kernel_symbol(), grid, block, args, 0, b->stream);
+    e = cudaLaunchCooperativeKernel(batch_kernel_symbol(), grid, block, args, batch_smem_bytes(), b->stream);
     if (e != cudaSuccess) return fail_cuda(e, "cooperative launch");
     return 0;
 }
@@ -105,9 +108,8 @@ int check_error_word(adsg_batch* b) {
     if (e != cudaSuccess) return fail_cuda(e, "batch synchronize");
     if (err) {
         cudaMemsetAsync(b->B.err, 0, sizeof(int), b->stream);
-        cudaMemsetAsync(b->B.bar_count, 0, sizeof(unsigned), b->stream);
         cudaStreamSynchronize(b->stream);
-        return fail(ADSG_ERR_DEVICE, "a grid barrier of the batched kernel timed out");
+        return fail(ADSG_ERR_DEVICE, "a wait of the batched kernel timed out");
     }
     return 0;
 }
@@ -229,7 +231,7 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return bail(fail(ADSG_ERR_UNSUPPORTED, "device lacks cooperative launch"));
 
-    std::vector<int> prefix(6 * (count + 1), 0);
+    if ((e = batch_prepare_kernel()) != cudaSuccess) return bail(fail_cuda(e, "batched kernel shared memory"));
     for (int i = 0; i < count; ++i) {
         dim_host& h = b->dims[i];
         if (!build_dimension(h, p[i], elements[i], 0.0, 1.0, p[i] + 1))
@@ -251,12 +253,30 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
         solve_tables t;
         if (make_solve_tables(h.n, h.kl, h.ku, h.ldab, h.lu.data(), h.ipiv.data(), t))
             return bail(fail(ADSG_ERR_SINGULAR, "zero pivot"));
-        std::vector<double> m = row_band(d, 0), k = row_band(d, 1), nr(m.size()), kd(m.size());
+        std::vector<double> m = row_band(d, 0), k = row_band(d, 1);
+        batch_inst& I = b->inst[i];
+        int sym_lo = 0, sym_hi = 0;
+        symmetric_row_range(m, k, h.n, h.p, sym_lo, sym_hi);
+        // two-ended unit-diagonal sweeps where the band allows them: the rows
+        // of every band are pre-multiplied by 1 / U(r, r) of the sweep
+        // (symmetric rows stay symmetric), as in a context's step view
+        twisted_tables tw, tu;
+        std::vector<double> scale;
+        I.twisted = make_twisted_tables(h.n, h.kl, h.ku, h.ldab, h.lu.data(), h.ipiv.data(), tw) == 0 ? 1 : 0;
+        if (I.twisted) {
+            scale_twisted(tw, h.n, tu, scale);
+            const int bw = 2 * h.p + 1;
+            for (int r = 0; r < h.n; ++r)
+                for (int c = 0; c < bw; ++c) {
+                    m[static_cast<size_t>(r) * bw + c] *= scale[r];
+                    k[static_cast<size_t>(r) * bw + c] *= scale[r];
+                }
+        }
+        std::vector<double> nr(m.size()), kd(m.size());
         for (size_t q = 0; q < m.size(); ++q) {
             nr[q] = std::fma(-dt[i], k[q], m[q]);
             kd[q] = -dt[i] * k[q];
         }
-        batch_inst& I = b->inst[i];
         I.ndim = ndim[i];
         I.p = p[i];
         I.n = h.n;
@@ -271,7 +291,10 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
         D.bwd_fast = t.bwd_fast;
         D.elements = h.elements;
         D.q = h.q;
+        D.sym_lo = sym_lo;
+        D.sym_hi = sym_hi;
         double *mrow, *krow, *nrow, *kdt, *lmul, *ucol, *rdiag;
+        double *tw_l = nullptr, *tw_u = nullptr, *tw_r = nullptr, *tw_g = nullptr;
         int *piv, *uext;
         arena& A = b->mem;
         cudaStream_t s = b->stream;
@@ -284,6 +307,12 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
         if (e == cudaSuccess) e = A.upload(&rdiag, t.rdiag.data(), t.rdiag.size(), s);
         if (e == cudaSuccess) e = A.upload(&piv, t.piv.data(), t.piv.size(), s);
         if (e == cudaSuccess) e = A.upload(&uext, t.uext.data(), t.uext.size(), s);
+        if (I.twisted) {
+            if (e == cudaSuccess) e = A.upload(&tw_l, tu.lmul.data(), tu.lmul.size(), s);
+            if (e == cudaSuccess) e = A.upload(&tw_u, tu.ucol.data(), tu.ucol.size(), s);
+            if (e == cudaSuccess) e = A.upload(&tw_r, tu.rdiag.data(), tu.rdiag.size(), s);
+            if (e == cudaSuccess) e = A.upload(&tw_g, tu.g.data(), tu.g.size(), s);
+        }
         if (e == cudaSuccess) e = A.alloc(&I.buf[0], I.size);
         if (e == cudaSuccess) e = A.alloc(&I.buf[1], I.size);
         for (int q = 0; q < (ndim[i] == 3 ? 4 : 2) && e == cudaSuccess; ++q) e = A.alloc(&I.T[q], I.size);
@@ -299,6 +328,17 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
         D.rdiag = rdiag;
         D.piv = piv;
         D.uext = uext;
+        if (I.twisted) {
+            D.tw_k = tu.k;
+            D.tw_n1 = tu.n1;
+            D.tw_n2 = tu.n2;
+            D.tw_rows = tu.rows;
+            D.tw_unit = 1;
+            D.tw_lmul = tw_l;
+            D.tw_ucol = tw_u;
+            D.tw_rdiag = tw_r;
+            D.tw_g = tw_g;
+        }
         const long long lines = I.size / I.n;
         if (I.ndim == 3) {
             const long long u[6] = {I.size, I.size, I.size, lines, lines, lines};
@@ -308,28 +348,35 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
             std::copy(u, u + 6, I.units);
         }
     }
+    // one step's items in stage-major order: prefix[stage * count + i]
+    std::vector<long long> prefix(6 * static_cast<size_t>(count) + 1, 0);
     for (int st = 0; st < 6; ++st)
         for (int i = 0; i < count; ++i) {
-            const long long items = (b->inst[i].units[st] + kUnitsPerItem - 1) / kUnitsPerItem;
-            prefix[st * (count + 1) + i + 1] = prefix[st * (count + 1) + i] + static_cast<int>(items);
+            batch_inst& I = b->inst[i];
+            const long long per = batch_units_per_item(st, I.twisted);
+            I.items[st] = static_cast<int>((I.units[st] + per - 1) / per);
+            const size_t k = static_cast<size_t>(st) * count + i;
+            prefix[k + 1] = prefix[k] + I.items[st];
         }
     batch_inst* dinst = nullptr;
-    int* dprefix = nullptr;
-    unsigned* bar = nullptr;
+    long long* dprefix = nullptr;
+    unsigned* done = nullptr;
+    unsigned long long* next = nullptr;
     int* err = nullptr;
     e = b->mem.upload(&dinst, b->inst.data(), b->inst.size(), b->stream);
     if (e == cudaSuccess) e = b->mem.upload(&dprefix, prefix.data(), prefix.size(), b->stream);
-    if (e == cudaSuccess) e = b->mem.alloc(&bar, 2);
+    if (e == cudaSuccess) e = b->mem.alloc(&done, 6 * static_cast<size_t>(count));
+    if (e == cudaSuccess) e = b->mem.alloc(&next, 1);
     if (e == cudaSuccess) e = b->mem.alloc(&err, 1);
-    if (e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
     b->B.count = count;
     b->B.inst = dinst;
     b->B.prefix = dprefix;
-    b->B.bar_count = bar;
-    b->B.bar_gen = bar + 1;
+    b->B.per_step = prefix.back();
+    b->B.done = done;
+    b->B.next = next;
     b->B.err = err;
 
     // autotune the persistent grid on the zero state (the state is reset after)
@@ -511,9 +558,9 @@ int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captur
 
 int adsg_batch_engine(const adsg_batch* b) { return b ? b->engine : -1; }
 
-int adsg_batch_test_barrier(adsg_batch* b, int extra_arrivals, long long spin_limit) {
+int adsg_batch_test_waits(adsg_batch* b, int extra_items, long long spin_limit) {
     if (!b) return fail(-1, "batch is NULL");
-    if (extra_arrivals < 0) return fail(-2, "extra_arrivals < 0");
+    if (extra_items < 0) return fail(-2, "extra_items < 0");
     if (spin_limit < 1) return fail(-3, "spin_limit < 1");
     if (b->stream) {
         cudaError_t e = cudaStreamSynchronize(b->stream);
@@ -525,7 +572,7 @@ int adsg_batch_test_barrier(adsg_batch* b, int extra_arrivals, long long spin_li
         b->graph = nullptr;
     }
     b->graph_steps = b->graph_par = -1;
-    b->B.barrier_extra = static_cast<unsigned>(extra_arrivals);
+    b->B.wait_extra = static_cast<unsigned>(extra_items);
     b->B.spin_limit = spin_limit;
     return 0;
 }

@@ -92,13 +92,16 @@ static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 // one-block small-grid step so that both perform the same operations in the
 // same order).  GIN: the inputs are in global memory (read through the
 // read-only path); otherwise in shared memory.
-template <bool GIN>
+template <int GIN>
 __device__ __forceinline__ double ldin(const double* p) {
-    if (GIN) return __ldg(p);
+    if (GIN == 2) return __ldcg(p);  // written earlier in the same launch (batched engine)
+    if (GIN == 1) return __ldg(p);
     return *p;
 }
 
-template <int P, bool IN1, bool OUT1, bool SYM, bool GIN>
+// GIN: 0 inputs in shared memory, 1 in global memory (read-only path), 2 in
+// global memory written earlier in the same launch (L2 loads).
+template <int P, bool IN1, bool OUT1, bool SYM, int GIN>
 __device__ __forceinline__ void band_out(long long g, const double* in0, const double* in1, double* out0,
                                          double* out1, const double* __restrict__ A0,
                                          const double* __restrict__ A1, const double* __restrict__ B0, int n_axis,
@@ -889,14 +892,16 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // (pays where the line is a shared-memory tile: 28.5 -> 26.8 us for the x
 // sweep at 130^3, 312 -> 303 us at 260^3 p=4; costs the global-memory sweep
 // its occupancy at p = 4: 245 -> 257 us).
-template <int K, int UNR, bool UNIT, bool TAIL = false>
+// CG: read the line through L2 (it was written by other blocks earlier in
+// the same launch: the batched engine).
+template <int K, int UNR, bool UNIT, bool TAIL = false, bool CG = false>
 __device__ __forceinline__ void twisted_chain(double* __restrict__ x, double* __restrict__ xo, const long long es,
                                               const int nc, const double* __restrict__ lmul,
                                               const double* __restrict__ ucol, const double* __restrict__ rdiag,
                                               const double* __restrict__ G, const unsigned mask) {
     auto ld = [&](int r) -> double {
         if (r < 0 || r >= nc) return 0.0;
-        return x[r * es];
+        return CG ? __ldcg(x + r * es) : x[r * es];
     };
     // ---- forward (unit lower factor, no row exchanges) ----
     double f[K + 1];
@@ -961,7 +966,7 @@ __device__ __forceinline__ void twisted_chain(double* __restrict__ x, double* __
     // ---- meeting point ----
     double own[K], oth[K], z[K];
 #pragma unroll
-    for (int i = 0; i < K; ++i) own[i] = TAIL ? tail[TAIL ? 1 + i : 0] : x[(nc - K + i) * es];  // rows nc-K .. nc-1
+    for (int i = 0; i < K; ++i) own[i] = TAIL ? tail[TAIL ? 1 + i : 0] : ld(nc - K + i);  // rows nc-K .. nc-1
 #pragma unroll
     for (int i = 0; i < K; ++i) oth[i] = __shfl_xor_sync(mask, own[i], 16);
 #pragma unroll
@@ -1160,13 +1165,17 @@ __device__ __forceinline__ long long chunk_offset(const chunk_lines& W, int line
 // buf[c][l][t] <- chain-local row (first[c] + dir * t) of line l, chain c
 // (0 outside the chain); dir = +1 (forward) or -1 (backward).  (Plain loads:
 // asynchronous copies measured slower here, unlike in the whole-line tile.)
+template <bool CG = false>
 __device__ __forceinline__ void chunk_stage(double* buf, const chunk_lines& W, const int first[2], int dir) {
     const int lane = threadIdx.x & 31;
     for (int idx = lane; idx < 2 * 16 * kChunk; idx += 32) {
         const int c = idx / (16 * kChunk), l = (idx / kChunk) % 16, t = idx % kChunk;
         const int r = first[c] + dir * t, nc = c ? W.n2 : W.n1;
         double v = 0.0;
-        if (l < W.nv && r >= 0 && r < nc) v = W.data[chunk_offset(W, l, c, r)];
+        if (l < W.nv && r >= 0 && r < nc) {
+            const double* src = W.data + chunk_offset(W, l, c, r);
+            v = CG ? __ldcg(src) : *src;
+        }
         buf[(c * 16 + l) * kChunkPitch + t] = v;
     }
 }
@@ -1180,25 +1189,13 @@ __device__ __forceinline__ void chunk_flush(const double* buf, const chunk_lines
     }
 }
 
-template <int K, bool UNIT>
-__global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double* __restrict__ data, dim_dev D,
-                                                                         line_layout L) {
-    extern __shared__ double smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4, line = lane & 15;
-    const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
-    if (g0 >= L.nlines) return;  // whole warp
-    pdl_wait();
-    chunk_lines W;
-    W.data = data + g0 * D.n;
-    W.n = D.n;
-    W.n1 = D.tw_n1;
-    W.n2 = D.tw_n2;
-    W.nv = static_cast<int>(min(16LL, L.nlines - g0));
-    double* buf = smem + static_cast<size_t>(warp) * 2 * 16 * kChunkPitch;
-    // bounds-checked build: the warp's buffer and its 16 lines (warp-uniform)
-    if (!(ADSG_SMEM_RANGE(buf, 2LL * 16 * kChunkPitch) && ADSG_IN(g0 * D.n, L.total) &&
-          ADSG_IN((g0 + W.nv) * D.n - 1, L.total)))
-        return;
+// The body of the chunked two-ended sweep for one warp: W.nv (<= 16) contiguous
+// lines starting at W.data, lanes 0-15 chain 0 and 16-31 chain 1 of line
+// lane & 15, buf this warp's 2 x 16 x kChunkPitch shared slots.  CG: the lines
+// were written by other blocks earlier in the same launch.
+template <int K, bool UNIT, bool CG = false>
+__device__ __forceinline__ void chunked_twisted_warp(const chunk_lines& W, const dim_dev& D, double* buf) {
+    const int lane = threadIdx.x & 31, chain = lane >> 4, line = lane & 15;
     double* mine = buf + (chain * 16 + line) * kChunkPitch;  // this lane's slots
     const bool active = line < W.nv;  // every lane stays to the end: the staging is warp-wide
     const int nc = chain ? W.n2 : W.n1, nmax = max(W.n1, W.n2);
@@ -1207,7 +1204,11 @@ __global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double*
     const double* ucol = D.tw_ucol + off * K;
     const double* rdiag = D.tw_rdiag + off;
     const double* G = D.tw_g + chain * 2 * K * K;
-    auto ld = [&](int r) -> double { return (active && r >= 0 && r < nc) ? W.data[chunk_offset(W, line, chain, r)] : 0.0; };
+    auto ld = [&](int r) -> double {
+        if (!(active && r >= 0 && r < nc)) return 0.0;
+        const double* src = W.data + chunk_offset(W, line, chain, r);
+        return CG ? __ldcg(src) : *src;
+    };
 
     // ---- forward: rows j0 .. j0+kChunk-1 read rows j+K+1 from the chunk ----
     double f[K + 1];
@@ -1219,7 +1220,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double*
     for (int j0 = 0; j0 < nmax; j0 += kChunk) {
         const int first[2] = {j0 + K + 1, j0 + K + 1};
         __syncwarp();
-        chunk_stage(buf, W, first, +1);
+        chunk_stage<CG>(buf, W, first, +1);
         __syncwarp();
         if (active) {
             const int tend = min(kChunk, nc - j0);
@@ -1281,7 +1282,7 @@ __global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double*
     for (int s = 0; s < steps; ++s) {
         const int in_first[2] = {chi0[0] - s * kChunk - K - 1, chi0[1] - s * kChunk - K - 1};
         __syncwarp();
-        chunk_stage(buf, W, in_first, -1);
+        chunk_stage<CG>(buf, W, in_first, -1);
         __syncwarp();
         if (active) {
             const int chi = chi0[chain] - s * kChunk;
@@ -1303,6 +1304,29 @@ __global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double*
         const int out_first[2] = {chi0[0] - s * kChunk, chi0[1] - s * kChunk};
         chunk_flush(buf, W, out_first, -1);
     }
+}
+
+
+template <int K, bool UNIT>
+__global__ void __launch_bounds__(128) line_solve_twisted_chunked_kernel(double* __restrict__ data, dim_dev D,
+                                                                         line_layout L) {
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4, line = lane & 15;
+    const long long g0 = (static_cast<long long>(blockIdx.x) * (blockDim.x >> 5) + warp) * 16;
+    if (g0 >= L.nlines) return;  // whole warp
+    pdl_wait();
+    chunk_lines W;
+    W.data = data + g0 * D.n;
+    W.n = D.n;
+    W.n1 = D.tw_n1;
+    W.n2 = D.tw_n2;
+    W.nv = static_cast<int>(min(16LL, L.nlines - g0));
+    double* buf = smem + static_cast<size_t>(warp) * 2 * 16 * kChunkPitch;
+    // bounds-checked build: the warp's buffer and its 16 lines (warp-uniform)
+    if (!(ADSG_SMEM_RANGE(buf, 2LL * 16 * kChunkPitch) && ADSG_IN(g0 * D.n, L.total) &&
+          ADSG_IN((g0 + W.nv) * D.n - 1, L.total)))
+        return;
+    chunked_twisted_warp<K, UNIT>(W, D, buf);
 }
 
 size_t twisted_chunked_smem_per_warp() { return sizeof(double) * 2 * 16 * kChunkPitch; }
@@ -1861,141 +1885,224 @@ cudaError_t launch_dot(const double* x, const double* y, long long n, double* pa
 
 // ---------------------------------------------------------------------------
 // Batched engine: many independent cubic heat problems (2D or 3D, p <= 4)
-// advanced by one persistent cooperative launch.  A step is six stages (RHS
-// passes outer / middle / x, then the x, y, z line solves); every stage's work
-// is cut into items of 256 units (outputs for a pass, lines for a solve) over
-// all instances, blocks take items round-robin, and a grid barrier separates
-// the stages.  Inputs written earlier in the same launch are read with
-// L1-bypassing loads.
+// advanced by one persistent cooperative launch.  A step is six stages per
+// instance (RHS passes outer / middle / x, then the x, y, z line solves).
+// The work of every stage of every instance is cut into items (2048 outputs
+// of a pass; 128 lines of a two-ended solve, 256 of a LAPACK-order one), and
+// the items of all steps, stages and instances form one sequence (step-major,
+// then stage, then instance).  Blocks take the next item from a global
+// counter; before working on it they wait until the same instance has
+// finished its previous stage (a per-instance, per-stage count of completed
+// items), so each instance runs its stages in order while the instances
+// overlap freely -- no grid-wide barrier, no stage waits for the slowest
+// instance.  Items are handed out in sequence order and every dependency lies
+// earlier in the sequence, so with all blocks resident (cooperative launch)
+// the earliest unfinished item can always proceed.  Waits are bounded: past
+// the spin limit a block sets the error word and the launch winds down.
+// The kernels are those of the single-instance step: pair-sum band passes,
+// row-scaled right-hand sides and unit-diagonal two-ended sweeps (chunked
+// through shared memory on the contiguous x-lines), reading data written
+// earlier in the launch through L2.
 // ---------------------------------------------------------------------------
 namespace {
 
-template <int P>
-__device__ __forceinline__ void band_one_cg(long long g, const double* in0, const double* in1, double* out0, double* out1,
-                                            const double* A0, const double* A1, const double* B0, int n_axis,
-                                            long long stride, long long total) {
-    constexpr int BW = 2 * P + 1;
-    const int r = static_cast<int>((g / stride) % n_axis);
-    // bounds-checked build: the output and the rows the band reaches inside
-    // the instance's tensors of `total` doubles
-    if (!(ADSG_IN(g, total) && ADSG_IN(g - static_cast<long long>(min(r, P)) * stride, total) &&
-          ADSG_IN(g + static_cast<long long>(min(n_axis - 1 - r, P)) * stride, total)))
-        return;
-    const double* a0 = A0 + static_cast<long long>(r) * BW;
-    double acc0 = 0.0, acc1 = 0.0;
-#pragma unroll
-    for (int t = 0; t < BW; ++t) {
-        const int c = r - P + t;
-        if (c >= 0 && c < n_axis) {
-            const long long at = g + static_cast<long long>(t - P) * stride;
-            const double v0 = __ldcg(in0 + at);
-            acc0 = fma(__ldg(a0 + t), v0, acc0);
-            if (out1) acc1 = fma(__ldg(B0 + static_cast<long long>(r) * BW + t), v0, acc1);
-            if (in1) acc0 = fma(__ldg(A1 + static_cast<long long>(r) * BW + t), __ldcg(in1 + at), acc0);
-        }
-    }
-    out0[g] = acc0;
-    if (out1) out1[g] = acc1;
-}
+constexpr int kBatchPassUnits = 2048, kBatchTwistedLines = 128, kBatchLapackLines = 256;
 
 template <int P>
-__device__ __forceinline__ void batch_unit(const batch_inst& I, int stage, long long u, int par) {
+__device__ __forceinline__ void batch_pass(const batch_inst& I, int stage, long long first, int par) {
     const double* cur = I.buf[par];
     double* nxt = I.buf[par ^ 1];
     const int n = I.n;
     const dim_dev& D = I.dim;
     const long long nn = static_cast<long long>(n) * n;
-    if (I.ndim == 3) {
-        switch (stage) {
-            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn, I.size); return;
-            case 1: band_one_cg<P>(u, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n, I.size); return;
-            case 2: band_one_cg<P>(u, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, I.size); return;
-            case 3:
-                if (ADSG_LINE_OK(nxt, nxt + u * n, n, 1, I.size))
-                    sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D);
-                return;
-            case 4:
-                if (ADSG_LINE_OK(nxt, nxt + (u % n) + (u / n) * nn, n, n, I.size))
-                    sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + (u % n) + (u / n) * nn, n, D);
-                return;
-            default:
-                if (ADSG_LINE_OK(nxt, nxt + u, n, nn, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, nn, D);
-                return;
-        }
-    } else {
-        switch (stage) {
-            case 0: band_one_cg<P>(u, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n, I.size); return;
-            case 2: band_one_cg<P>(u, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, I.size); return;
-            case 3:
-                if (ADSG_LINE_OK(nxt, nxt + u * n, n, 1, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u * n, 1, D);
-                return;
-            case 4:
-                if (ADSG_LINE_OK(nxt, nxt + u, n, n, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(nxt + u, n, D);
-                return;
-            default: return;
+    const int lo = max(D.sym_lo, P), hi = min(D.sym_hi, n - P);
+    const bool sym = hi > lo;
+#pragma unroll 1
+    for (int k = 0; k < kBatchPassUnits / 256; ++k) {
+        const long long g = first + k * 256 + threadIdx.x;
+        if (g >= I.size) return;
+        if (I.ndim == 3) {
+            if (stage == 0) {
+                if (sym)
+                    band_out<P, false, true, true, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn,
+                                                      lo, hi, I.size);
+                else
+                    band_out<P, false, true, false, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn,
+                                                       0, 0, I.size);
+            } else if (stage == 1) {
+                if (sym)
+                    band_out<P, true, true, true, 2>(g, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n, lo,
+                                                     hi, I.size);
+                else
+                    band_out<P, true, true, false, 2>(g, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n, 0,
+                                                      0, I.size);
+            } else {
+                band_out<P, true, false, false, 2>(g, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, 0, 0,
+                                                   I.size);
+            }
+        } else {
+            if (stage == 0) {
+                if (sym)
+                    band_out<P, false, true, true, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n,
+                                                      lo, hi, I.size);
+                else
+                    band_out<P, false, true, false, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n,
+                                                       0, 0, I.size);
+            } else {
+                band_out<P, true, false, false, 2>(g, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, 0, 0,
+                                                   I.size);
+            }
         }
     }
 }
 
-// Grid barrier with a bounded wait: thread 0 of each block arrives on a
-// counter; the last arrival resets it and advances the generation; the
-// others poll the generation with a spin limit, after which they set the
-// error word and the kernel winds down instead of waiting forever.
-__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err, unsigned nblocks,
-                                             long long spin_limit) {
-    __syncthreads();
-    __shared__ int ok;
-    if (threadIdx.x == 0) {
-        ok = 1;
-        const unsigned g = atomicAdd(gen, 0u);
-        __threadfence();
-        const unsigned arrived = atomicAdd(count, 1u) + 1u;
-        if (arrived == nblocks) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            long long spins = 0;
-            while (atomicAdd(gen, 0u) == g) {
-                if (++spins > spin_limit || atomicAdd(reinterpret_cast<unsigned*>(err), 0u) != 0u) {
-                    atomicExch(err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
+// Where line g of direction dir (0 x, 1 y, 2 z) of an instance starts, and
+// its element stride.
+__device__ __forceinline__ long long batch_line(const batch_inst& I, int dir, long long g, long long* es) {
+    const long long n = I.n, nn = n * n;
+    if (dir == 0) {
+        *es = 1;
+        return g * n;
     }
-    __syncthreads();
-    return ok != 0;
+    if (dir == 1) {
+        *es = n;
+        return I.ndim == 3 ? (g % n) + (g / n) * nn : g;
+    }
+    *es = nn;
+    return g;
+}
+
+// Two-ended unit-diagonal sweeps of 128 lines: 8 warps x 16 lines.
+template <int K>
+__device__ __forceinline__ void batch_solve_twisted(const batch_inst& I, int stage, long long first, int par,
+                                                    double* wbuf) {
+    double* x = I.buf[par ^ 1];
+    const dim_dev& D = I.dim;
+    const int n = I.n, dir = stage - 3;
+    const long long lines = I.units[stage];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long g0 = first + static_cast<long long>(warp) * 16;
+    if (g0 >= lines) return;  // whole warp
+    if (dir == 0) {
+        // contiguous x-lines: streamed through this warp's shared chunk buffer
+        chunk_lines W;
+        W.data = x + g0 * n;
+        W.n = n;
+        W.n1 = D.tw_n1;
+        W.n2 = D.tw_n2;
+        W.nv = static_cast<int>(min(16LL, lines - g0));
+        if (!(ADSG_SMEM_RANGE(wbuf, 2LL * 16 * kChunkPitch) && ADSG_IN(g0 * n, I.size) &&
+              ADSG_IN((g0 + W.nv) * n - 1, I.size)))
+            return;
+        chunked_twisted_warp<K, true, true>(W, D, wbuf);
+        return;
+    }
+    const int chain = lane >> 4;
+    const long long g = g0 + (lane & 15);
+    long long es = 1;
+    double* xl = x + batch_line(I, dir, g < lines ? g : 0, &es);
+    const bool active = g < lines && ADSG_LINE_OK(x, xl, n, es, I.size);
+    const unsigned mask = __ballot_sync(0xffffffffu, active);  // lanes g and g^16 share a line
+    if (!active) return;
+    const long long off = static_cast<long long>(chain) * D.tw_rows;
+    if (chain) xl += static_cast<long long>(n - 1) * es;
+    twisted_chain<K, (K > 2 ? 4 : 8), true, false, true>(xl, xl, chain ? -es : es, chain ? D.tw_n2 : D.tw_n1,
+                                                         D.tw_lmul + off * K, D.tw_ucol + off * K, D.tw_rdiag + off,
+                                                         D.tw_g + chain * 2 * K * K, mask);
+}
+
+// LAPACK-order sweeps (instances without two-ended tables): one line per thread.
+template <int P>
+__device__ __forceinline__ void batch_solve_lapack(const batch_inst& I, int stage, long long g, int par) {
+    if (g >= I.units[stage]) return;
+    double* x = I.buf[par ^ 1];
+    long long es = 1;
+    double* xl = x + batch_line(I, stage - 3, g, &es);
+    if (ADSG_LINE_OK(x, xl, I.n, es, I.size)) sweep_global<P, P, (P > 2 ? 4 : 8), true>(xl, es, I.dim);
+}
+
+// Thread 0: wait until instance i has finished the stage before (stage, step
+// t) -- the nearest earlier stage with work, in this step or the last.
+// Returns 0 when the wait ran out (or another block's did): the error word is
+// set and the launch winds down.
+__device__ __noinline__ int batch_wait(const batch_dev& B, const batch_inst& I, int i, int stage, int t) {
+    int ps = stage, pt = t;
+    do {
+        if (ps == 0) {
+            if (pt == 0) return 1;  // the launch's first stage of this instance
+            ps = 5;
+            --pt;
+        } else {
+            --ps;
+        }
+    } while (I.items[ps] == 0);
+    const unsigned target = static_cast<unsigned>((pt + 1) * I.items[ps]) + B.wait_extra;
+    const volatile unsigned* c = B.done + i * 6 + ps;
+    long long spins = 0;
+    while (*c < target) {
+        if (++spins > B.spin_limit || *reinterpret_cast<volatile int*>(B.err) != 0) {
+            atomicExch(B.err, 1);
+            return 0;
+        }
+        __nanosleep(64);
+    }
+    __threadfence();
+    return 1;
 }
 
 __global__ void __launch_bounds__(256) batch_steps_kernel(batch_dev B, int nsteps, int par0) {
-    const unsigned nblocks = gridDim.x;
-    for (int step = 0; step < nsteps; ++step) {
-        const int par = (par0 + step) & 1;
-        for (int stage = 0; stage < 6; ++stage) {
-            const int* pre = B.prefix + stage * (B.count + 1);
-            const int total = pre[B.count];
-            for (int item = blockIdx.x; item < total; item += nblocks) {
-                int lo = 0, hi = B.count;  // find i with pre[i] <= item < pre[i+1]
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (pre[mid] <= item) lo = mid; else hi = mid;
-                }
-                const batch_inst& I = B.inst[lo];
-                const long long u = static_cast<long long>(item - pre[lo]) * 256 + threadIdx.x;
-                if (u < I.units[stage]) {
-                    switch (I.p) {
-                        case 1: batch_unit<1>(I, stage, u, par); break;
-                        case 2: batch_unit<2>(I, stage, u, par); break;
-                        case 3: batch_unit<3>(I, stage, u, par); break;
-                        default: batch_unit<4>(I, stage, u, par); break;
-                    }
-                }
+    extern __shared__ double smem[];  // per warp: 2 x 16 x kChunkPitch doubles for the x-lines
+    __shared__ long long s_item;
+    __shared__ int s_go;
+    double* wbuf = smem + static_cast<size_t>(threadIdx.x >> 5) * 2 * 16 * kChunkPitch;
+    const long long total = static_cast<long long>(nsteps) * B.per_step;
+    const int pairs = 6 * B.count;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = static_cast<long long>(atomicAdd(B.next, 1ULL));
+        __syncthreads();
+        const long long item = s_item;
+        if (item >= total) return;
+        const int t = static_cast<int>(item / B.per_step);
+        const long long r = item - static_cast<long long>(t) * B.per_step;
+        int lo = 0, hi = pairs;  // (stage, instance) pair k with prefix[k] <= r < prefix[k+1]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (B.prefix[mid] <= r) lo = mid; else hi = mid;
+        }
+        const int stage = lo / B.count, i = lo - stage * B.count;
+        const batch_inst& I = B.inst[i];
+        const long long it = r - B.prefix[lo];
+        if (threadIdx.x == 0) s_go = batch_wait(B, I, i, stage, t);
+        __syncthreads();
+        if (!s_go) return;
+        const int par = (par0 + t) & 1;
+        if (stage < 3) {
+            switch (I.p) {
+                case 1: batch_pass<1>(I, stage, it * kBatchPassUnits, par); break;
+                case 2: batch_pass<2>(I, stage, it * kBatchPassUnits, par); break;
+                case 3: batch_pass<3>(I, stage, it * kBatchPassUnits, par); break;
+                default: batch_pass<4>(I, stage, it * kBatchPassUnits, par); break;
             }
-            if (!grid_barrier(B.bar_count, B.bar_gen, B.err, nblocks + B.barrier_extra, B.spin_limit)) return;
+        } else if (I.twisted) {
+            switch (I.p) {
+                case 1: batch_solve_twisted<1>(I, stage, it * kBatchTwistedLines, par, wbuf); break;
+                case 2: batch_solve_twisted<2>(I, stage, it * kBatchTwistedLines, par, wbuf); break;
+                case 3: batch_solve_twisted<3>(I, stage, it * kBatchTwistedLines, par, wbuf); break;
+                default: batch_solve_twisted<4>(I, stage, it * kBatchTwistedLines, par, wbuf); break;
+            }
+        } else {
+            const long long g = it * kBatchLapackLines + threadIdx.x;
+            switch (I.p) {
+                case 1: batch_solve_lapack<1>(I, stage, g, par); break;
+                case 2: batch_solve_lapack<2>(I, stage, g, par); break;
+                case 3: batch_solve_lapack<3>(I, stage, g, par); break;
+                default: batch_solve_lapack<4>(I, stage, g, par); break;
+            }
+        }
+        __syncthreads();  // every thread's writes of the item precede its completion count
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(B.done + i * 6 + stage, 1u);
         }
     }
 }
@@ -2004,9 +2111,20 @@ __global__ void __launch_bounds__(256) batch_steps_kernel(batch_dev B, int nstep
 
 const void* batch_kernel_symbol() { return reinterpret_cast<const void*>(batch_steps_kernel); }
 
+size_t batch_smem_bytes() { return sizeof(double) * 8 * 2 * 16 * kChunkPitch; }
+
+int batch_units_per_item(int stage, int twisted) {
+    return stage < 3 ? kBatchPassUnits : (twisted ? kBatchTwistedLines : kBatchLapackLines);
+}
+
+cudaError_t batch_prepare_kernel() {
+    return ensure_smem_attribute(batch_kernel_symbol(), batch_smem_bytes());
+}
+
 int batch_max_blocks_per_sm() {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_steps_kernel, 256, 0);
+    if (batch_prepare_kernel() != cudaSuccess) return 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_steps_kernel, 256, batch_smem_bytes());
     return nb;
 }
 

@@ -99,8 +99,10 @@ cudaError_t launch_line_solve_permat(double* data, const line_tables& T, const l
 // One instance of the batched engine (cubic: the same dimension in every direction).
 struct batch_inst {
     int ndim = 0, p = 0, n = 0;
+    int twisted = 0;  // 1: row-scaled bands and unit two-ended tables in dim; 0: LAPACK-order sweeps
     long long size = 0;
     long long units[6] = {};  // outputs (passes) or lines (solves) per stage; 0 = no work
+    int items[6] = {};        // work items per stage (batch_units_per_item units each)
     double* buf[2] = {nullptr, nullptr};
     double* T[4] = {nullptr, nullptr, nullptr, nullptr};
     dim_dev dim;
@@ -109,20 +111,24 @@ struct batch_inst {
 struct batch_dev {
     int count = 0;
     const batch_inst* inst = nullptr;  // device array [count]
-    const int* prefix = nullptr;       // device array [6][count+1]: items (256 units) before instance i
-    unsigned* bar_count = nullptr;
-    unsigned* bar_gen = nullptr;
+    const long long* prefix = nullptr;  // device array [6 count + 1]: items of one step before (stage, instance)
+    long long per_step = 0;             // items of one step
+    unsigned* done = nullptr;           // device array [count][6]: items completed in this launch
+    unsigned long long* next = nullptr;  // the work counter (zeroed before each launch)
     int* err = nullptr;
-    // bounded wait of the grid barrier: polls of the generation before a
-    // waiting block gives up (sets *err and winds down)
+    // bounded wait: polls of a completion count before a waiting block gives
+    // up (sets *err and winds down)
     long long spin_limit = 1LL << 26;
-    // test hook (failure detection): arrivals the barrier expects beyond the
-    // blocks launched; nonzero makes every wait run out
-    unsigned barrier_extra = 0;
+    // test hook (failure detection): items every wait expects beyond those
+    // that exist; nonzero makes every wait run out
+    unsigned wait_extra = 0;
 };
 
 const void* batch_kernel_symbol();
 int batch_max_blocks_per_sm();
+size_t batch_smem_bytes();
+int batch_units_per_item(int stage, int twisted);
+cudaError_t batch_prepare_kernel();
 
 // rhs passes -------------------------------------------------------------
 // out0 = A0 (.) in0 [+ A1 (.) in1],  out1 = B0 (.) in0  along one axis, where

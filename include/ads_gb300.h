@@ -369,8 +369,9 @@ int adsg_mass_loss(adsg_ctx* ctx, const double* u_dev, const double* target_dev,
  * elements and degree in every direction), 1 <= p <= 4, its own dt, open
  * uniform knots on [0,1] -- advance together.  adsg_batch_steps runs nsteps
  * of every instance as ONE persistent cooperative launch (all RHS passes and
- * line solves of all instances, grid barriers with bounded waits between
- * stages), replayed from a CUDA graph; the grid size is chosen at creation by
+ * line solves of all instances as work items taken in order from a counter,
+ * each instance's stages ordered by bounded waits on its own completion
+ * counts), replayed from a CUDA graph; the grid size is chosen at creation by
  * timing every feasible blocks-per-SM count on the batch.  States start at
  * zero.  adsg_batch_steps_looped advances the same states with the plain
  * per-instance entry points (adsg_heat_rhs + adsg_ads_solve per instance and
@@ -384,23 +385,25 @@ int adsg_batch_set_state(adsg_batch* b, int i, const double* u_host);  /* synchr
 int adsg_batch_get_state(adsg_batch* b, int i, double* u_host);        /* synchronises */
 int adsg_batch_steps(adsg_batch* b, int nsteps);
 int adsg_batch_steps_looped(adsg_batch* b, int nsteps);
-/* Waits for the batch's work; ADSG_ERR_DEVICE if a grid barrier timed out. */
+/* Waits for the batch's work; ADSG_ERR_DEVICE if a wait of the persistent kernel timed out. */
 int adsg_batch_synchronize(adsg_batch* b);
 /* Autotuned blocks per SM and whether the launch is replayed from a graph. */
 int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captured);
 /* The engine the batch chose at creation by timing both on itself: 0 the
- * persistent cooperative kernel (grid barriers between stages), 1 a CUDA
- * graph of independent per-instance chains (each instance's own tuned step
- * kernels, run side by side); -1 for a NULL batch.  ADSG_BATCH_ENGINE=0/1
- * forces it. */
+ * persistent cooperative kernel (one launch per call: every stage of every
+ * instance as a sequence of work items taken from a counter, each instance's
+ * stages ordered by its own completion counts), 1 a CUDA graph of independent
+ * per-instance chains (each instance's own tuned step kernels, run side by
+ * side); -1 for a NULL batch.  ADSG_BATCH_ENGINE=0/1 forces it. */
 int adsg_batch_engine(const adsg_batch* b);
-/* Test hook for failure detection (no reference counterpart): the persistent
- * kernel's grid barriers expect extra_arrivals blocks beyond those launched
- * (nonzero: no barrier can complete) and a waiting block gives up after
- * spin_limit polls, sets the batch's error word and the kernel winds down.
+/* Test hook for failure detection (no reference counterpart): every wait of
+ * the persistent kernel for an instance's previous stage expects
+ * extra_items completed work items beyond those that exist (nonzero: no
+ * such wait can end) and a waiting block gives up after spin_limit polls,
+ * sets the batch's error word and the kernel winds down.
  * The next adsg_batch_synchronize returns ADSG_ERR_DEVICE and clears the
- * word; adsg_batch_test_barrier(b, 0, 1 << 26) restores the defaults. */
-int adsg_batch_test_barrier(adsg_batch* b, int extra_arrivals, long long spin_limit);
+ * word; adsg_batch_test_waits(b, 0, 1 << 26) restores the defaults. */
+int adsg_batch_test_waits(adsg_batch* b, int extra_items, long long spin_limit);
 
 /* ---- debug build: device-side bounds checks ----------------------------------
  * No reference counterpart (the reference's debug builds assert in

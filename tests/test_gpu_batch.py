@@ -94,13 +94,13 @@ def test_batch_rejects_bad_specs():
         ads.Batch([(3, 5, 8, 1e-6)])
 
 
-def test_grid_barrier_wait_runs_out_and_the_batch_recovers(cuda, monkeypatch):
-    """Failure detection without a fault: the persistent kernel's grid barrier
-    is told to expect one block more than was launched, with a spin limit of
-    a few thousand polls, so every wait runs out; each waiting block sets the
-    error word and returns.  adsg_batch_synchronize reports ADSG_ERR_DEVICE
-    (and clears the word), and with the defaults back the next call runs the
-    steps correctly."""
+def test_persistent_kernel_wait_runs_out_and_the_batch_recovers(cuda, monkeypatch):
+    """Failure detection without a fault: every wait of the persistent kernel
+    for an instance's previous stage is told to expect one work item more
+    than exists, with a spin limit of a few thousand polls, so every wait runs
+    out; each waiting block sets the error word and returns.
+    adsg_batch_synchronize reports ADSG_ERR_DEVICE (and clears the word), and
+    with the defaults back the next call runs the steps correctly."""
     import ctypes
 
     monkeypatch.setenv("ADSG_BATCH_ENGINE", "0")
@@ -111,22 +111,22 @@ def test_grid_barrier_wait_runs_out_and_the_batch_recovers(cuda, monkeypatch):
     u0 = [rng.uniform(-1, 1, n) for n in b.sizes]
     for i, u in enumerate(u0):
         b.set_state(i, u)
-    assert lib.adsg_batch_test_barrier(b._h, 1, 4000) == 0
+    assert lib.adsg_batch_test_waits(b._h, 1, 4000) == 0
     code = lib.adsg_batch_steps(b._h, 2)
     if code == 0:
         code = lib.adsg_batch_synchronize(b._h)
     assert code == 1004, code  # ADSG_ERR_DEVICE
     assert b"timed out" in lib.adsg_last_error()
-    assert lib.adsg_batch_test_barrier(b._h, 0, 1 << 26) == 0
+    assert lib.adsg_batch_test_waits(b._h, 0, 1 << 26) == 0
     for i, u in enumerate(u0):
         b.set_state(i, u)
     b.steps(2)
     b.synchronize()
     for i, (nd, p, e, dt) in enumerate(SMALL[:3]):
         pr = oracle.Problem([p] * nd, [e] * nd)
-        check(f"after a barrier timeout {SMALL[i]} 2 steps", oracle.rel_l2(b.get_state(i), pr.heat_steps(u0[i], dt, 2)),
+        check(f"after a wait timeout {SMALL[i]} 2 steps", oracle.rel_l2(b.get_state(i), pr.heat_steps(u0[i], dt, 2)),
               2 * STEP, oracle_self(pr, u0[i], dt, 2))
-    assert lib.adsg_batch_test_barrier(None, 0, 1) == -1
-    assert lib.adsg_batch_test_barrier(b._h, -1, 1) == -2
-    assert lib.adsg_batch_test_barrier(b._h, 0, 0) == -3
+    assert lib.adsg_batch_test_waits(None, 0, 1) == -1
+    assert lib.adsg_batch_test_waits(b._h, -1, 1) == -2
+    assert lib.adsg_batch_test_waits(b._h, 0, 0) == -3
     del ctypes
