@@ -186,7 +186,7 @@ std::string autotune_key(const adsg_ctx* c, int d) {
 
 // Autotuner: time every applicable line-solve variant per direction on the
 // context's own state buffer (zeros) and keep the fastest.  ADSG_SOLVE_VARIANT
-// (0..6) forces one variant where applicable; ADSG_AUTOTUNE_LOG=1 prints each
+// (0..7) forces one variant where applicable; ADSG_AUTOTUNE_LOG=1 prints each
 // candidate's time to stderr.  A candidate whose launch reports an error is
 // dropped (the error is cleared so that it cannot leak into the next one).
 int autotune_solves(adsg_ctx* c) {
@@ -230,7 +230,9 @@ int autotune_solves(adsg_ctx* c) {
             if (!line_solve_variant_ok(v, D)) continue;
             D.solve_variant = v;
             float ms = 0.f;
-            const cudaError_t e = time_line_solve(c, D, L, a, b, &ms);
+            cudaError_t e = time_line_solve(c, D, L, a, b, &ms);
+            if (e == cudaSuccess && v == SOLVE_TWISTED_BULK && bulk_wait_timeouts(1) != 0)
+                e = cudaErrorLaunchTimeout;  // a copy wait ran out: not a candidate
             if (e != cudaSuccess) {
                 if (log)
                     std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d variant %d dropped: %s\n", d, D.n, v,
@@ -357,11 +359,13 @@ int build_step_dim(adsg_ctx* c, int d, const adsg_dim_desc& h, const twisted_tab
             float plain = 1e30f, best = 1e30f;
             pick = c->dims[d].solve_variant;
             if (time_line_solve(c, c->dims[d], L, a, b, &plain) != cudaSuccess) plain = 1e30f;
-            for (int v : {SOLVE_TWISTED, SOLVE_TWISTED_STAGED, SOLVE_TWISTED_CHUNKED}) {
+            for (int v : {SOLVE_TWISTED, SOLVE_TWISTED_STAGED, SOLVE_TWISTED_CHUNKED, SOLVE_TWISTED_BULK}) {
                 S.solve_variant = v;
                 if (!line_solve_variant_ok(v, S)) continue;
                 float ms = 0.f;
-                const cudaError_t te = time_line_solve(c, S, L, a, b, &ms);
+                cudaError_t te = time_line_solve(c, S, L, a, b, &ms);
+                if (te == cudaSuccess && v == SOLVE_TWISTED_BULK && bulk_wait_timeouts(1) != 0)
+                    te = cudaErrorLaunchTimeout;
                 if (log)
                     std::fprintf(stderr, "ads_gb300 autotune: dim %d n=%d step view variant %d %s %.2f us (plain %.2f)\n",
                                  d, S.n, v, te == cudaSuccess ? "" : cudaGetErrorString(te), ms * 1000.f / 3,
@@ -842,6 +846,9 @@ int adsg_ctx_set_stream(adsg_ctx* ctx, void* cuda_stream) {
 int adsg_ctx_synchronize(adsg_ctx* ctx) {
     if (!ctx) return fail(-1, "ctx is NULL");
     ADSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+    if (solve_variant_twisted(ctx->dims[0].solve_variant) || solve_variant_twisted(ctx->sdims[0].solve_variant))
+        if (bulk_wait_timeouts(1) > 0)
+            return fail(ADSG_ERR_DEVICE, "a bulk-copy wait of an x-line solve ran out (lines left unsolved)");
     return 0;
 }
 

@@ -1117,6 +1117,132 @@ __global__ void __launch_bounds__(128) line_solve_twisted_staged_kernel(const do
 
 size_t twisted_staged_smem_per_warp(int n) { return static_cast<size_t>(16) * twisted_pitch(n) * sizeof(double); }
 
+// ---------------------------------------------------------------------------
+// The staged two-ended sweep with its tile moved by the copy engine.  A warp's
+// 16 contiguous x-lines are 16 n consecutive doubles in global memory; one
+// lane issues a single bulk copy (cp.async.bulk) of them into the warp's
+// shared tile, completing on an mbarrier the warp waits on, and after the
+// sweeps one bulk copy writes the tile back.  The tile keeps the lines' own
+// pitch n (a bulk copy moves contiguous bytes, 16 at a time); for even n that
+// costs the sweep's 16-lane shared loads a two-way bank conflict, which an
+// FP64-bound sweep does not feel.  Same operations in the same order as the
+// other two-ended variants: bitwise equal results.
+// The wait for the copy is bounded: past the limit the warp records it in
+// g_bulk_wait_timeouts, waits (bounded again) for its copy and returns with
+// its lines unsolved; the context reports ADSG_ERR_DEVICE.
+// ---------------------------------------------------------------------------
+__device__ int g_bulk_wait_timeouts;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst_smem)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_store(void* dst, const void* src_smem, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src_smem)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_store_wait() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+constexpr long long kBulkWaitPolls = 1LL << 22;
+
+template <int K, int UNR, bool UNIT>
+__global__ void __launch_bounds__(128) line_solve_twisted_bulk_kernel(double* __restrict__ data, dim_dev D,
+                                                                      line_layout L) {
+    extern __shared__ __align__(16) double smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, chain = lane >> 4, wpb = blockDim.x >> 5;
+    const int n = D.n;
+    const long long g0 = (static_cast<long long>(blockIdx.x) * wpb + warp) * 16;
+    if (g0 >= L.nlines) return;  // whole warp
+    pdl_wait();
+    const int nv = static_cast<int>(min(16LL, L.nlines - g0));
+    double* tile = smem + static_cast<size_t>(warp) * 16 * n;  // 128 n bytes per warp: 16-byte aligned
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + static_cast<size_t>(wpb) * 16 * n) + warp;
+    const long long count = static_cast<long long>(nv) * n;
+    const unsigned bytes = static_cast<unsigned>((count * 8) & ~15LL);  // whole 16-byte units by the engine
+    double* src = data + g0 * n;                                         // 128 g0 n bytes in: 16-byte aligned
+    // bounds-checked build: the warp's tile and barrier, and its 16 lines (warp-uniform)
+    if (!(ADSG_SMEM_RANGE(tile, 16LL * n) && ADSG_SMEM_RANGE(reinterpret_cast<double*>(bar), 1) &&
+          ADSG_IN(g0 * n, L.total) && ADSG_IN(g0 * n + count - 1, L.total)))
+        return;
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive_expect_tx(bar, bytes);
+        bulk_load(tile, src, bytes, bar);
+    }
+    if (lane == 1 && bytes < count * 8) tile[count - 1] = src[count - 1];  // an odd last double
+    bool arrived = false;
+    for (long long it = 0; it < kBulkWaitPolls && !arrived; ++it) arrived = mbar_try_wait(bar, 0);
+    if (!__all_sync(0xffffffffu, arrived)) {
+        if (lane == 0) atomicAdd(&g_bulk_wait_timeouts, 1);
+        for (long long it = 0; it < kBulkWaitPolls && !arrived; ++it) arrived = mbar_try_wait(bar, 0);
+        return;  // lines left unsolved; reported to the host
+    }
+    __syncwarp();
+    const int line = lane & 15;
+    const bool active = line < nv;
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (active) {
+        double* x = tile + line * n + (chain ? n - 1 : 0);
+        const long long off = static_cast<long long>(chain) * D.tw_rows;
+        twisted_chain<K, UNR, UNIT, true>(x, x, chain ? -1 : 1, chain ? D.tw_n2 : D.tw_n1, D.tw_lmul + off * K,
+                                          D.tw_ucol + off * K, D.tw_rdiag + off, D.tw_g + chain * 2 * K * K, mask);
+    }
+    __syncwarp();
+    // the sweeps' shared-memory writes are made visible to the copy engine, then one bulk store
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncwarp();
+    if (lane == 0) {
+        bulk_store(src, tile, bytes);
+        bulk_store_wait();  // the tile must be read before the warp's shared memory goes away
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+    }
+    if (lane == 1 && bytes < count * 8) src[count - 1] = tile[count - 1];
+}
+
+size_t twisted_bulk_smem_per_warp(int n) { return static_cast<size_t>(16) * n * sizeof(double) + 8; }
+
+int bulk_wait_timeouts(int reset) {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_bulk_wait_timeouts, sizeof(int)) != cudaSuccess) return -1;
+    if (reset && v) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_bulk_wait_timeouts, &zero, sizeof(int));
+    }
+    return v;
+}
+
 // Warps per block (1, 2 or 4) for kernels whose warps each hold a tile of
 // per_warp bytes: the one that keeps the most warps resident per SM (228 KB
 // of shared memory, 1 KB reserved per block), the smaller on a tie (finer
@@ -1562,7 +1688,22 @@ static cudaError_t twisted_t(double* data, const dim_dev& d, const line_layout& 
                           dim3(static_cast<unsigned>((L.nlines + 15) / 16)), dim3(32),
                           twisted_chunked_smem_per_warp(), s, data, d, L);
     }
-    const bool staged = variant == SOLVE_TWISTED_STAGED;
+    if (variant == SOLVE_TWISTED_BULK && L.contiguous && out == data &&
+        reinterpret_cast<uintptr_t>(data) % 16 == 0) {
+        const size_t per_warp = twisted_bulk_smem_per_warp(d.n);
+        const int wpb = tile_warps_per_block(per_warp);
+        if (wpb == 0) return cudaErrorInvalidConfiguration;
+        const size_t smem = per_warp * wpb;
+        auto kern = line_solve_twisted_bulk_kernel<K, UNR, UNIT>;
+        if (smem > 48 * 1024) {
+            cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(kern), smem);
+            if (e != cudaSuccess) return e;
+        }
+        const long long per = 16LL * wpb;
+        return launch_pdl(kern, dim3(static_cast<unsigned>((L.nlines + per - 1) / per)), dim3(32 * wpb), smem, s, data,
+                          d, L);
+    }
+    const bool staged = variant == SOLVE_TWISTED_STAGED || variant == SOLVE_TWISTED_BULK;  // bulk: unaligned fallback
     if (staged && L.contiguous) {
         const size_t per_warp = twisted_staged_smem_per_warp(d.n);
         const int wpb = tile_warps_per_block(per_warp);
@@ -1651,6 +1792,9 @@ bool line_solve_variant_ok(int variant, const dim_dev& d) {
         return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr;
     if (variant == SOLVE_TWISTED_STAGED)
         return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr && twisted_staged_smem_per_warp(d.n) <= 227 * 1024;
+    if (variant == SOLVE_TWISTED_BULK)
+        return d.tw_k >= 1 && d.tw_k <= 4 && d.tw_lmul != nullptr && twisted_bulk_smem_per_warp(d.n) <= 227 * 1024 &&
+               twisted_staged_smem_per_warp(d.n) <= 227 * 1024;
     const int kl = d.kl, ku = d.ku_regular, w = d.w;
     const bool reg = (kl == 1 && ku <= 2 && w <= 3 && w >= 1) || (kl == 2 && ku <= 2 && w <= 4 && w >= 2) ||
                      (kl == 3 && ku <= 3 && w <= 6 && w >= 3) || (kl == 4 && ku <= 4 && w <= 8 && w >= 4);
@@ -1917,7 +2061,7 @@ __device__ __forceinline__ void batch_pass(const batch_inst& I, int stage, long 
     const long long nn = static_cast<long long>(n) * n;
     const int lo = max(D.sym_lo, P), hi = min(D.sym_hi, n - P);
     const bool sym = hi > lo;
-#pragma unroll 1
+#pragma unroll 2
     for (int k = 0; k < kBatchPassUnits / 256; ++k) {
         const long long g = first + k * 256 + threadIdx.x;
         if (g >= I.size) return;

@@ -23,11 +23,15 @@ enum solve_variant_id {
     SOLVE_TWISTED = 4,
     SOLVE_TWISTED_STAGED = 5,
     SOLVE_TWISTED_CHUNKED = 6,
-    SOLVE_NVARIANTS = 7
+    SOLVE_TWISTED_BULK = 7,  // the staged tile moved by the copy engine (cp.async.bulk) both ways
+    SOLVE_NVARIANTS = 8
 };
 inline bool solve_variant_twisted(int v) {
-    return v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED || v == SOLVE_TWISTED_CHUNKED;
+    return v == SOLVE_TWISTED || v == SOLVE_TWISTED_STAGED || v == SOLVE_TWISTED_CHUNKED || v == SOLVE_TWISTED_BULK;
 }
+// Bulk-copy waits of the x-line tiles that ran out (their lines were left
+// unsolved); nonzero never happens in a healthy run.  reset != 0 clears it.
+int bulk_wait_timeouts(int reset);
 
 struct dim_dev {
     int n = 0, p = 0, kl = 0, w = 0;  // w = kl + ku: widest upper extent of U

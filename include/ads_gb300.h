@@ -172,7 +172,9 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes);
  * 4 the two-ended sweep (each line swept from both ends by two lanes, the
  * meeting unknowns from a small dense inverse) in global memory, 5 the same
  * with contiguous lines staged whole through shared memory, 6 the same with
- * contiguous lines streamed through shared memory in 32-row chunks.  variants has 3 entries
+ * contiguous lines streamed through shared memory in 32-row chunks, 7 the
+ * same as 5 with the tile moved by the copy engine (one bulk copy in and one
+ * out per 16 lines; 4-7 agree bitwise).  variants has 3 entries
  * (-1 for absent dimensions).  The environment variable ADSG_SOLVE_VARIANT
  * forces a variant where it applies; ADSG_AUTOTUNE_LOG=1 prints the timings.
  * Decisions are cached per shape for the process. */

@@ -318,7 +318,7 @@ def test_full_size_against_oracle_one_step_sampled(big):
     check("130^3 p=2 1 step vs oracle", oracle.rel_l2(got, ref), STEP)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize("p,elements", [
     ((2, 2, 2), (30, 7, 9)),
     ((4, 4, 4), (12, 9, 6)),
@@ -345,11 +345,11 @@ def test_every_solve_variant_against_oracle(variant, p, elements, cuda, monkeypa
     ctx.heat_steps_host(s, 1e-5, 2)
     check(f"{label} 2 steps", oracle.rel_l2(s, pr.heat_steps(u, 1e-5, 2)), STEP * 2, oracle_self(pr, u, 1e-5, 2))
     chosen = ctx.solve_variants()
-    assert all(0 <= v <= 6 for v in chosen)
+    assert all(0 <= v <= 7 for v in chosen)
     if variant in (0, 3):  # always applicable for p <= 4; a forced variant rules the step's view too
         assert chosen == [variant] * len(p)
         assert ctx.step_solve_variants() == chosen
-    if variant in (4, 5, 6):  # the twisted sweeps need n >= 4p + 2 along the direction
+    if variant in (4, 5, 6, 7):  # the twisted sweeps need n >= 4p + 2 along the direction
         for d, v in zip(dims, chosen):
             assert (v == variant) == (d.dofs() >= 4 * d.p + 2)
 
@@ -523,7 +523,7 @@ def test_step_view_takes_its_own_variant(p, elements, cuda, monkeypatch):
     ctx = ads.Context(dims)
     plain, step = ctx.solve_variants(), ctx.step_solve_variants()
     for a, b in zip(plain, step):
-        assert a == b or (a <= 3 and b in (4, 5, 6))
+        assert a == b or (a <= 3 and b in (4, 5, 6, 7))
     pr = oracle.Problem(list(p), list(elements))
     u = np.random.default_rng(9).uniform(-1, 1, pr.size)
     ud = torch.from_numpy(u).cuda()
@@ -537,12 +537,13 @@ def test_step_view_takes_its_own_variant(p, elements, cuda, monkeypatch):
 @pytest.mark.parametrize("p,elements", [((2, 2, 2), (40, 33, 20)), ((4, 4, 4), (30, 20, 18)), ((3, 3), (70, 45))])
 def test_twisted_variants_agree_bitwise(p, elements, cuda, monkeypatch):
     """The two-ended sweep in global memory (4), with whole lines staged in
-    shared memory (5) and streamed in 32-row chunks (6) perform the same
-    operations in the same order: identical results, plain and row-scaled."""
+    shared memory (5), streamed in 32-row chunks (6) and staged by bulk copies
+    of the copy engine (7) perform the same operations in the same order:
+    identical results, plain and row-scaled."""
     import torch
 
     out = []
-    for v in ("4", "5", "6"):
+    for v in ("4", "5", "6", "7"):
         monkeypatch.setenv("ADSG_SOLVE_VARIANT", v)
         ctx = ads.Context([ads.Dimension(pp, e) for pp, e in zip(p, elements)])
         assert ctx.solve_variants() == [int(v)] * len(p)

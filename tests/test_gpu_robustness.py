@@ -53,7 +53,7 @@ def _fixed(A, k, p):
     return A
 
 
-@pytest.mark.parametrize("variant", [None, "0", "3", "4", "5", "6"])
+@pytest.mark.parametrize("variant", [None, "0", "3", "4", "5", "6", "7"])
 def test_fixed_dofs_every_variant(variant, cuda, monkeypatch):
     import torch
 
