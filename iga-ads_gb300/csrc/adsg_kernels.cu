@@ -1805,8 +1805,12 @@ bool line_solve_variant_ok(int variant, const dim_dev& d) {
     return true;
 }
 
+// The x sweep that writes its tiles to another buffer (mapped host memory)
+// is the whole-line staged one (variant 5, plain coalesced stores); it serves
+// variant 7 too, whose results it equals bitwise.
 bool line_solve_out_ok(const dim_dev& d, const line_layout& L) {
-    return L.contiguous && d.solve_variant == SOLVE_TWISTED_STAGED && line_solve_variant_ok(SOLVE_TWISTED_STAGED, d);
+    return L.contiguous && (d.solve_variant == SOLVE_TWISTED_STAGED || d.solve_variant == SOLVE_TWISTED_BULK) &&
+           line_solve_variant_ok(SOLVE_TWISTED_STAGED, d);
 }
 
 cudaError_t launch_line_solve_out(const double* data, double* out, const dim_dev& d, const line_layout& L,
