@@ -549,6 +549,114 @@ int autotune_launch_mode(adsg_ctx* c) {
 // arithmetic instead of before it.  The result is copied back once after the
 // last step (stores to host memory from the solve kernels were measured
 // slower than one copy).
+// Host entry, slab-chunked.  The first step's right-hand side reads the pinned
+// input over the host link (outer-axis column sweeps); its later passes need
+// only their own slab of the outer axis, so running the step's passes chunk
+// by chunk of outer-axis slabs on two streams lets one chunk's host reads
+// overlap another chunk's FP64 passes.  Likewise the last step's solves after
+// the outer-axis one are slab-local (y-lines and x-lines stay within a
+// z-slab), so the x sweep writing one chunk to the host overlaps the next
+// chunk's y solve.  Every output and every line takes the same operations as
+// unchunked: the results are the same bits.
+int ensure_aux(adsg_ctx* c) {
+    if (c->aux) return 0;
+    ADSG_CUDA_TRY(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking), "aux stream");
+    ADSG_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "fork event");
+    ADSG_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "join event");
+    return 0;
+}
+
+int host_chunks(adsg_ctx* c) {
+    if (c->host_chunks < 0) {
+        const char* v = std::getenv("ADSG_HOST_CHUNKS");
+        int k = v && *v ? std::atoi(v) : 4;
+        c->host_chunks = std::max(1, std::min(k, c->n[c->ndim - 1] / 4));
+    }
+    return c->ndim >= 2 ? c->host_chunks : 1;
+}
+
+int fork_aux(adsg_ctx* c) {
+    ADSG_CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream), "fork");
+    ADSG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->ev_fork, 0), "fork");
+    return 0;
+}
+
+int join_aux(adsg_ctx* c) {
+    ADSG_CUDA_TRY(cudaEventRecord(c->ev_join, c->aux), "join");
+    ADSG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
+    return 0;
+}
+
+// rows [r0, r1) of chunk k of K over an outer axis of n rows
+void chunk_rows(int n, int k, int K, int* r0, int* r1) {
+    *r0 = static_cast<int>(static_cast<long long>(n) * k / K);
+    *r1 = static_cast<int>(static_cast<long long>(n) * (k + 1) / K);
+}
+
+// The whole right-hand side of the first step from the pinned input (device
+// view in_dev), in K slab chunks of the outer axis alternating between the
+// context's stream and aux.
+int enqueue_rhs_from_host_chunked(adsg_ctx* c, const dim_dev* D, const double* in_dev, double* rhs, int K) {
+    pdl_scope pdl(c->pdl);
+    const int o = c->ndim - 1;
+    const long long so = c->size / c->n[o];
+    double** T = c->scratch;
+    if (int st = fork_aux(c)) return st;
+    for (int k = 0; k < K; ++k) {
+        int r0, r1;
+        chunk_rows(c->n[o], k, K, &r0, &r1);
+        cudaStream_t s = (k & 1) ? c->aux : c->stream;
+        const long long off = r0 * so, cnt = (r1 - r0) * so;
+        ADSG_CUDA_TRY(launch_outer_pass_columns(D[o].p, in_dev, T[0], T[1], D[o].mrow, D[o].nrow, c->n[o], so, s,
+                                                D[o].sym_lo, D[o].sym_hi, r0, r1),
+                      "rhs pass (outer, from host, chunk)");
+        if (c->ndim == 3) {
+            // F = (-dt Ky) A + My C, G = My A on the chunk's slabs
+            ADSG_CUDA_TRY(launch_band_pass(D[1].p, T[0] + off, T[1] + off, T[2] + off, T[3] + off, D[1].kdt, D[1].mrow,
+                                           D[1].mrow, D[1].n, c->n[0], cnt, s, D[1].sym_lo, D[1].sym_hi),
+                          "rhs pass y (chunk)");
+            ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[3] + off, T[2] + off, rhs + off, nullptr, D[0].kdt, D[0].mrow,
+                                           nullptr, D[0].n, 1, cnt, s),
+                          "rhs pass x (chunk)");
+        } else {
+            ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[0] + off, T[1] + off, rhs + off, nullptr, D[0].kdt, D[0].mrow,
+                                           nullptr, D[0].n, 1, cnt, s),
+                          "rhs pass x (chunk)");
+        }
+    }
+    return join_aux(c);
+}
+
+// The last step's solves with the x sweep writing to `out` (mapped host
+// memory): the outer-axis solve whole, then per slab chunk the y solve (3D)
+// and the x sweep into out, chunks alternating between the two streams.
+int enqueue_step_solves_to_host_chunked(adsg_ctx* c, double* x, double* out, int K) {
+    pdl_scope pdl(c->pdl);
+    const int o = c->ndim - 1;
+    const long long so = c->size / c->n[o];
+    ADSG_CUDA_TRY(launch_line_solve(x, c->sdims[o], make_line_layout(c->n, c->ndim, o), 0, c->stream),
+                  "line solve (outer)");
+    if (int st = fork_aux(c)) return st;
+    for (int k = 0; k < K; ++k) {
+        int r0, r1;
+        chunk_rows(c->n[o], k, K, &r0, &r1);
+        cudaStream_t s = (k & 1) ? c->aux : c->stream;
+        const long long off = r0 * so;
+        if (c->ndim == 3) {
+            line_layout Ly = make_line_layout(c->n, c->ndim, 1);
+            Ly.nlines = static_cast<long long>(r1 - r0) * c->n[0];
+            Ly.total = (r1 - r0) * so;
+            ADSG_CUDA_TRY(launch_line_solve(x + off, c->sdims[1], Ly, 0, s), "line solve y (chunk)");
+        }
+        line_layout Lx = make_line_layout(c->n, c->ndim, 0);
+        Lx.nlines = (r1 - r0) * so / c->n[0];
+        Lx.a = Lx.nlines;
+        Lx.total = (r1 - r0) * so;
+        ADSG_CUDA_TRY(launch_line_solve_out(x + off, out + off, c->sdims[0], Lx, s), "line solve x (to output, chunk)");
+    }
+    return join_aux(c);
+}
+
 int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, double dt, int nsteps) {
     const int o = c->ndim - 1;  // outermost axis
     const long long so = c->size / c->n[o];
@@ -567,7 +675,14 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
     // below ~2 MB the copy is a few microseconds and the column sweeps would
     // run nearly serially
     const bool direct_in = in_dev && outer_pass_columns_ok(D[o].p) && c->size >= (1LL << 18);
-    if (direct_in) {
+    // slab chunks on two streams (not with stage timers, which time one stream)
+    const int K = c->timing ? 1 : host_chunks(c);
+    if (K > 1)
+        if (int st2 = ensure_aux(c)) return st2;
+    const bool chunked_in = direct_in && K > 1 && !(c->fuse_x && fusion_ok(c));
+    if (chunked_in) {
+        // the first step's whole right-hand side, below
+    } else if (direct_in) {
         pdl_scope pdl(c->pdl);
         stage_scope sc(c, ADSG_STAGE_RHS_OUTER);
         ADSG_CUDA_TRY(launch_outer_pass_columns(D[o].p, in_dev, c->scratch[0], c->scratch[1], D[o].mrow, D[o].nrow,
@@ -587,10 +702,16 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
     }
     for (int step = 0; step < nsteps; ++step) {
         const bool fused = c->fuse_x && fusion_ok(c);
-        st = enqueue_rhs_with(c, D, cur, nxt, dt, fused, /*outer_done=*/step == 0 && direct_in);
+        if (step == 0 && chunked_in)
+            st = enqueue_rhs_from_host_chunked(c, D, in_dev, nxt, K);
+        else
+            st = enqueue_rhs_with(c, D, cur, nxt, dt, fused, /*outer_done=*/step == 0 && direct_in);
         if (st) return st;
         const bool to_host = step + 1 == nsteps && !fused && out_dev && step_x_out_ok(c) && c->size >= (1LL << 18);
-        st = enqueue_step_solves(c, nxt, fused, to_host ? out_dev : nullptr);
+        if (to_host && K > 1)
+            st = enqueue_step_solves_to_host_chunked(c, nxt, out_dev, K);
+        else
+            st = enqueue_step_solves(c, nxt, fused, to_host ? out_dev : nullptr);
         if (st) return st;
         if (to_host) return 0;
         std::swap(cur, nxt);
@@ -619,6 +740,7 @@ int heat_steps_host_graph(adsg_ctx* c, double* u, double dt, int nsteps) {
         return heat_steps_host_direct(c, u, u, dt, nsteps);
     int st = ensure_dt_bands(c, dt);
     if (st) return st;
+    if (host_chunks(c) > 1 && (st = ensure_aux(c)) != 0) return st;  // created outside the capture
     if (!(c->host_graph && c->host_graph_u == u && c->host_graph_dt == dt && c->host_graph_steps == nsteps)) {
         if (c->host_graph) cudaGraphExecDestroy(c->host_graph);
         c->host_graph = nullptr;

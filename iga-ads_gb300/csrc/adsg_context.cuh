@@ -80,6 +80,11 @@ struct adsg_ctx {
     size_t qpool_size = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // second stream and fork/join events of the host entry's slab-chunked
+    // first and last steps (created on first use)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    int host_chunks = -1;  // slab chunks of the host entry (1 = none); -1 = not chosen yet
     dev_arena arena;
     // graph of two steps u -> ping -> u, specialised on (u, dt)
     cudaGraphExec_t graph = nullptr;
@@ -156,6 +161,12 @@ struct adsg_ctx {
             cudaEventDestroy(t.b);
         }
         for (auto e : spare) cudaEventDestroy(e);
+        if (aux) {
+            cudaStreamSynchronize(aux);
+            cudaStreamDestroy(aux);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };

@@ -229,14 +229,15 @@ template <int P, bool SYM>
 __global__ void __launch_bounds__(128) outer_columns_kernel(const double* __restrict__ in, double* __restrict__ out0,
                                                             double* __restrict__ out1, const double* __restrict__ A0,
                                                             const double* __restrict__ B0, int n, long long so,
-                                                            int seg, int sym_lo, int sym_hi) {
+                                                            int seg, int sym_lo, int sym_hi, int row_begin,
+                                                            int row_end) {
     constexpr int BW = 2 * P + 1, PRE = 8;
     const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const long long nseg = (n + seg - 1) / seg;
+    const long long nseg = (row_end - row_begin + seg - 1) / seg;
     if (t >= so * nseg) return;
     pdl_wait_and_release();
     const long long col = t % so;
-    const int r0 = static_cast<int>(t / so) * seg, r1 = min(n, r0 + seg);
+    const int r0 = row_begin + static_cast<int>(t / so) * seg, r1 = min(row_end, r0 + seg);
     const double* src = in + col;
     if (!(ADSG_IN(col, so) && ADSG_IN(col + static_cast<long long>(n - 1) * so, static_cast<long long>(n) * so)))
         return;  // bounds-checked build: the column inside the n x so tensor
@@ -293,24 +294,27 @@ bool outer_pass_columns_ok(int p) { return p >= 1 && p <= 4; }
 
 cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, double* out1, const double* A0,
                                       const double* B0, int n_axis, long long stride, cudaStream_t s, int sym_lo,
-                                      int sym_hi) {
+                                      int sym_hi, int row_begin, int row_end) {
     if (!outer_pass_columns_ok(p)) return cudaErrorInvalidValue;
+    if (row_end < 0) row_end = n_axis;
+    if (row_begin < 0 || row_end > n_axis || row_begin >= row_end) return cudaErrorInvalidValue;
+    const int rows = row_end - row_begin;
     // whole columns (each input read exactly once) unless there are too few
     // columns to give every sub-partition a few warps; segments re-read a
     // 2p-row halo each
     const long long want = 16384;
-    int seg = n_axis;
-    if (stride < want) seg = static_cast<int>(std::max<long long>(32, (n_axis * stride + want - 1) / want));
-    const long long threads = stride * ((n_axis + seg - 1) / seg);
+    int seg = rows;
+    if (stride < want) seg = static_cast<int>(std::max<long long>(32, (rows * stride + want - 1) / want));
+    const long long threads = stride * ((rows + seg - 1) / seg);
     if (threads <= 0) return cudaSuccess;
     const dim3 grid(static_cast<unsigned>((threads + 127) / 128)), block(128);
     const int lo = std::max(sym_lo, p), hi = std::min(sym_hi, n_axis - p);
     const bool sym = hi > lo;
 #define ADSG_COLS(P_)                                                                                          \
     (sym ? launch_pdl(outer_columns_kernel<P_, true>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg, \
-                      lo, hi)                                                                                   \
+                      lo, hi, row_begin, row_end)                                                               \
          : launch_pdl(outer_columns_kernel<P_, false>, grid, block, 0, s, in, out0, out1, A0, B0, n_axis, stride, seg, \
-                      0, 0))
+                      0, 0, row_begin, row_end))
     switch (p) {
         case 1: return ADSG_COLS(1);
         case 2: return ADSG_COLS(2);

@@ -147,9 +147,11 @@ cudaError_t launch_band_pass(int p, const double* in0, const double* in1, double
 // input in pinned host memory, read over the host link while the pass
 // computes.  Same operations in the same order as launch_band_pass; p <= 4.
 bool outer_pass_columns_ok(int p);
+// row_begin / row_end restrict the outputs to rows [row_begin, row_end) of the
+// outer axis (the rows around them are still read for the band); -1 = all.
 cudaError_t launch_outer_pass_columns(int p, const double* in, double* out0, double* out1, const double* A0,
                                       const double* B0, int n_axis, long long stride, cudaStream_t s, int sym_lo,
-                                      int sym_hi);
+                                      int sym_hi, int row_begin = 0, int row_end = -1);
 
 // Set the plane {index along d == k} of an x-fastest tensor with dofs n[0..ndim)
 // to values (device, x-fastest over the other directions) or to 0 (NULL).
