@@ -550,19 +550,24 @@ int autotune_launch_mode(adsg_ctx* c) {
 // last step (stores to host memory from the solve kernels were measured
 // slower than one copy).
 // Host entry, slab-chunked.  The first step's right-hand side reads the pinned
-// input over the host link (outer-axis column sweeps); its later passes need
-// only their own slab of the outer axis, so running the step's passes chunk
-// by chunk of outer-axis slabs on two streams lets one chunk's host reads
-// overlap another chunk's FP64 passes.  Likewise the last step's solves after
-// the outer-axis one are slab-local (y-lines and x-lines stay within a
-// z-slab), so the x sweep writing one chunk to the host overlaps the next
-// chunk's y solve.  Every output and every line takes the same operations as
-// unchunked: the results are the same bits.
+// input over the host link (outer-axis column sweeps), and its later passes
+// need only their own slab of the outer axis; the last step's solves after
+// the outer-axis one are slab-local too (y-lines and x-lines stay within a
+// z-slab).  So those steps run in chunks of outer-axis slabs as a two-stage
+// pipeline on two streams: the link-bound kernels (the column sweeps reading
+// the host; the x sweeps writing their tiles to the host) on one, the
+// FP64-bound ones (the y and x passes; the y solves) on the other, each chunk
+// waiting only for its own predecessor through an event.  Every output and
+// every line takes the same operations as unchunked: the results are the same
+// bits.
+constexpr int kMaxHostChunks = 16;
+
 int ensure_aux(adsg_ctx* c) {
     if (c->aux) return 0;
     ADSG_CUDA_TRY(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking), "aux stream");
     ADSG_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "fork event");
     ADSG_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "join event");
+    for (auto& e : c->ev_chunk) ADSG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "chunk event");
     return 0;
 }
 
@@ -570,20 +575,15 @@ int host_chunks(adsg_ctx* c) {
     if (c->host_chunks < 0) {
         const char* v = std::getenv("ADSG_HOST_CHUNKS");
         int k = v && *v ? std::atoi(v) : 4;
-        c->host_chunks = std::max(1, std::min(k, c->n[c->ndim - 1] / 4));
+        c->host_chunks = std::max(1, std::min({k, kMaxHostChunks, c->n[c->ndim - 1] / 4}));
     }
     return c->ndim >= 2 ? c->host_chunks : 1;
 }
 
+// aux waits for everything issued so far on the context's stream
 int fork_aux(adsg_ctx* c) {
     ADSG_CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream), "fork");
     ADSG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->ev_fork, 0), "fork");
-    return 0;
-}
-
-int join_aux(adsg_ctx* c) {
-    ADSG_CUDA_TRY(cudaEventRecord(c->ev_join, c->aux), "join");
-    ADSG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
     return 0;
 }
 
@@ -594,8 +594,8 @@ void chunk_rows(int n, int k, int K, int* r0, int* r1) {
 }
 
 // The whole right-hand side of the first step from the pinned input (device
-// view in_dev), in K slab chunks of the outer axis alternating between the
-// context's stream and aux.
+// view in_dev): the host-reading column sweeps of all chunks on aux, the
+// chunks' y and x passes on the context's stream.
 int enqueue_rhs_from_host_chunked(adsg_ctx* c, const dim_dev* D, const double* in_dev, double* rhs, int K) {
     pdl_scope pdl(c->pdl);
     const int o = c->ndim - 1;
@@ -605,31 +605,36 @@ int enqueue_rhs_from_host_chunked(adsg_ctx* c, const dim_dev* D, const double* i
     for (int k = 0; k < K; ++k) {
         int r0, r1;
         chunk_rows(c->n[o], k, K, &r0, &r1);
-        cudaStream_t s = (k & 1) ? c->aux : c->stream;
-        const long long off = r0 * so, cnt = (r1 - r0) * so;
-        ADSG_CUDA_TRY(launch_outer_pass_columns(D[o].p, in_dev, T[0], T[1], D[o].mrow, D[o].nrow, c->n[o], so, s,
+        ADSG_CUDA_TRY(launch_outer_pass_columns(D[o].p, in_dev, T[0], T[1], D[o].mrow, D[o].nrow, c->n[o], so, c->aux,
                                                 D[o].sym_lo, D[o].sym_hi, r0, r1),
                       "rhs pass (outer, from host, chunk)");
+        ADSG_CUDA_TRY(cudaEventRecord(c->ev_chunk[k], c->aux), "chunk event");
+    }
+    for (int k = 0; k < K; ++k) {
+        int r0, r1;
+        chunk_rows(c->n[o], k, K, &r0, &r1);
+        const long long off = r0 * so, cnt = (r1 - r0) * so;
+        ADSG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_chunk[k], 0), "chunk wait");
         if (c->ndim == 3) {
             // F = (-dt Ky) A + My C, G = My A on the chunk's slabs
             ADSG_CUDA_TRY(launch_band_pass(D[1].p, T[0] + off, T[1] + off, T[2] + off, T[3] + off, D[1].kdt, D[1].mrow,
-                                           D[1].mrow, D[1].n, c->n[0], cnt, s, D[1].sym_lo, D[1].sym_hi),
+                                           D[1].mrow, D[1].n, c->n[0], cnt, c->stream, D[1].sym_lo, D[1].sym_hi),
                           "rhs pass y (chunk)");
             ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[3] + off, T[2] + off, rhs + off, nullptr, D[0].kdt, D[0].mrow,
-                                           nullptr, D[0].n, 1, cnt, s),
+                                           nullptr, D[0].n, 1, cnt, c->stream),
                           "rhs pass x (chunk)");
         } else {
             ADSG_CUDA_TRY(launch_band_pass(D[0].p, T[0] + off, T[1] + off, rhs + off, nullptr, D[0].kdt, D[0].mrow,
-                                           nullptr, D[0].n, 1, cnt, s),
+                                           nullptr, D[0].n, 1, cnt, c->stream),
                           "rhs pass x (chunk)");
         }
     }
-    return join_aux(c);
+    return 0;  // the context's stream waited for every chunk's sweep on aux
 }
 
 // The last step's solves with the x sweep writing to `out` (mapped host
-// memory): the outer-axis solve whole, then per slab chunk the y solve (3D)
-// and the x sweep into out, chunks alternating between the two streams.
+// memory): the outer-axis solve whole, then the chunks' y solves (3D) on the
+// context's stream and their x sweeps into out on aux.
 int enqueue_step_solves_to_host_chunked(adsg_ctx* c, double* x, double* out, int K) {
     pdl_scope pdl(c->pdl);
     const int o = c->ndim - 1;
@@ -640,21 +645,29 @@ int enqueue_step_solves_to_host_chunked(adsg_ctx* c, double* x, double* out, int
     for (int k = 0; k < K; ++k) {
         int r0, r1;
         chunk_rows(c->n[o], k, K, &r0, &r1);
-        cudaStream_t s = (k & 1) ? c->aux : c->stream;
-        const long long off = r0 * so;
         if (c->ndim == 3) {
             line_layout Ly = make_line_layout(c->n, c->ndim, 1);
             Ly.nlines = static_cast<long long>(r1 - r0) * c->n[0];
             Ly.total = (r1 - r0) * so;
-            ADSG_CUDA_TRY(launch_line_solve(x + off, c->sdims[1], Ly, 0, s), "line solve y (chunk)");
+            ADSG_CUDA_TRY(launch_line_solve(x + r0 * so, c->sdims[1], Ly, 0, c->stream), "line solve y (chunk)");
         }
+        ADSG_CUDA_TRY(cudaEventRecord(c->ev_chunk[k], c->stream), "chunk event");
+    }
+    for (int k = 0; k < K; ++k) {
+        int r0, r1;
+        chunk_rows(c->n[o], k, K, &r0, &r1);
+        const long long off = r0 * so;
+        ADSG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->ev_chunk[k], 0), "chunk wait");
         line_layout Lx = make_line_layout(c->n, c->ndim, 0);
         Lx.nlines = (r1 - r0) * so / c->n[0];
         Lx.a = Lx.nlines;
         Lx.total = (r1 - r0) * so;
-        ADSG_CUDA_TRY(launch_line_solve_out(x + off, out + off, c->sdims[0], Lx, s), "line solve x (to output, chunk)");
+        ADSG_CUDA_TRY(launch_line_solve_out(x + off, out + off, c->sdims[0], Lx, c->aux),
+                      "line solve x (to output, chunk)");
     }
-    return join_aux(c);
+    ADSG_CUDA_TRY(cudaEventRecord(c->ev_join, c->aux), "join");
+    ADSG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
+    return 0;
 }
 
 int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, double dt, int nsteps) {

@@ -84,6 +84,7 @@ struct adsg_ctx {
     // first and last steps (created on first use)
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_chunk[16] = {};  // one per slab chunk
     int host_chunks = -1;  // slab chunks of the host entry (1 = none); -1 = not chosen yet
     dev_arena arena;
     // graph of two steps u -> ping -> u, specialised on (u, dt)
@@ -167,6 +168,8 @@ struct adsg_ctx {
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
+        for (auto e : ev_chunk)
+            if (e) cudaEventDestroy(e);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
