@@ -549,17 +549,17 @@ int autotune_launch_mode(adsg_ctx* c) {
 // arithmetic instead of before it.  The result is copied back once after the
 // last step (stores to host memory from the solve kernels were measured
 // slower than one copy).
-// Host entry, slab-chunked.  The first step's right-hand side reads the pinned
-// input over the host link (outer-axis column sweeps), and its later passes
-// need only their own slab of the outer axis; the last step's solves after
-// the outer-axis one are slab-local too (y-lines and x-lines stay within a
-// z-slab).  So those steps run in chunks of outer-axis slabs as a two-stage
-// pipeline on two streams: the link-bound kernels (the column sweeps reading
-// the host; the x sweeps writing their tiles to the host) on one, the
-// FP64-bound ones (the y and x passes; the y solves) on the other, each chunk
-// waiting only for its own predecessor through an event.  Every output and
-// every line takes the same operations as unchunked: the results are the same
-// bits.
+// Host entry, slab-chunked first step.  The first step's right-hand side
+// reads the pinned input over the host link (outer-axis column sweeps), and
+// its later passes need only their own slab of the outer axis.  So that step's
+// passes run in chunks of outer-axis slabs as a two-stage pipeline on two
+// streams: the host-reading column sweeps of all chunks on one, the y and x
+// passes of each chunk on the other as soon as that chunk's sweep is done
+// (an event per chunk), which overlaps the link transfer with FP64 passes.
+// Every output takes the same operations as unchunked: the same bits.  (The
+// last step's line solves are not chunked: a sweep's time is set by its line
+// length, not by the number of lines, so chunks of lines would run one after
+// another where they now run side by side.)
 constexpr int kMaxHostChunks = 16;
 
 int ensure_aux(adsg_ctx* c) {
@@ -632,44 +632,6 @@ int enqueue_rhs_from_host_chunked(adsg_ctx* c, const dim_dev* D, const double* i
     return 0;  // the context's stream waited for every chunk's sweep on aux
 }
 
-// The last step's solves with the x sweep writing to `out` (mapped host
-// memory): the outer-axis solve whole, then the chunks' y solves (3D) on the
-// context's stream and their x sweeps into out on aux.
-int enqueue_step_solves_to_host_chunked(adsg_ctx* c, double* x, double* out, int K) {
-    pdl_scope pdl(c->pdl);
-    const int o = c->ndim - 1;
-    const long long so = c->size / c->n[o];
-    ADSG_CUDA_TRY(launch_line_solve(x, c->sdims[o], make_line_layout(c->n, c->ndim, o), 0, c->stream),
-                  "line solve (outer)");
-    if (int st = fork_aux(c)) return st;
-    for (int k = 0; k < K; ++k) {
-        int r0, r1;
-        chunk_rows(c->n[o], k, K, &r0, &r1);
-        if (c->ndim == 3) {
-            line_layout Ly = make_line_layout(c->n, c->ndim, 1);
-            Ly.nlines = static_cast<long long>(r1 - r0) * c->n[0];
-            Ly.total = (r1 - r0) * so;
-            ADSG_CUDA_TRY(launch_line_solve(x + r0 * so, c->sdims[1], Ly, 0, c->stream), "line solve y (chunk)");
-        }
-        ADSG_CUDA_TRY(cudaEventRecord(c->ev_chunk[k], c->stream), "chunk event");
-    }
-    for (int k = 0; k < K; ++k) {
-        int r0, r1;
-        chunk_rows(c->n[o], k, K, &r0, &r1);
-        const long long off = r0 * so;
-        ADSG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->ev_chunk[k], 0), "chunk wait");
-        line_layout Lx = make_line_layout(c->n, c->ndim, 0);
-        Lx.nlines = (r1 - r0) * so / c->n[0];
-        Lx.a = Lx.nlines;
-        Lx.total = (r1 - r0) * so;
-        ADSG_CUDA_TRY(launch_line_solve_out(x + off, out + off, c->sdims[0], Lx, c->aux),
-                      "line solve x (to output, chunk)");
-    }
-    ADSG_CUDA_TRY(cudaEventRecord(c->ev_join, c->aux), "join");
-    ADSG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
-    return 0;
-}
-
 int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, double dt, int nsteps) {
     const int o = c->ndim - 1;  // outermost axis
     const long long so = c->size / c->n[o];
@@ -721,10 +683,7 @@ int heat_steps_host_direct(adsg_ctx* c, const double* u_in, double* u_out, doubl
             st = enqueue_rhs_with(c, D, cur, nxt, dt, fused, /*outer_done=*/step == 0 && direct_in);
         if (st) return st;
         const bool to_host = step + 1 == nsteps && !fused && out_dev && step_x_out_ok(c) && c->size >= (1LL << 18);
-        if (to_host && K > 1)
-            st = enqueue_step_solves_to_host_chunked(c, nxt, out_dev, K);
-        else
-            st = enqueue_step_solves(c, nxt, fused, to_host ? out_dev : nullptr);
+        st = enqueue_step_solves(c, nxt, fused, to_host ? out_dev : nullptr);
         if (st) return st;
         if (to_host) return 0;
         std::swap(cur, nxt);
