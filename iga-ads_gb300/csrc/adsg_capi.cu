@@ -574,7 +574,7 @@ int ensure_aux(adsg_ctx* c) {
 int host_chunks(adsg_ctx* c) {
     if (c->host_chunks < 0) {
         const char* v = std::getenv("ADSG_HOST_CHUNKS");
-        int k = v && *v ? std::atoi(v) : 4;
+        int k = v && *v ? std::atoi(v) : 2;
         c->host_chunks = std::max(1, std::min({k, kMaxHostChunks, c->n[c->ndim - 1] / 4}));
     }
     return c->ndim >= 2 ? c->host_chunks : 1;
