@@ -130,16 +130,12 @@ int adsg_adjoint_forward(adsg_adjoint* a, const double* u0_dev, const double* ka
     ADSG_CUDA_TRY(cudaMemcpyAsync(a->ck, u0_dev, bytes, cudaMemcpyDeviceToDevice, s), "checkpoint 0");
     const double* cur = a->ck;
     for (int k = 0; k < a->nsteps; ++k) {
-        double* nxt = a->work[k & 1];
-        if (int st = elem_step(a, cur, nxt)) return st;
         const int kk = k + 1;
-        if (kk < a->nsteps && kk % a->every == 0) {
-            double* slot = a->ck + static_cast<size_t>(kk / a->every) * c->size;
-            ADSG_CUDA_TRY(cudaMemcpyAsync(slot, nxt, bytes, cudaMemcpyDeviceToDevice, s), "checkpoint");
-            cur = slot;
-        } else {
-            cur = nxt;
-        }
+        // a state that is checkpointed is computed straight into its slot
+        double* nxt = (kk < a->nsteps && kk % a->every == 0) ? a->ck + static_cast<size_t>(kk / a->every) * c->size
+                                                             : a->work[k & 1];
+        if (int st = elem_step(a, cur, nxt)) return st;
+        cur = nxt;
     }
     ADSG_CUDA_TRY(cudaMemcpyAsync(uT_dev, cur, bytes, cudaMemcpyDeviceToDevice, s), "copy u(T)");
     a->forward_done = true;
@@ -164,20 +160,21 @@ int adsg_adjoint_backward(adsg_adjoint* a, const double* dL_duT_dev, double* gra
     for (int sidx = a->nck - 1; sidx >= 0; --sidx) {
         const int k0 = sidx * a->every;
         const int k1 = std::min(k0 + a->every, a->nsteps);
-        // recompute u_{k0} .. u_{k1-1} from the checkpoint
-        ADSG_CUDA_TRY(cudaMemcpyAsync(a->seg, a->ck + static_cast<size_t>(sidx) * n, bytes, cudaMemcpyDeviceToDevice, s),
-                      "segment start");
-        for (int i = 0; i + 1 < k1 - k0; ++i)
-            if (int st = elem_step(a, a->seg + static_cast<size_t>(i) * n, a->seg + static_cast<size_t>(i + 1) * n))
-                return st;
+        // u_{k0} is the checkpoint itself; recompute u_{k0+1} .. u_{k1-1} from it
+        const double* ckp = a->ck + static_cast<size_t>(sidx) * n;
+        auto state = [&](int k) -> const double* {
+            return k == k0 ? ckp : a->seg + static_cast<size_t>(k - k0) * n;
+        };
+        for (int k = k0 + 1; k < k1; ++k)
+            if (int st = elem_step(a, state(k - 1), a->seg + static_cast<size_t>(k - k0) * n)) return st;
         for (int k = k1 - 1; k >= k0; --k) {
             if (int st = ctx_solve(c, lam, 1)) return st;  // lam <- mu_{k+1} = M^{-T} lambda_{k+1}
             ADSG_CUDA_TRY(cudaMemsetAsync(other, 0, bytes, s), "memset");
             {
                 // grad kappa += mu^T (dR/dkappa) u_k and other = R^T mu (R is symmetric)
                 stage_scope sc(c, ADSG_STAGE_RHS_ELEM);
-                ADSG_CUDA_TRY(launch_adjoint_pair(c->ndim, c->dims, a->seg + static_cast<size_t>(k - k0) * n, lam,
-                                                  a->kappa, other, grad_kappa_dev, a->dt, s),
+                ADSG_CUDA_TRY(launch_adjoint_pair(c->ndim, c->dims, state(k), lam, a->kappa, other, grad_kappa_dev,
+                                                  a->dt, s),
                               "kappa gradient and R^T mu");
             }
             std::swap(lam, other);  // lam <- lambda_k = R mu_{k+1}
