@@ -23,6 +23,10 @@ The reference arm (--impl reference) times the CPU oracle (a C restatement
 of the reference's heat step: Galois-style element loop on all host threads,
 single-threaded ADS solve) on the same workload, initial field, step count
 and warm-up.
+The default run's line also carries `other_configs`: the 2D p=2 34^2 grid,
+the 3D p=4 260^3 grid, the batched 64-instance set and the adjoint run, each
+measured by this script in a child process on the same GPU right after
+(--no-other-configs skips them).
 Multi-GPU: replicas only (the single-grid step does not shard); each rank
 runs its own copy and value is the sum over ranks.
 """
@@ -63,6 +67,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="heat3d_p2_128", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the summaries of the other configurations in the default workload's line")
     return ap.parse_args()
 
 
@@ -506,6 +512,9 @@ def run_ours(args, cfg):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["parity"] = step_parity(ctx, u0, cfg, args.workload, os.cpu_count() or 1)
         line["cpu_baseline"] = cpu_baseline(cfg)
+    if rank == 0 and world == 1 and args.workload == "heat3d_p2_128" and not args.no_other_configs:
+        ctx.close()
+        line["other_configs"] = other_configs(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -703,6 +712,41 @@ def run_adjoint(args, cfg):
             "dot_product_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs))}
     print(json.dumps(line), flush=True)
     return 0
+
+
+OTHER_CONFIGS = ("heat2d_p2_32", "heat3d_p4_256", "batch64", "adjoint_p2_96")
+
+
+def other_configs(args):
+    """The other configurations, each measured by this script in a child
+    process on the same GPU right after the default workload, summarised
+    for the default line: the 2D p=2 34^2 grid, the 3D p=4 260^3 grid, the
+    batched 64-instance set and the adjoint run."""
+    out = {}
+    for w in OTHER_CONFIGS:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", w, "--steps", str(args.steps), "--warmup",
+               str(args.warmup), "--no-cpu-baseline", "--no-other-configs"]
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+        except (subprocess.TimeoutExpired, ValueError, IndexError) as e:
+            out[w] = {"error": f"{type(e).__name__}: {e}"[:300]}
+            continue
+        keep = {k: d[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "clocks") if k in d}
+        keep["config"] = {k: v for k, v in d.get("config", {}).items() if k != "specs"}
+        if "e2e" in d:
+            keep["e2e"] = d["e2e"]["value"]
+        if "roofline" in d:
+            keep["roofline"] = {k: d["roofline"].get(k) for k in ("kernel", "achieved", "peak", "frac", "unit")}
+        for k in ("parity", "speedup_vs_loop", "engines", "looped_plain_kernels", "forward_ms", "gradient_ms",
+                  "gradient_over_forward", "all_states_kept", "fd_max_rel_err", "dot_product_rel_err",
+                  "element_rhs", "tuning", "gpu_launches"):
+            if k in d:
+                keep[k] = d[k]
+        keep["wall_s"] = time.perf_counter() - t0
+        out[w] = keep
+    return out
 
 
 def main():
