@@ -509,8 +509,9 @@ def run_ours(args, cfg):
         "clocks": clocks,
         "wall_s": wall,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1:
         line["parity"] = step_parity(ctx, u0, cfg, args.workload, os.cpu_count() or 1)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg)
     if rank == 0 and world == 1 and args.workload == "heat3d_p2_128" and not args.no_other_configs:
         ctx.close()
