@@ -139,6 +139,7 @@ def library() -> ctypes.CDLL:
         "adsg_ctx_launch_pdl": (i, [vp]),
         "adsg_ctx_fused_x": (i, [vp]),
         "adsg_ctx_step_1block": (i, [vp]),
+        "adsg_ctx_step_cluster": (i, [vp]),
         "adsg_ctx_step_graphs": (i, [vp]),
         "adsg_quad_size": (ll, [vp]),
         "adsg_count_nonfinite": (i, [vp, vp, ctypes.POINTER(ll)]),
@@ -374,6 +375,10 @@ class Context:
     def step_1block(self) -> bool:
         """Whether heat_step runs a whole (small 2D) step in one block."""
         return library().adsg_ctx_step_1block(self._h) == 1
+
+    def step_cluster(self) -> bool:
+        """Whether the one-launch small-grid step runs on a thread-block cluster."""
+        return library().adsg_ctx_step_cluster(self._h) == 1
 
     def step_graphs(self) -> bool:
         """Whether heat_step replays cached single-step CUDA graphs."""

@@ -286,7 +286,8 @@ int enqueue_step(adsg_ctx* c, const double* prev, double* next, double dt) {
     if (c->step_1block && step_1block_ok(c)) {
         pdl_scope pdl(c->pdl);
         stage_scope sc(c, ADSG_STAGE_STEP_1BLOCK);
-        ADSG_CUDA_TRY(launch_small2d_step(prev, next, c->sdims[0], c->sdims[1], c->stream), "one-block step");
+        set_small2d_cluster(c->step_cluster);
+        ADSG_CUDA_TRY(launch_small2d_step(prev, next, c->sdims[0], c->sdims[1], c->stream), "one-launch step");
         return 0;
     }
     const bool fused = c->fuse_x && fusion_ok(c);
@@ -462,26 +463,30 @@ int step_via_graph(adsg_ctx* c, const double* prev, double* next, double dt) {
 // direct launches.  None of the switches changes any result bit: programmatic
 // dependent launch (ADSG_PDL=0/1 forces it), fusing the x band pass into the
 // staged two-ended x solve where that is the x variant (ADSG_FUSE_X), the
-// one-block step of small 2D grids (ADSG_STEP_1BLOCK) and the graph replay
-// (ADSG_STEP_GRAPHS).
+// one-launch step of small 2D grids (ADSG_STEP_1BLOCK), that step on a
+// thread-block cluster rather than one block (ADSG_STEP_CLUSTER) and the graph
+// replay (ADSG_STEP_GRAPHS).
 int autotune_launch_mode(adsg_ctx* c) {
     auto forced = [](const char* name) -> int {
         const char* v = std::getenv(name);
         return v && (*v == '0' || *v == '1') ? *v - '0' : -1;
     };
     const int f_pdl = forced("ADSG_PDL"), f_fuse = forced("ADSG_FUSE_X"), f_one = forced("ADSG_STEP_1BLOCK"),
-              f_graph = forced("ADSG_STEP_GRAPHS");
+              f_graph = forced("ADSG_STEP_GRAPHS"), f_cluster = forced("ADSG_STEP_CLUSTER");
     const bool can_fuse = fusion_ok(c), can_one = step_1block_ok(c);
-    std::vector<int> modes;  // bit 0: pdl, bit 1: fuse, bit 2: one-block step, bit 3: graph replay
-    for (int m = 0; m < 16; ++m) {
-        const int pdl = m & 1, fuse = (m >> 1) & 1, one = (m >> 2) & 1, graph = (m >> 3) & 1;
+    // bit 0: pdl, bit 1: fuse, bit 2: one-launch step, bit 3: graph replay, bit 4: that step on a cluster
+    std::vector<int> modes;
+    for (int m = 0; m < 32; ++m) {
+        const int pdl = m & 1, fuse = (m >> 1) & 1, one = (m >> 2) & 1, graph = (m >> 3) & 1, cl = (m >> 4) & 1;
         if (fuse && !can_fuse) continue;
         if (one && !can_one) continue;
-        if (one && fuse) continue;  // the one-block step has no separate x pass
+        if (one && fuse) continue;  // the one-launch step has no separate x pass
+        if (cl && !one) continue;
         if (f_pdl >= 0 && pdl != f_pdl) continue;
         if (f_fuse >= 0 && fuse != (f_fuse && can_fuse)) continue;
         if (f_one >= 0 && one != (f_one && can_one)) continue;
         if (f_graph >= 0 && graph != f_graph) continue;
+        if (f_cluster >= 0 && one && cl != f_cluster) continue;
         modes.push_back(m);
     }
     if (modes.empty()) modes.push_back(0);
@@ -492,6 +497,7 @@ int autotune_launch_mode(adsg_ctx* c) {
         c->fuse_x = (m >> 1) & 1;
         c->step_1block = (m >> 2) & 1;
         c->step_graphs_on = (m >> 3) & 1;
+        c->step_cluster = (m >> 4) & 1;
     };
     if (modes.size() == 1) {
         apply(modes[0]);
@@ -516,6 +522,14 @@ int autotune_launch_mode(adsg_ctx* c) {
         };
         rc = step(c->ping, tmp);  // warm-up (also builds the dt bands and captures the graphs)
         if (rc == 0) rc = step(tmp, c->ping);
+        if (rc != 0 && c->step_cluster) {
+            // a cluster launch the device refuses drops the mode, not the context
+            cudaGetLastError();
+            if (cudaStreamSynchronize(c->stream) == cudaSuccess) {
+                rc = 0;
+                continue;
+            }
+        }
         if (rc == 0) e = cudaEventRecord(a, c->stream);
         for (int r = 0; r < reps && rc == 0 && e == cudaSuccess; ++r) {
             rc = step(c->ping, tmp);
@@ -1235,6 +1249,11 @@ int adsg_ctx_stage_work(const adsg_ctx* ctx, double* flops, double* bytes) {
                                     flops[ADSG_STAGE_SOLVE_Z];
     bytes[ADSG_STAGE_STEP_1BLOCK] = 16.0 * total;
     return 0;
+}
+
+int adsg_ctx_step_cluster(const adsg_ctx* ctx) {
+    if (!ctx) return -1;
+    return ctx->step_1block && ctx->step_cluster && step_1block_ok(ctx) ? 1 : 0;
 }
 
 int adsg_heat_steps_host(adsg_ctx* ctx, double* u_host, double dt, int nsteps) {

@@ -127,7 +127,8 @@ struct adsg_ctx {
     std::vector<adsg_adjoint*> adjoints;
     int pdl = 0;     // programmatic dependent launch for the step kernels (chosen at creation)
     int fuse_x = 0;  // the step fuses the x band pass with the x solve (chosen at creation)
-    int step_1block = 0;  // small 2D grids: the whole step in one block (chosen at creation)
+    int step_1block = 0;  // small 2D grids: the whole step in one launch (chosen at creation)
+    int step_cluster = 0;  // ... on a thread-block cluster rather than one block (chosen at creation)
 
     cudaEvent_t take_event() {
         if (!spare.empty()) {

@@ -6,6 +6,7 @@
 // work is arranged so that no FP64 operation is redundant, and loads, index
 // arithmetic and shared-memory traffic (which run on other pipes) are spent
 // freely to keep it busy.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,6 +58,10 @@ void set_launch_pdl(int on) { t_pdl_mode = on ? 1 : 0; }
 int launch_pdl_mode() { return t_pdl_mode; }
 
 static bool pdl_enabled() { return t_pdl_mode == 1; }
+
+static thread_local int t_small2d_cluster = 1;  // the small 2D step on a cluster (1) or one block (0)
+void set_small2d_cluster(int on) { t_small2d_cluster = on ? 1 : 0; }
+int small2d_cluster_mode() { return t_small2d_cluster; }
 
 template <typename... KArgs, typename... Args>
 static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
@@ -1625,6 +1630,88 @@ __global__ void __launch_bounds__(512) small2d_step_kernel(const double* __restr
     for (int g = threadIdx.x; g < N; g += blockDim.x) out[g] = R[g];
 }
 
+// The same step on a thread-block cluster of kSmallClusterCtas CTAs: the four
+// tensors live in the shared memory of the cluster's first CTA, every CTA
+// computes a share of the two band passes reading and writing them through
+// distributed shared memory (cluster barriers between the phases), and the
+// first CTA then runs both sweeps on its own shared memory and writes the
+// result.  The passes get the FP64 pipes of kSmallClusterCtas SMs instead of
+// one; the sweeps, latency-bound chains, stay on one SM.  Same device
+// functions as the separate kernels: the same bits.
+constexpr int kSmallClusterCtas = 8;
+
+template <int K>
+__global__ void __launch_bounds__(256) small2d_cluster_step_kernel(const double* __restrict__ u, double* __restrict__ out,
+                                                                   dim_dev X, dim_dev Y) {
+    namespace cg = cooperative_groups;
+    extern __shared__ double sm[];
+    constexpr int UNR = K > 2 ? 4 : 8;
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned rank = cluster.block_rank(), nblk = cluster.num_blocks();
+    const int nx = X.n, ny = Y.n, N = nx * ny;
+    // every CTA has the same dynamic shared memory: all decide alike, before any barrier
+    if (!ADSG_SMEM_RANGE(sm, 4LL * N)) return;
+    double* home = cluster.map_shared_rank(sm, 0);  // the first CTA's tensors
+    double* U = home;
+    double* A = home + N;
+    double* C = home + 2 * N;
+    double* R = home + 3 * N;
+    pdl_wait_and_release();  // the tables may come from the previous launch (the dt bands)
+    if (rank == 0) {
+        prefetch_step_tables<K>(X, true);
+        prefetch_step_tables<K>(Y, false);
+    }
+    const int tid = static_cast<int>(rank * blockDim.x + threadIdx.x), stride = static_cast<int>(nblk * blockDim.x);
+    for (int g = tid; g < N; g += stride) U[g] = u[g];
+    cluster.sync();
+    // y pass: A = My u, C = Ny u (pair sums on the symmetric rows, as launch_band_pass)
+    const int ylo = max(Y.sym_lo, K), yhi = min(Y.sym_hi, ny - K);
+    for (int g = tid; g < N; g += stride) {
+        if (yhi > ylo)
+            band_out<K, false, true, true, 0>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, ylo, yhi, N);
+        else
+            band_out<K, false, true, false, 0>(g, U, nullptr, A, C, Y.mrow, nullptr, Y.nrow, ny, nx, 0, 0, N);
+    }
+    cluster.sync();
+    // x pass: R = (-dt Kx) A + Mx C
+    for (int g = tid; g < N; g += stride)
+        band_out<K, true, false, false, 0>(g, A, C, R, nullptr, X.kdt, X.mrow, nullptr, nx, 1, 0, 0, N);
+    cluster.sync();  // nothing reads another CTA's shared memory after this
+    if (rank != 0) return;
+    double* Rl = sm + 3 * N;
+    small_sweeps<K, UNR>(Rl, Y, nx, 1, nx);  // y-lines: columns of R
+    __syncthreads();
+    small_sweeps<K, UNR>(Rl, X, ny, nx, 1);  // x-lines: rows of R
+    __syncthreads();
+    for (int g = threadIdx.x; g < N; g += blockDim.x) out[g] = Rl[g];
+}
+
+template <int K>
+static cudaError_t launch_small2d_cluster(const double* u, double* out, const dim_dev& x, const dim_dev& y, size_t smem,
+                                          cudaStream_t s) {
+    auto kern = small2d_cluster_step_kernel<K>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(kern), smem);
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kSmallClusterCtas);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kSmallClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, u, out, x, y);
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
 size_t small2d_smem(const dim_dev& x, const dim_dev& y) { return sizeof(double) * 4 * static_cast<size_t>(x.n) * y.n; }
 
 bool small2d_step_ok(const dim_dev& x, const dim_dev& y) {
@@ -1638,6 +1725,14 @@ bool small2d_step_ok(const dim_dev& x, const dim_dev& y) {
 cudaError_t launch_small2d_step(const double* u, double* out, const dim_dev& x, const dim_dev& y, cudaStream_t s) {
     if (!small2d_step_ok(x, y)) return cudaErrorInvalidValue;
     const size_t smem = small2d_smem(x, y);
+    if (small2d_cluster_mode()) {
+        switch (x.p) {
+            case 1: return launch_small2d_cluster<1>(u, out, x, y, smem, s);
+            case 2: return launch_small2d_cluster<2>(u, out, x, y, smem, s);
+            case 3: return launch_small2d_cluster<3>(u, out, x, y, smem, s);
+            default: return launch_small2d_cluster<4>(u, out, x, y, smem, s);
+        }
+    }
     auto go = [&](auto kern) -> cudaError_t {
         if (smem > 48 * 1024) {
             cudaError_t e = ensure_smem_attribute(reinterpret_cast<const void*>(kern), smem);

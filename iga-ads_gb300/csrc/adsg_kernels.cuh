@@ -178,6 +178,10 @@ bool rhs_x_solve_ok(const dim_dev& d, const line_layout& L);
 // A whole 2D step (the step view's passes and two-ended unit-diagonal sweeps)
 // in one block, for grids whose four working tensors fit in shared memory.
 bool small2d_step_ok(const dim_dev& x, const dim_dev& y);
+// Whether launch_small2d_step runs on a thread-block cluster (1, default) or one block (0),
+// per calling thread.
+void set_small2d_cluster(int on);
+int small2d_cluster_mode();
 cudaError_t launch_small2d_step(const double* u, double* out, const dim_dev& x, const dim_dev& y, cudaStream_t s);
 cudaError_t launch_rhs_x_solve(const double* in0, const double* in1, double* out, const double* A0, const double* A1,
                                const dim_dev& d, const line_layout& L, cudaStream_t s);

@@ -199,6 +199,12 @@ int adsg_ctx_fused_x(const adsg_ctx* ctx);
  * two-ended sweep; chosen at creation by timing, ADSG_STEP_1BLOCK=0/1 forces
  * it), 0 when not, -1 for a NULL context.  Results do not depend on it. */
 int adsg_ctx_step_1block(const adsg_ctx* ctx);
+/* 1 when that one-launch step runs on a thread-block cluster (8 CTAs: the
+ * band passes spread over their SMs through distributed shared memory, the
+ * sweeps in the first CTA), 0 when on one block or not used; chosen at
+ * creation by timing both, ADSG_STEP_CLUSTER=0/1 forces it; -1 for NULL.
+ * Results do not depend on it. */
+int adsg_ctx_step_cluster(const adsg_ctx* ctx);
 /* 1 when adsg_heat_step replays a cached single-step CUDA graph per
  * (u_prev, u_next, dt) (up to four, the least recently used replaced; steps
  * issued into a stream under capture, with stage timers on, or with buffers

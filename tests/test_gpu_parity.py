@@ -376,22 +376,26 @@ def test_failure_detection_counts_nonfinite(cuda):
                                         ((3,), (64,)), ((4, 4), (25, 14)), ((1, 1), (40, 9))])
 def test_launch_mode_does_not_change_results(p, elements, cuda, monkeypatch):
     """Programmatic dependent launch only moves when the next kernel's blocks
-    are scheduled, and the one-block 2D step runs the separate kernels'
-    operations in the same order: those modes agree bitwise.  The fused x
+    are scheduled, and the one-launch 2D step (on one block or on a
+    thread-block cluster) runs the separate kernels' operations in the same
+    order: those modes agree bitwise.  The fused x
     pass + x solve solves x first (the others solve x last), so the fused
     modes agree bitwise among themselves and with the rest to rounding."""
     out = []
-    for pdl, fuse, one in (("0", "0", "0"), ("1", "0", "0"), ("0", "1", "0"), ("1", "1", "0"), ("0", "0", "1"),
-                           ("1", "0", "1")):
+    for pdl, fuse, one, cluster in (("0", "0", "0", "0"), ("1", "0", "0", "0"), ("0", "1", "0", "0"),
+                                    ("1", "1", "0", "0"), ("0", "0", "1", "0"), ("1", "0", "1", "0"),
+                                    ("0", "0", "1", "1"), ("1", "0", "1", "1")):
         monkeypatch.setenv("ADSG_PDL", pdl)
         monkeypatch.setenv("ADSG_FUSE_X", fuse)
         monkeypatch.setenv("ADSG_STEP_1BLOCK", one)
+        monkeypatch.setenv("ADSG_STEP_CLUSTER", cluster)
         monkeypatch.setenv("ADSG_SOLVE_VARIANT", "5")
         dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
         ctx = ads.Context(dims)
         assert ctx.launch_pdl() == (pdl == "1")
         assert ctx.fused_x() == (fuse == "1" and one == "0")
         assert ctx.step_1block() == (one == "1" and len(p) == 2 and p[0] == p[1])
+        assert ctx.step_cluster() == (ctx.step_1block() and cluster == "1")
         u = np.random.default_rng(3).uniform(-1, 1, ctx.size)
         ctx.heat_steps_host(u, 1e-5, 5)
         r = np.empty_like(u)
