@@ -496,7 +496,7 @@ def run_ours(args, cfg):
                    "parallelism": f"replicas x{world}"},
         "tuning": {"solve_variants": ctx.solve_variants(), "step_solve_variants": ctx.step_solve_variants(),
                    "launch_pdl": ctx.launch_pdl(), "fused_x": ctx.fused_x(), "step_1block": ctx.step_1block(),
-                   "step_graphs": ctx.step_graphs(), "rhs": "factored quadrature (1D Gauss-assembled bands)"},
+                   "step_cluster": ctx.step_cluster(), "step_graphs": ctx.step_graphs(), "rhs": "factored quadrature (1D Gauss-assembled bands)"},
         "e2e": {"value": e2e, "unit": "DOF-updates/s", "h2d_bytes_per_step": 8 * size, "d2h_bytes_per_step": 8 * size,
                 "steps": ke, "entry": "adsg_heat_steps_host"},
         "gpu_launches": sum(v["launches"] for v in per_stage.values()),

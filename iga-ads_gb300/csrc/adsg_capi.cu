@@ -514,7 +514,11 @@ int autotune_launch_mode(adsg_ctx* c) {
     if (e == cudaSuccess) e = cudaEventCreate(&b);
     float best = 1e30f;
     int best_mode = modes[0], rc = 0;
-    const int reps = 4;
+    // steps of small grids take tens of microseconds: time enough of them
+    // that launch jitter does not pick the mode
+    const int reps = c->size < (1 << 20) ? 32 : 4;
+    const char* logv = std::getenv("ADSG_AUTOTUNE_LOG");
+    const bool log = logv && *logv == '1';
     for (size_t i = 0; i < modes.size() && e == cudaSuccess && rc == 0; ++i) {
         apply(modes[i]);
         auto step = [&](const double* p, double* q) {
@@ -539,6 +543,10 @@ int autotune_launch_mode(adsg_ctx* c) {
         if (rc == 0 && e == cudaSuccess) e = cudaEventSynchronize(b);
         float ms = 0.f;
         if (rc == 0 && e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        if (rc == 0 && e == cudaSuccess && log)
+            std::fprintf(stderr, "ads_gb300 autotune: launch mode pdl=%d fuse_x=%d one_launch=%d graphs=%d cluster=%d %.2f us/step\n",
+                         modes[i] & 1, (modes[i] >> 1) & 1, (modes[i] >> 2) & 1, (modes[i] >> 3) & 1,
+                         (modes[i] >> 4) & 1, 1e3 * ms / (2 * reps));
         if (rc == 0 && e == cudaSuccess && ms < best) {
             best = ms;
             best_mode = modes[i];
