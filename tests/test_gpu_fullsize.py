@@ -118,6 +118,28 @@ def test_heat_260cubed_p4_run(cuda):
           if "self_uN" in g.files else 0.0)
 
 
+_MIXED_REF = {}  # instance -> oracle result, and the oracle's own spread once measured
+
+
+def _mixed_ref(i, pr, u0, dt):
+    if i not in _MIXED_REF:
+        _MIXED_REF[i] = {"ref": pr.heat_steps(u0, dt, 2, nthreads=THREADS)}
+    return _MIXED_REF[i]
+
+
+def _mixed_spread(i, pr, u0, dt):
+    """The largest pairwise disagreement among the oracle's sequential element
+    loop and its executor on several thread counts (the CPU forms of the
+    reference's algorithm) at instance i."""
+    c = _MIXED_REF[i]
+    if "spread" not in c:
+        forms = [c["ref"], pr.heat_steps(u0, dt, 2)]
+        for t in sorted({max(2, THREADS - 3), max(2, THREADS - 5), max(2, THREADS // 2)}):
+            forms.append(pr.heat_steps(u0, dt, 2, nthreads=t))
+        c["spread"] = max(oracle.rel_l2(a, b) for k, a in enumerate(forms) for b in forms[k + 1:])
+    return c["spread"]
+
+
 @pytest.mark.parametrize("engine", ["0", "1"])
 def test_mixed_64_batch_against_oracle(engine, cuda, monkeypatch):
     """Both batch engines (persistent kernel, concurrent per-instance graph) on
@@ -139,17 +161,9 @@ def test_mixed_64_batch_against_oracle(engine, cuda, monkeypatch):
     worst = 0.0
     for i, (nd, p, e, dt) in enumerate(specs):
         pr = oracle.Problem([p] * nd, [e] * nd)
-        ref = pr.heat_steps(u0[i], dt, 2, nthreads=THREADS)
+        ref = _mixed_ref(i, pr, u0[i], dt)["ref"]
         err = oracle.rel_l2(b.get_state(i), ref)
-        spread = 0.0
-        if err > 2 * STEP:
-            # the CPU forms of the reference's algorithm: the sequential element
-            # loop and the executor on several thread counts; their largest
-            # pairwise disagreement
-            forms = [ref, pr.heat_steps(u0[i], dt, 2)]
-            for t in sorted({max(2, THREADS - 3), max(2, THREADS - 5), max(2, THREADS // 2)}):
-                forms.append(pr.heat_steps(u0[i], dt, 2, nthreads=t))
-            spread = max(oracle.rel_l2(a, b) for k, a in enumerate(forms) for b in forms[k + 1:])
+        spread = _mixed_spread(i, pr, u0[i], dt) if err > 2 * STEP else 0.0
         check(f"engine {engine} instance {i} {nd}D p={p} {e} elements 2 steps", err, 2 * STEP, spread)
         worst = max(worst, err)
     print(f"[parity] engine {engine}: worst instance rel L2 {worst:.3e}")
