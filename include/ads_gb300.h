@@ -98,7 +98,7 @@ const char* adsg_last_error(void);
 /* ---- the hot path (device buffers) ---------------------------------------- */
 
 /* heat_3d::compute_rhs (reference examples/heat/heat_3d.hpp:49-67; 2D:
- * heat_2d.hpp:166-192): rhs_a = sum_e sum_q w_q J_e (u v_a - dt grad u . grad v_a)
+ * heat_2d.hpp:80-106): rhs_a = sum_e sum_q w_q J_e (u v_a - dt grad u . grad v_a)
  * with u from u_prev.  Computed by the factored quadrature: the tensor-product
  * Gauss rule and the separable Jacobian make the element sum equal to
  * (Mx(x)My(x)Mz - dt (Kx(x)My(x)Mz + Mx(x)Ky(x)Mz + Mx(x)My(x)Kz)) u_prev with the

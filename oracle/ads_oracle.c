@@ -430,7 +430,7 @@ int orc_problem_dim(const orc_problem* pr, int d, double* btab, double* w, doubl
 }
 
 /* ------------------------------------------------------------------------ */
-/* Heat RHS (heat_3d.hpp:49-67; 2D heat_2d.hpp:166-192).                     */
+/* Heat RHS (heat_3d.hpp:49-67; 2D heat_2d.hpp:80-106).                      */
 /* Loop order of util/iter/product.hpp: the last index runs fastest, so     */
 /* elements, quadrature points and dofs iterate with z (or y in 2D) inner.  */
 /* ------------------------------------------------------------------------ */

@@ -68,14 +68,14 @@ long orc_problem_size(const orc_problem* pr);
 int orc_problem_dim(const orc_problem* pr, int d, double* btab, double* w, double* J,
                     int* first_dofs, double* mass_ab, double* lu_ab, int* ipiv);
 
-/* heat_3d::compute_rhs (heat_3d.hpp:49-67) / heat_2d (heat_2d.hpp:166-192),
+/* heat_3d::compute_rhs (heat_3d.hpp:49-67) / heat_2d (heat_2d.hpp:80-106),
  * with eval_fun hoisted out of the dof loop as in scalability/test3d.hpp:79
  * (same arithmetic).  Sequential, in the reference's loop order. */
 int orc_heat_rhs(const orc_problem* pr, const double* u_prev, double* rhs, double dt);
 
 /* The same RHS with the executor pattern (for_each over elements + a local
  * element tile + synchronized scatter, executor/galois.hpp:27-44 with
- * heat_2d.hpp:172-190), on nthreads host threads. */
+ * heat_2d.hpp:86-104), on nthreads host threads. */
 int orc_heat_rhs_mt(const orc_problem* pr, const double* u_prev, double* rhs, double dt,
                     int nthreads);
 

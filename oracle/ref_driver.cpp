@@ -105,8 +105,8 @@ struct output_manager<2> {
 
 namespace {
 
-// 3D heat step in the executor form of heat_2d.hpp:166-192 /
-// scalability/test3d.hpp:223-251 (eval_fun hoisted, local element tile,
+// 3D heat step in the executor form of heat_2d.hpp:80-106 /
+// scalability/test3d.hpp:66-95 (eval_fun hoisted, local element tile,
 // synchronized scatter), driven by the reference's sequential_executor or by
 // the galois_executor stand-in above on several threads.
 template <typename Exec>
