@@ -166,6 +166,7 @@ def library() -> ctypes.CDLL:
         "adsg_batch_tuning": (i, [vp, _c_int_p, _c_int_p]),
         "adsg_batch_engine": (i, [vp]),
         "adsg_batch_test_waits": (i, [vp, i, ll]),
+        "adsg_test_fail_device_alloc": (i, [i]),
         "adsg_debug_bounds": (i, [ctypes.POINTER(ll), _c_int_p, _c_int_p, ctypes.POINTER(ll), ctypes.POINTER(ll), i]),
         "adsg_dgbtrs_": (i, [ctypes.c_char_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_double_p, _c_int_p,
                              _c_int_p, _c_double_p, _c_int_p, _c_int_p]),
@@ -192,6 +193,13 @@ def debug_bounds(reset: bool = False) -> dict:
     files = ("adsg_kernels.cu", "adsg_elem.cu", "adsg_quad.cu")
     return {"violations": v.value, "file": files[f.value] if 0 <= f.value < 3 else None, "line": line.value,
             "index": idx.value, "extent": ext.value}
+
+
+def test_fail_device_alloc(k: int) -> int:
+    """Test hook: the k-th device allocation of the library from now on
+    fails as on a full device (ADSG_ERR_NOMEM), then the hook is off; -1 turns
+    it off.  Returns the previous setting (-1: no failure was pending)."""
+    return int(library().adsg_test_fail_device_alloc(int(k)))
 
 
 def _check(code: int) -> None:

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -27,7 +28,22 @@ int fail(int code, const char* msg) {
 
 int fail_cuda(int err, const char* where) {
     g_last_error = std::string(where) + ": " + cudaGetErrorString(static_cast<cudaError_t>(err));
-    return ADSG_ERR_CUDA;
+    return err == cudaErrorMemoryAllocation ? ADSG_ERR_NOMEM : ADSG_ERR_CUDA;
+}
+
+// Allocation-failure hook: the k-th device allocation from now fails (k >= 0,
+// counted across threads), then the hook turns itself off; -1 = off.
+std::atomic<int> g_alloc_fail_in{-1};
+
+cudaError_t device_alloc(void** p, size_t bytes) {
+    int k = g_alloc_fail_in.load();
+    while (k >= 0 && !g_alloc_fail_in.compare_exchange_weak(k, k - 1)) {
+    }
+    if (k == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
 }
 
 }  // namespace adsg
@@ -504,7 +520,7 @@ int autotune_launch_mode(adsg_ctx* c) {
         return 0;
     }
     double* tmp = nullptr;
-    if (cudaMalloc(&tmp, sizeof(double) * c->size) != cudaSuccess) {  // no room: keep plain launches
+    if (device_alloc(reinterpret_cast<void**>(&tmp), sizeof(double) * c->size) != cudaSuccess) {  // no room: keep plain launches
         cudaGetLastError();
         apply(modes[0]);
         return 0;
@@ -1403,6 +1419,8 @@ int adsg_dgbtrs_(const char* trans, const int* n, const int* kl, const int* ku, 
     }
     return 0;
 }
+
+int adsg_test_fail_device_alloc(int k) { return g_alloc_fail_in.exchange(k < 0 ? -1 : k); }
 
 int adsg_debug_bounds(long long* violations, int* file, int* line, long long* index, long long* extent, int reset) {
     if (!violations) return fail(-1, "violations is NULL");

@@ -32,7 +32,7 @@ struct dev_arena {
     template <typename T>
     cudaError_t alloc(T** out, size_t count) {
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        cudaError_t e = device_alloc(&p, std::max<size_t>(count, 1) * sizeof(T));
         if (e != cudaSuccess) return e;
         blocks.push_back(p);
         *out = static_cast<T*>(p);

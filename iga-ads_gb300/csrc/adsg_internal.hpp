@@ -76,7 +76,12 @@ int ctx_prepare_dt(adsg_ctx* c, double dt);
 
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const char* msg);
+// A CUDA error: ADSG_ERR_NOMEM for a failed allocation, else ADSG_ERR_CUDA.
 int fail_cuda(int err, const char* where);
+
+// Every device allocation of the library: cudaMalloc, unless the test hook
+// (adsg_test_fail_device_alloc) makes this one fail as a full device would.
+cudaError_t device_alloc(void** p, size_t bytes);
 
 }  // namespace adsg
 

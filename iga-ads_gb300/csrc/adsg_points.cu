@@ -36,7 +36,8 @@ int qpool_get(adsg_ctx* c, size_t doubles, double** out) {
             c->qpool = nullptr;
             c->qpool_size = 0;
         }
-        ADSG_CUDA_TRY(cudaMalloc(&c->qpool, doubles * sizeof(double)), "Gauss-point work space");
+        ADSG_CUDA_TRY(device_alloc(reinterpret_cast<void**>(&c->qpool), doubles * sizeof(double)),
+                      "Gauss-point work space");
         c->qpool_size = doubles;
     }
     *out = c->qpool;

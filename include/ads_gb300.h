@@ -427,6 +427,18 @@ int adsg_batch_test_waits(adsg_batch* b, int extra_items, long long spin_limit);
  * ADSG_ERR_UNSUPPORTED in the release build. */
 int adsg_debug_bounds(long long* violations, int* file, int* line, long long* index, long long* extent, int reset);
 
+/* ---- test hook: a device allocation that fails ---------------------------
+ * No reference counterpart.  Makes the k-th device allocation of the library
+ * from now on (k >= 0, counted across threads) fail as cudaMalloc does on a
+ * full device, after which the hook turns itself off; k = -1 turns it off.
+ * Every allocation goes through it: contexts (tables, state and work
+ * tensors, the launch-mode tuner's buffer), Gauss-point work space,
+ * adjoints and batches.  The call that meets the failure returns
+ * ADSG_ERR_NOMEM with nothing leaked, and the next call works.  Returns the
+ * previous setting (how many allocations were still to pass, -1 if none was
+ * pending). */
+int adsg_test_fail_device_alloc(int k);
+
 /* ---- the heat RHS without any allocation --------------------------------
  * No counterpart in the reference: an addition for callers that cannot call
  * cudaMalloc -- code running inside a host application that owns every
