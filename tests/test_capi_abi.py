@@ -129,6 +129,16 @@ def test_ctx_create_rejects_bad_arguments_without_gpu():
     assert b"invalid" in lib.adsg_last_error()
 
 
+def test_ctx_create_rejects_tensors_beyond_int32_indexing_without_gpu():
+    """1300^3 dofs (> 2^31) is refused with -2 before any device call."""
+    lib = ads.library()
+    d = ads.Dimension(2, 1298)
+    descs = (ads.DimDesc * 3)(d._desc, d._desc, d._desc)
+    h = ctypes.c_void_p()
+    assert lib.adsg_ctx_create(3, descs, ctypes.byref(h)) == -2
+    assert b"2^31" in lib.adsg_last_error() and not h.value
+
+
 def test_device_entry_points_reject_null_context():
     lib = ads.library()
     assert lib.adsg_heat_rhs(None, None, None, 1.0) == -1
