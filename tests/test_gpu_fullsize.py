@@ -7,8 +7,10 @@
   reference sources) and the whole field against the multi-threaded oracle;
 - 260^3 dofs, p = 4, dt = 1e-6, 20 steps (unstable at this dt: the top modes
   grow ~16.6x per step, so errors are relative L2 after scaling by the
-  largest entry): one whole step against the multi-threaded oracle, and the
-  first and last steps against the reference's own run;
+  largest entry): one whole step against the multi-threaded oracle, the
+  first and last steps against the reference's own run, and the last step
+  against the oracle's own 20-step run (tests/golden/run_3d_p4_e256_oracle.npz,
+  made by tests/golden/oracle_run.py);
 - the seeded mixed 64-instance batch (sides up to 512^2 and 96^3, p in
   {2, 3, 4}), two steps under both batch engines, instance by instance against
   the oracle.
@@ -69,6 +71,17 @@ def _vs_run(u, g, prefix, n, ctx):
     return max(errs)
 
 
+def _records_apart(a, b, prefix):
+    """The largest relative difference between two records of the same run
+    (planes, L2 and mass norms): how far two CPU forms drifted apart."""
+    errs = [oracle.rel_l2(a[prefix + "plane_z"], b[prefix + "plane_z"])]
+    if prefix + "plane_y" in a.files and prefix + "plane_y" in b.files:
+        errs.append(oracle.rel_l2(a[prefix + "plane_y"], b[prefix + "plane_y"]))
+    for k in ("norm", "mass_norm"):
+        errs.append(abs(float(a[prefix + k]) - float(b[prefix + k])) / float(b[prefix + k]))
+    return max(errs)
+
+
 def _initial(dims, g):
     u0 = inputs.initial_field(dims, seed=int(g["seed"]))
     # the field is recomputed here; it must be the one the reference started from
@@ -114,8 +127,13 @@ def test_heat_260cubed_p4_run(cuda):
     d_cpu1 = _vs_run(ref1, g, "u1_", n, None)  # oracle against the reference after one step
     check("260^3 p=4 1 step vs oracle (whole field)", oracle.rel_l2(u1, ref1), STEP, d_cpu1)
     check("260^3 p=4 1 step vs reference run", _vs_run(u1, g, "u1_", n, ctx), STEP, d_cpu1)
-    check(f"260^3 p=4 {N} steps vs reference run", _vs_run(uN, g, "uN_", n, ctx), RUN, float(g["self_uN"])
-          if "self_uN" in g.files else 0.0)
+    # the run's other CPU form: the oracle's executor over the same 20 steps
+    # (tests/golden/oracle_run.py), recorded like the reference's run
+    o = _fixture("run_3d_p4_e256_oracle")
+    assert int(o["nsteps"]) == N and abs(float(o["u0_norm"]) - float(g["u0_norm"])) <= 1e-14 * float(g["u0_norm"])
+    d_cpuN = _records_apart(o, g, "uN_")
+    check(f"260^3 p=4 {N} steps vs reference run", _vs_run(uN, g, "uN_", n, ctx), RUN, d_cpuN)
+    check(f"260^3 p=4 {N} steps vs oracle run", _vs_run(uN, o, "uN_", n, ctx), RUN, d_cpuN)
 
 
 _MIXED_REF = {}  # instance -> oracle result, and the oracle's own spread once measured
