@@ -165,6 +165,7 @@ def library() -> ctypes.CDLL:
         "adsg_batch_synchronize": (i, [vp]),
         "adsg_batch_tuning": (i, [vp, _c_int_p, _c_int_p]),
         "adsg_batch_engine": (i, [vp]),
+        "adsg_batch_order": (i, [vp]),
         "adsg_batch_test_waits": (i, [vp, i, ll]),
         "adsg_test_fail_device_alloc": (i, [i]),
         "adsg_debug_bounds": (i, [ctypes.POINTER(ll), _c_int_p, _c_int_p, ctypes.POINTER(ll), ctypes.POINTER(ll), i]),
@@ -591,8 +592,10 @@ class Batch:
         g = ctypes.c_int()
         _check(library().adsg_batch_tuning(self._h, ctypes.byref(b), ctypes.byref(g)))
         engine = library().adsg_batch_engine(self._h)
+        order = library().adsg_batch_order(self._h)
         return {"blocks_per_sm": b.value, "graph": bool(g.value),
-                "engine": "concurrent" if engine == 1 else "persistent"}
+                "engine": "concurrent" if engine == 1 else "persistent",
+                "order": "wavefront" if order == 1 else "stage-major"}
 
 
 def batch_specs(seed: int = 0, n2d: int = 32, n3d: int = 32, dt: float = 1e-6):

@@ -61,6 +61,7 @@ struct adsg_batch {
     cudaStream_t stream = nullptr;
     int par = 0;            // which buffer holds the state
     int blocks_per_sm = 1;  // autotuned
+    int order = 0;          // autotuned: 0 stage-major, 1 wavefront over instance groups (pair_order)
     int sms = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_steps = -1, graph_par = -1;
@@ -88,6 +89,45 @@ struct adsg_batch {
     } while (0)
 
 namespace {
+
+// Bytes of the L2 that one dof of a wavefront group may take: up to six
+// groups are in flight (one per stage), each with about three live tensors.
+constexpr long long kWavefrontBytesPerDof = 6 * 3 * 8;
+
+// The order in which one step's (stage, instance) pairs are handed out
+// (entries stage * count + instance).  0, stage-major: every instance's stage
+// 0, then every instance's stage 1, and so on; all instances' tensors are live
+// at once.  1, wavefront: the instances in consecutive groups of at most
+// group_dofs dofs (an instance above that is a group of its own), group g
+// running stage w - g in wave w, the groups further along first within a wave,
+// so that only the groups of six consecutive waves hold live tensors.  In both
+// a pair comes after the pair it waits for (the same instance's stage before,
+// or the last stage of the step before), which is all the kernel's waits need;
+// the items compute the same outputs in either order.
+std::vector<int> pair_order(const std::vector<batch_inst>& inst, int wavefront, long long group_dofs) {
+    const int count = static_cast<int>(inst.size());
+    std::vector<int> order;
+    order.reserve(6 * static_cast<size_t>(count));
+    if (!wavefront) {
+        for (int k = 0; k < 6 * count; ++k) order.push_back(k);
+        return order;
+    }
+    std::vector<std::vector<int>> groups;
+    long long acc = 0;
+    for (int i = 0; i < count; ++i) {
+        if (groups.empty() || (acc > 0 && acc + inst[i].size > group_dofs)) {
+            groups.emplace_back();
+            acc = 0;
+        }
+        groups.back().push_back(i);
+        acc += inst[i].size;
+    }
+    const int G = static_cast<int>(groups.size());
+    for (int w = 0; w < G + 5; ++w)
+        for (int g = std::max(0, w - 5); g <= std::min(G - 1, w); ++g)
+            for (int i : groups[g]) order.push_back((w - g) * count + i);
+    return order;
+}
 
 int launch_steps(adsg_batch* b, int nsteps, int blocks_per_sm) {
     // completion counts and the work counter start at zero in every launch
@@ -348,23 +388,36 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
             std::copy(u, u + 6, I.units);
         }
     }
-    // one step's items in stage-major order: prefix[stage * count + i]
-    std::vector<long long> prefix(6 * static_cast<size_t>(count) + 1, 0);
     for (int st = 0; st < 6; ++st)
         for (int i = 0; i < count; ++i) {
             batch_inst& I = b->inst[i];
             const long long per = batch_units_per_item(st, I.twisted);
             I.items[st] = static_cast<int>((I.units[st] + per - 1) / per);
-            const size_t k = static_cast<size_t>(st) * count + i;
-            prefix[k + 1] = prefix[k] + I.items[st];
         }
+    // the two orders of a step's pairs, and their item prefixes
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    std::vector<int> order[2];
+    std::vector<long long> prefix[2];
+    for (int o = 0; o < 2; ++o) {
+        order[o] = pair_order(b->inst, o, std::max(1LL, static_cast<long long>(l2) / kWavefrontBytesPerDof));
+        prefix[o].assign(order[o].size() + 1, 0);
+        for (size_t k = 0; k < order[o].size(); ++k) {
+            const int st = order[o][k] / count, i = order[o][k] % count;
+            prefix[o][k + 1] = prefix[o][k] + b->inst[i].items[st];
+        }
+    }
     batch_inst* dinst = nullptr;
-    long long* dprefix = nullptr;
+    int* dorder[2] = {nullptr, nullptr};
+    long long* dprefix[2] = {nullptr, nullptr};
     unsigned* done = nullptr;
     unsigned long long* next = nullptr;
     int* err = nullptr;
     e = b->mem.upload(&dinst, b->inst.data(), b->inst.size(), b->stream);
-    if (e == cudaSuccess) e = b->mem.upload(&dprefix, prefix.data(), prefix.size(), b->stream);
+    for (int o = 0; o < 2; ++o) {
+        if (e == cudaSuccess) e = b->mem.upload(&dorder[o], order[o].data(), order[o].size(), b->stream);
+        if (e == cudaSuccess) e = b->mem.upload(&dprefix[o], prefix[o].data(), prefix[o].size(), b->stream);
+    }
     if (e == cudaSuccess) e = b->mem.alloc(&done, 6 * static_cast<size_t>(count));
     if (e == cudaSuccess) e = b->mem.alloc(&next, 1);
     if (e == cudaSuccess) e = b->mem.alloc(&err, 1);
@@ -373,32 +426,46 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
     if (e != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
     b->B.count = count;
     b->B.inst = dinst;
-    b->B.prefix = dprefix;
-    b->B.per_step = prefix.back();
+    b->B.per_step = prefix[0].back();  // the same items in either order
     b->B.done = done;
     b->B.next = next;
     b->B.err = err;
+    auto use_order = [&](int o) {
+        b->order = o;
+        b->B.pair = dorder[o];
+        b->B.prefix = dprefix[o];
+    };
 
-    // autotune the persistent grid on the zero state (the state is reset after)
+    // autotune the persistent grid and the order on the zero state (the state
+    // is reset after); ADSG_BATCH_ORDER=0/1 forces the order
     const int maxb = std::max(1, batch_max_blocks_per_sm());
+    const char* fo = std::getenv("ADSG_BATCH_ORDER");
+    const int forced_order = fo && (*fo == '0' || *fo == '1') ? *fo - '0' : -1;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
     float best = 1e30f;
-    for (int bps = 1; bps <= maxb; ++bps) {
-        int st = launch_steps(b, 1, bps);  // warm-up
-        if (st) break;
-        cudaEventRecord(t0, b->stream);
-        st = launch_steps(b, 2, bps);
-        cudaEventRecord(t1, b->stream);
-        if (st || cudaEventSynchronize(t1) != cudaSuccess) break;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, t0, t1);
-        if (ms < best) {
-            best = ms;
-            b->blocks_per_sm = bps;
+    int best_order = forced_order >= 0 ? forced_order : 0;
+    for (int o = 0; o < 2; ++o) {
+        if (forced_order >= 0 && o != forced_order) continue;
+        use_order(o);
+        for (int bps = 1; bps <= maxb; ++bps) {
+            int st = launch_steps(b, 1, bps);  // warm-up
+            if (st) break;
+            cudaEventRecord(t0, b->stream);
+            st = launch_steps(b, 2, bps);
+            cudaEventRecord(t1, b->stream);
+            if (st || cudaEventSynchronize(t1) != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (ms < best) {
+                best = ms;
+                b->blocks_per_sm = bps;
+                best_order = o;
+            }
         }
     }
+    use_order(best_order);
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     if (int st = check_error_word(b)) return bail(st);
@@ -557,6 +624,8 @@ int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captur
 }
 
 int adsg_batch_engine(const adsg_batch* b) { return b ? b->engine : -1; }
+
+int adsg_batch_order(const adsg_batch* b) { return b ? b->order : -1; }
 
 int adsg_batch_test_waits(adsg_batch* b, int extra_items, long long spin_limit) {
     if (!b) return fail(-1, "batch is NULL");

@@ -2311,12 +2311,12 @@ __global__ void __launch_bounds__(256) batch_steps_kernel(batch_dev B, int nstep
         if (item >= total) return;
         const int t = static_cast<int>(item / B.per_step);
         const long long r = item - static_cast<long long>(t) * B.per_step;
-        int lo = 0, hi = pairs;  // (stage, instance) pair k with prefix[k] <= r < prefix[k+1]
+        int lo = 0, hi = pairs;  // the position k with prefix[k] <= r < prefix[k+1]
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
             if (B.prefix[mid] <= r) lo = mid; else hi = mid;
         }
-        const int stage = lo / B.count, i = lo - stage * B.count;
+        const int k = B.pair[lo], stage = k / B.count, i = k - stage * B.count;
         const batch_inst& I = B.inst[i];
         const long long it = r - B.prefix[lo];
         if (threadIdx.x == 0) s_go = batch_wait(B, I, i, stage, t);

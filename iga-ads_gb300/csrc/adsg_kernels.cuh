@@ -115,7 +115,11 @@ struct batch_inst {
 struct batch_dev {
     int count = 0;
     const batch_inst* inst = nullptr;  // device array [count]
-    const long long* prefix = nullptr;  // device array [6 count + 1]: items of one step before (stage, instance)
+    // one step's (stage, instance) pairs in the order their items are handed
+    // out: pair[k] = stage * count + instance at position k, prefix[k] the
+    // step's items before position k
+    const int* pair = nullptr;          // device array [6 count]
+    const long long* prefix = nullptr;  // device array [6 count + 1]
     long long per_step = 0;             // items of one step
     unsigned* done = nullptr;           // device array [count][6]: items completed in this launch
     unsigned long long* next = nullptr;  // the work counter (zeroed before each launch)

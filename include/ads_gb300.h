@@ -404,6 +404,13 @@ int adsg_batch_tuning(const adsg_batch* b, int* blocks_per_sm, int* graph_captur
  * per-instance chains (each instance's own tuned step kernels, run side by
  * side); -1 for a NULL batch.  ADSG_BATCH_ENGINE=0/1 forces it. */
 int adsg_batch_engine(const adsg_batch* b);
+/* The order in which the persistent kernel hands out a step's work, chosen
+ * with its grid by timing: 0 stage-major (every instance's first stage, then
+ * every instance's second, ...), 1 a wavefront over groups of instances whose
+ * tensors fit in L2 together (group g runs stage w - g in wave w, so few
+ * groups' tensors are live at once); -1 for a NULL batch.  Results do not
+ * depend on it.  ADSG_BATCH_ORDER=0/1 forces it. */
+int adsg_batch_order(const adsg_batch* b);
 /* Test hook for failure detection (no reference counterpart): every wait of
  * the persistent kernel for an instance's previous stage expects
  * extra_items completed work items beyond those that exist (nonzero: no

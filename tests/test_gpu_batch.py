@@ -87,6 +87,28 @@ def test_mixed_64_batch_matches_plain_kernels(cuda):
             check(f"mixed-64 batch vs looped {specs[i]}", err, 2 * STEP, oracle_self(pr, u0[i], dt, 2))
 
 
+def test_item_order_does_not_change_results(cuda, monkeypatch):
+    """The persistent kernel hands out the same items in either order
+    (stage-major, or a wavefront over groups of instances that fit in L2
+    together): bitwise equal states on the seeded 64-instance set."""
+    monkeypatch.setenv("ADSG_BATCH_ENGINE", "0")
+    specs = ads.batch_specs(seed=0)
+    rng = np.random.default_rng(4)
+    out = []
+    for order in ("0", "1"):
+        monkeypatch.setenv("ADSG_BATCH_ORDER", order)
+        b = ads.Batch(specs)
+        assert b.tuning()["order"] == ("wavefront" if order == "1" else "stage-major")
+        for i, n in enumerate(b.sizes):
+            b.set_state(i, np.random.default_rng(100 + i).uniform(-1, 1, n))
+        b.steps(3)
+        b.synchronize()
+        out.append([b.get_state(i) for i in range(len(specs))])
+        b.close()
+    for i in range(len(specs)):
+        np.testing.assert_array_equal(out[0][i], out[1][i])
+
+
 def test_batch_rejects_bad_specs():
     with pytest.raises(ads.AdsError):
         ads.Batch([(4, 2, 8, 1e-6)])
