@@ -476,7 +476,7 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
     b->par = 0;
     if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return bail(fail_cuda(e, "batch set-up"));
     // engine: the persistent kernel (best grid above) against the concurrent
-    // per-instance graph, two steps each on the zero state
+    // per-instance graph, timed on the zero state
     {
         const char* force = std::getenv("ADSG_BATCH_ENGINE");
         if (force && (*force == '0' || *force == '1')) {
@@ -484,19 +484,21 @@ int adsg_batch_create(int count, const int* ndim, const int* p, const int* eleme
         } else if (ensure_contexts(b) == 0) {
             cudaEventCreate(&t0);
             cudaEventCreate(&t1);
+            // the faster of two timings of six steps each, after a warm-up:
+            // the engines can be within a few percent of each other, and the
+            // persistent launch's fixed cost spreads over the steps of a call
             float tp = 1e30f, tc = 1e30f;
-            if (launch_steps(b, 2, b->blocks_per_sm) == 0) {  // warm-up
-                cudaEventRecord(t0, b->stream);
-                if (launch_steps(b, 2, b->blocks_per_sm) == 0) {
+            for (int eng = 0; eng < 2; ++eng) {
+                auto run = [&]() { return eng == 0 ? launch_steps(b, 6, b->blocks_per_sm) : concurrent_steps(b, 6); };
+                if (run() != 0) continue;  // warm-up (the concurrent one builds both graphs)
+                for (int rep = 0; rep < 2; ++rep) {
+                    cudaEventRecord(t0, b->stream);
+                    if (run() != 0) break;
                     cudaEventRecord(t1, b->stream);
-                    if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&tp, t0, t1);
-                }
-            }
-            if (concurrent_steps(b, 2) == 0) {  // warm-up, builds both graphs
-                cudaEventRecord(t0, b->stream);
-                if (concurrent_steps(b, 2) == 0) {
-                    cudaEventRecord(t1, b->stream);
-                    if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&tc, t0, t1);
+                    float ms = 1e30f;
+                    if (cudaEventSynchronize(t1) == cudaSuccess) cudaEventElapsedTime(&ms, t0, t1);
+                    float& t = eng == 0 ? tp : tc;
+                    t = std::min(t, ms);
                 }
             }
             cudaEventDestroy(t0);

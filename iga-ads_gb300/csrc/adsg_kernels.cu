@@ -2153,7 +2153,32 @@ cudaError_t launch_dot(const double* x, const double* y, long long n, double* pa
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int kBatchPassUnits = 2048, kBatchTwistedLines = 128, kBatchLapackLines = 256;
+// Work per item: outputs of a band pass, lines of a two-ended sweep (8 warps
+// x 16), lines of a LAPACK-order sweep (one per thread).  Larger pass items
+// spread the per-item cost (the counter, the wait, the completion count) over
+// more work: 1.54 / 1.37 / 1.33 / 1.47 ms per step of the 64-instance set at
+// 2048 / 8192 / 16384 / 32768 outputs (stage-major order); two rounds of
+// sweeps per warp and item took 1.53 ms against 1.33.
+constexpr int kBatchPassUnits = 16384, kBatchTwistedLines = 128, kBatchLapackLines = 256;
+
+// One item of a band pass: kBatchPassUnits consecutive outputs, 256 at a
+// time.  The buffers of a pass never overlap (each stage reads the tensors the
+// one before wrote and writes others), which the restrict qualifiers tell the
+// compiler: the loads of later outputs can then be issued before the stores
+// of earlier ones, several outputs' loads in flight per thread -- what keeps
+// the FP64 pipe fed at the kernel's 16 resident warps per SM.
+template <int P, bool IN1, bool OUT1, bool SYM>
+__device__ __forceinline__ void batch_pass_run(long long first, long long size, const double* __restrict__ in0,
+                                               const double* __restrict__ in1, double* __restrict__ out0,
+                                               double* __restrict__ out1, const double* __restrict__ A0,
+                                               const double* __restrict__ A1, const double* __restrict__ B0,
+                                               int n_axis, long long stride, int lo, int hi) {
+#pragma unroll 4
+    for (int k = 0; k < kBatchPassUnits / 256; ++k) {
+        const long long g = first + k * 256 + threadIdx.x;
+        if (g < size) band_out<P, IN1, OUT1, SYM, 2>(g, in0, in1, out0, out1, A0, A1, B0, n_axis, stride, lo, hi, size);
+    }
+}
 
 template <int P>
 __device__ __forceinline__ void batch_pass(const batch_inst& I, int stage, long long first, int par) {
@@ -2161,45 +2186,31 @@ __device__ __forceinline__ void batch_pass(const batch_inst& I, int stage, long 
     double* nxt = I.buf[par ^ 1];
     const int n = I.n;
     const dim_dev& D = I.dim;
-    const long long nn = static_cast<long long>(n) * n;
+    const long long nn = static_cast<long long>(n) * n, size = I.size;
     const int lo = max(D.sym_lo, P), hi = min(D.sym_hi, n - P);
     const bool sym = hi > lo;
-#pragma unroll 2
-    for (int k = 0; k < kBatchPassUnits / 256; ++k) {
-        const long long g = first + k * 256 + threadIdx.x;
-        if (g >= I.size) return;
-        if (I.ndim == 3) {
-            if (stage == 0) {
-                if (sym)
-                    band_out<P, false, true, true, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn,
-                                                      lo, hi, I.size);
-                else
-                    band_out<P, false, true, false, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, nn,
-                                                       0, 0, I.size);
-            } else if (stage == 1) {
-                if (sym)
-                    band_out<P, true, true, true, 2>(g, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n, lo,
-                                                     hi, I.size);
-                else
-                    band_out<P, true, true, false, 2>(g, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n, 0,
-                                                      0, I.size);
-            } else {
-                band_out<P, true, false, false, 2>(g, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, 0, 0,
-                                                   I.size);
-            }
-        } else {
-            if (stage == 0) {
-                if (sym)
-                    band_out<P, false, true, true, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n,
-                                                      lo, hi, I.size);
-                else
-                    band_out<P, false, true, false, 2>(g, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n, n,
-                                                       0, 0, I.size);
-            } else {
-                band_out<P, true, false, false, 2>(g, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1, 0, 0,
-                                                   I.size);
-            }
-        }
+    // the outer axis (z in 3D, y in 2D), then y in 3D, then x
+    const long long outer = I.ndim == 3 ? nn : n;
+    if (stage == 0) {
+        if (sym)
+            batch_pass_run<P, false, true, true>(first, size, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n,
+                                                 outer, lo, hi);
+        else
+            batch_pass_run<P, false, true, false>(first, size, cur, nullptr, I.T[0], I.T[1], D.mrow, nullptr, D.nrow, n,
+                                                  outer, 0, 0);
+    } else if (stage == 1) {  // 3D only
+        if (sym)
+            batch_pass_run<P, true, true, true>(first, size, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n, n,
+                                                lo, hi);
+        else
+            batch_pass_run<P, true, true, false>(first, size, I.T[0], I.T[1], I.T[2], I.T[3], D.kdt, D.mrow, D.mrow, n,
+                                                 n, 0, 0);
+    } else if (I.ndim == 3) {
+        batch_pass_run<P, true, false, false>(first, size, I.T[3], I.T[2], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1,
+                                              0, 0);
+    } else {
+        batch_pass_run<P, true, false, false>(first, size, I.T[0], I.T[1], nxt, nullptr, D.kdt, D.mrow, nullptr, n, 1,
+                                              0, 0);
     }
 }
 
