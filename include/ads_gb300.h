@@ -460,7 +460,7 @@ int adsg_test_fail_device_alloc(int k);
  * host memory.
  *  - The first call on a device looks up the array's device address
  *    (cudaGetSymbolAddress) with that device current and creates one event
- *    for that device; make that first call before any stream capture.
+ *    for that device.
  *  - All calls share the array: calls whose work overlaps on the GPU race and
  *    must be serialised by the caller.  Nothing carries over between calls.
  *    Calls on one stream need no synchronisation between them: a call waits
