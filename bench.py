@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-other-configs", action="store_true",
                     help="skip the summaries of the other configurations in the default workload's line")
+    ap.add_argument("--adjoint-steps", type=int, default=200,
+                    help="steps of the adjoint workload (its configuration has 200; fewer for a profiling run)")
     return ap.parse_args()
 
 
@@ -615,7 +617,7 @@ def run_batch(args, cfg):
 
 
 def run_adjoint(args, cfg):
-    """Reverse mode: forward 200 steps of the kappa-weighted step with sqrt(N)
+    """Reverse mode: forward 200 steps (--adjoint-steps) of the kappa-weighted step with sqrt(N)
     checkpoints, mass-norm loss against a second seeded field, gradients with
     respect to u0 and kappa; checked by central differences along 16 seeded
     directions (8 in u0, 8 in kappa) and the dot-product identity."""
@@ -627,7 +629,7 @@ def run_adjoint(args, cfg):
 
     torch.cuda.set_device(0)
     nd, p, E, dt = cfg["ndim"], cfg["p"], cfg["elements"], cfg["dt"]
-    nsteps = 200
+    nsteps = max(1, args.adjoint_steps)
     dims = [ads.Dimension(p, E) for _ in range(nd)]
     ctx = ads.Context(dims)
     adj = ads.Adjoint(ctx, nsteps, dt)
