@@ -121,6 +121,9 @@ def library() -> ctypes.CDLL:
         "adsg_last_error": (ctypes.c_char_p, []),
         "adsg_heat_rhs": (i, [vp, vp, vp, d]),
         "adsg_heat_rhs_elem": (i, [vp, vp, vp, vp, d]),
+        "adsg_kappa_points_count": (ll, [vp]),
+        "adsg_kappa_points": (i, [vp, vp, vp]),
+        "adsg_heat_rhs_elem_points": (i, [vp, vp, vp, vp, d]),
         "adsg_ads_solve": (i, [vp, vp, vp]),
         "adsg_ads_solve_t": (i, [vp, vp]),
         "adsg_heat_step": (i, [vp, vp, vp, d]),
@@ -406,6 +409,16 @@ class Context:
 
     def heat_rhs_elem(self, u_prev, rhs, dt: float, kappa=None) -> None:
         _check(library().adsg_heat_rhs_elem(self._h, _devptr(u_prev), _devptr(kappa), _devptr(rhs), float(dt)))
+
+    def kappa_points_count(self) -> int:
+        return int(library().adsg_kappa_points_count(self._h))
+
+    def kappa_points(self, kappa, kq) -> None:
+        """kappa at every element's Gauss points (3D), for heat_rhs_elem_points."""
+        _check(library().adsg_kappa_points(self._h, _devptr(kappa), _devptr(kq)))
+
+    def heat_rhs_elem_points(self, u_prev, rhs, dt: float, kq) -> None:
+        _check(library().adsg_heat_rhs_elem_points(self._h, _devptr(u_prev), _devptr(kq), _devptr(rhs), float(dt)))
 
     def ads_solve(self, rhs, buf=None) -> None:
         _check(library().adsg_ads_solve(self._h, _devptr(rhs), _devptr(buf)))

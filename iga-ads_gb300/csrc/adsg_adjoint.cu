@@ -33,6 +33,7 @@ struct adsg_adjoint {
     double* seg = nullptr;    // every states
     double* work[2] = {nullptr, nullptr};
     double* kappa = nullptr;  // copy of the field used by the forward pass
+    double* kq = nullptr;     // 3D: that field at every element's Gauss points, computed once per forward pass
     double* partial = nullptr;
     double* scalar = nullptr;
     dev_arena arena;
@@ -56,7 +57,11 @@ int elem_step(adsg_adjoint* a, const double* u, double* out) {
     ADSG_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * c->size, c->stream), "memset");
     {
         stage_scope sc(c, ADSG_STAGE_RHS_ELEM);
-        ADSG_CUDA_TRY(launch_rhs_elem(c->ndim, c->dims, u, a->kappa, out, a->dt, c->stream), "element rhs");
+        // the kappa values at the Gauss points are the ones the element kernel
+        // would interpolate from the coefficients, bit for bit: read them
+        ADSG_CUDA_TRY(a->kq ? launch_rhs_elem_points(c->dims, u, a->kq, out, a->dt, c->stream)
+                            : launch_rhs_elem(c->ndim, c->dims, u, a->kappa, out, a->dt, c->stream),
+                      "element rhs");
     }
     return ctx_solve(c, out, 0);
 }
@@ -88,6 +93,8 @@ int adsg_adjoint_create(adsg_ctx* ctx, int nsteps, double dt, int checkpoint_eve
     if (e == cudaSuccess) e = a->arena.alloc(&a->work[0], n);
     if (e == cudaSuccess) e = a->arena.alloc(&a->work[1], n);
     if (e == cudaSuccess) e = a->arena.alloc(&a->kappa, n);
+    if (e == cudaSuccess && ctx->ndim == 3)
+        e = a->arena.alloc(&a->kq, static_cast<size_t>(kappa_points_count(3, ctx->dims)));
     if (e == cudaSuccess) e = a->arena.alloc(&a->partial, 1024);
     if (e == cudaSuccess) e = a->arena.alloc(&a->scalar, 1);
     if (e != cudaSuccess) {
@@ -127,6 +134,7 @@ int adsg_adjoint_forward(adsg_adjoint* a, const double* u0_dev, const double* ka
     const size_t bytes = sizeof(double) * c->size;
     cudaStream_t s = c->stream;
     ADSG_CUDA_TRY(cudaMemcpyAsync(a->kappa, kappa_dev, bytes, cudaMemcpyDeviceToDevice, s), "copy kappa");
+    if (a->kq) ADSG_CUDA_TRY(launch_kappa_points(c->dims, a->kappa, a->kq, s), "kappa at the Gauss points");
     ADSG_CUDA_TRY(cudaMemcpyAsync(a->ck, u0_dev, bytes, cudaMemcpyDeviceToDevice, s), "checkpoint 0");
     const double* cur = a->ck;
     for (int k = 0; k < a->nsteps; ++k) {

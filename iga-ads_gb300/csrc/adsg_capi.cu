@@ -1007,6 +1007,32 @@ int adsg_heat_rhs_elem(adsg_ctx* ctx, const double* u_prev_dev, const double* ka
     return 0;
 }
 
+long long adsg_kappa_points_count(const adsg_ctx* ctx) { return ctx ? kappa_points_count(ctx->ndim, ctx->dims) : 0; }
+
+int adsg_kappa_points(adsg_ctx* ctx, const double* kappa_dev, double* kq_dev) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!kappa_dev) return fail(-2, "kappa is NULL");
+    if (!kq_dev) return fail(-3, "kq is NULL");
+    if (ctx->ndim != 3) return fail(ADSG_ERR_UNSUPPORTED, "Gauss-point kappa values are for 3D contexts");
+    ADSG_CUDA_TRY(launch_kappa_points(ctx->dims, kappa_dev, kq_dev, ctx->stream), "kappa at the Gauss points");
+    return 0;
+}
+
+int adsg_heat_rhs_elem_points(adsg_ctx* ctx, const double* u_prev_dev, const double* kq_dev, double* rhs_dev,
+                              double dt) {
+    if (!ctx) return fail(-1, "ctx is NULL");
+    if (!u_prev_dev) return fail(-2, "u_prev is NULL");
+    if (!kq_dev) return fail(-3, "kq is NULL");
+    if (!rhs_dev) return fail(-4, "rhs is NULL");
+    if (u_prev_dev == rhs_dev || kq_dev == rhs_dev) return fail(-4, "rhs must not alias an input");
+    if (!std::isfinite(dt)) return fail(-5, "dt must be finite");
+    if (ctx->ndim != 3) return fail(ADSG_ERR_UNSUPPORTED, "Gauss-point kappa values are for 3D contexts");
+    ADSG_CUDA_TRY(cudaMemsetAsync(rhs_dev, 0, sizeof(double) * ctx->size, ctx->stream), "memset rhs");
+    stage_scope sc(ctx, ADSG_STAGE_RHS_ELEM);
+    ADSG_CUDA_TRY(launch_rhs_elem_points(ctx->dims, u_prev_dev, kq_dev, rhs_dev, dt, ctx->stream), "element rhs");
+    return 0;
+}
+
 int adsg_ads_solve(adsg_ctx* ctx, double* rhs_dev, double* buf_dev) {
     (void)buf_dev;
     if (!ctx) return fail(-1, "ctx is NULL");

@@ -28,6 +28,7 @@ ADSG_BOUNDS_TU(elem)
 
 namespace {
 
+constexpr int kNoKappa = 0, kKappaCoef = 1, kKappaPoints = 2;
 
 // One element's buffers (the kappa buffers have one entry without KAPPA).
 // SHARED lays them out so that buffers whose lives do not overlap share
@@ -51,6 +52,7 @@ struct elem3_smem<N, Q, KAPPA, false> {
     double f[Q * Q * Q], gx[Q * Q * Q], gy[Q * Q * Q], gz[Q * Q * Q];
     double K0[NK * N * N * Q + 1 - NK], K1[NK * N * Q * Q + 1 - NK];
     double J;
+    long long id;  // index in the colour launch
     int e[3], f0[3];
     int valid;
 };
@@ -72,6 +74,7 @@ struct elem3_smem<N, Q, KAPPA, true> {
         };
     };
     double J;
+    long long id;  // index in the colour launch
     int e[3], f0[3];
     int valid;
 };
@@ -119,13 +122,17 @@ __device__ __forceinline__ void each_item(S* el, int lane, F&& f) {
 
 // FORM: the general pointwise form of point_form (kappa and dt unused; one
 // element per warp, whose D terms are summed across the warp).
-template <int P, int Q, bool FORM, bool KAPPA, bool SHARED, int EPW, int kWarpsPerBlock>
+// KAPPA: kNoKappa; kKappaCoef, kappa holds the field's spline coefficients,
+// interpolated to the Gauss points alongside u; kKappaPoints, kappa holds the
+// field's values at every element's Gauss points (kappa_points_kernel, the
+// same operations), read in the pointwise stage.
+template <int P, int Q, bool FORM, int KAPPA, bool SHARED, int EPW, int kWarpsPerBlock>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     elem3_kernel(const double* __restrict__ u, const double* __restrict__ kappa, double* __restrict__ rhs,
                  dim_dev X, dim_dev Y, dim_dev Z, int cx, int cy, int cz, int mx, int my, int mz, double dt,
                  point_form F) {
     constexpr int N = P + 1;
-    using S_t = elem3_smem<N, Q, KAPPA, SHARED>;
+    using S_t = elem3_smem<N, Q, KAPPA == kKappaCoef, SHARED>;
     __shared__ elem_group<S_t, EPW> sm_all[kWarpsPerBlock];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -136,6 +143,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     if (lane < EPW) {
         S_t& S = el[lane];
         const long long id = wid * EPW + lane;
+        S.id = id;
         S.valid = id < count;
         if (S.valid) {
             const int iz = static_cast<int>(id % mz);
@@ -161,7 +169,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         const int ax = t % N, ay = (t / N) % N, az = t / (N * N);
         const long long g = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
         S.c[t] = u ? u[g] : 0.0;
-        if constexpr (KAPPA) S.kc[t] = kappa[g];
+        if constexpr (KAPPA == kKappaCoef) S.kc[t] = kappa[g];
     });
     each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
@@ -185,11 +193,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             const double cv = S.c[byz * N + b];
             a0 = fma(S.B[0][qx * N + b], cv, a0);
             a1 = fma(S.dB[0][qx * N + b], cv, a1);
-            if constexpr (KAPPA) k0 = fma(S.B[0][qx * N + b], S.kc[byz * N + b], k0);
+            if constexpr (KAPPA == kKappaCoef) k0 = fma(S.B[0][qx * N + b], S.kc[byz * N + b], k0);
         }
         S.T0[t] = a0;
         S.T1[t] = a1;
-        if constexpr (KAPPA) S.K0[t] = k0;
+        if constexpr (KAPPA == kKappaCoef) S.K0[t] = k0;
     });
     __syncwarp();
     // y: V..[bz][qy][qx]
@@ -203,12 +211,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             v00 = fma(by, S.T0[src], v00);
             v01 = fma(dby, S.T0[src], v01);
             v10 = fma(by, S.T1[src], v10);
-            if constexpr (KAPPA) k1 = fma(by, S.K0[src], k1);
+            if constexpr (KAPPA == kKappaCoef) k1 = fma(by, S.K0[src], k1);
         }
         S.V00[t] = v00;
         S.V01[t] = v01;
         S.V10[t] = v10;
-        if constexpr (KAPPA) S.K1[t] = k1;
+        if constexpr (KAPPA == kKappaCoef) S.K1[t] = k1;
     });
     __syncwarp();
     // z + pointwise form: f = W u, g* = -dt kappa W d*u
@@ -225,8 +233,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             uz = fma(dbz, S.V00[src], uz);
             uy = fma(bz, S.V01[src], uy);
             ux = fma(bz, S.V10[src], ux);
-            if constexpr (KAPPA) kv = fma(bz, S.K1[src], kv);
+            if constexpr (KAPPA == kKappaCoef) kv = fma(bz, S.K1[src], kv);
         }
+        if constexpr (KAPPA == kKappaPoints)  // this colour's block: the warp's elements are consecutive
+            kv = kappa[S.id * (Q * Q * Q) + t];
         const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
         if (FORM) {
             const long long Qx = static_cast<long long>(X.elements) * Q, Qy = static_cast<long long>(Y.elements) * Q;
@@ -244,7 +254,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S.gz[t] = uz * g;
             dsum = fma(de, W, dsum);
         } else {
-            const double g = (KAPPA ? -dt * kv : -dt) * W;
+            const double g = (KAPPA != kNoKappa ? -dt * kv : -dt) * W;
             S.f[t] = uv * W;
             S.gx[t] = ux * g;
             S.gy[t] = uy * g;
@@ -787,11 +797,25 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     });
 }
 
-int colour_count(int E, int c, int N) { return E > c ? (E - c + N - 1) / N : 0; }
+__host__ __device__ inline int colour_count(int E, int c, int N) { return E > c ? (E - c + N - 1) / N : 0; }
 
+// Elements before colour (cx, cy, cz) in the launch order of the colours (cx
+// outermost, cz innermost): where that colour's block of Gauss-point kappa
+// values starts, in elements.
+__host__ __device__ inline long long colour_base(int Ex, int Ey, int Ez, int N, int cx, int cy, int cz) {
+    long long sx = 0, sy = 0, sz = 0;
+    for (int c = 0; c < cx; ++c) sx += colour_count(Ex, c, N);
+    for (int c = 0; c < cy; ++c) sy += colour_count(Ey, c, N);
+    for (int c = 0; c < cz; ++c) sz += colour_count(Ez, c, N);
+    const long long mx = colour_count(Ex, cx, N), my = colour_count(Ey, cy, N);
+    return sx * Ey * Ez + mx * (sy * Ez + my * sz);
+}
+
+// kappa_points: kappa holds the field at the Gauss points (3D only).
 template <int P, bool FORM>
 cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* kappa, double* rhs, double dt,
-                   const point_form& F, cudaStream_t s) {
+                   const point_form& F, cudaStream_t s, bool kappa_points = false) {
+    if (kappa_points && (ndim != 3 || FORM || !kappa)) return cudaErrorNotSupported;
     constexpr int N = P + 1, Q = P + 1;
     constexpr int E3 = FORM ? 1 : elems_per_warp<N * N * N>();
     constexpr int E2 = FORM ? 1 : elems_per_warp<N * N>();
@@ -814,13 +838,20 @@ cudaError_t elem_p(int ndim, const dim_dev* d, const double* u, const double* ka
                               mz = colour_count(d[2].elements, cz, N);
                     const long long work = static_cast<long long>(mx) * my * mz;
                     if (!work) continue;
-                    if (!FORM && kappa) {
+                    if (kappa_points) {
+                        // the tile without kappa buffers, as without kappa
+                        const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
+                        const double* kc = kappa + colour_base(d[0].elements, d[1].elements, d[2].elements, N, cx, cy,
+                                                               cz) * (Q * Q * Q);
+                        elem3_kernel<P, Q, FORM, kKappaPoints, kShared, E3, W3><<<blocks, 32 * W3, 0, s>>>(
+                            u, kc, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
+                    } else if (!FORM && kappa) {
                         const long long blocks = ((work + E3k - 1) / E3k + W3k - 1) / W3k;
-                        elem3_kernel<P, Q, FORM, true, kSharedKappa, E3k, W3k><<<blocks, 32 * W3k, 0, s>>>(
+                        elem3_kernel<P, Q, FORM, kKappaCoef, kSharedKappa, E3k, W3k><<<blocks, 32 * W3k, 0, s>>>(
                             u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
                     } else {
                         const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
-                        elem3_kernel<P, Q, FORM, false, kShared, E3, W3><<<blocks, 32 * W3, 0, s>>>(
+                        elem3_kernel<P, Q, FORM, kNoKappa, kShared, E3, W3><<<blocks, 32 * W3, 0, s>>>(
                             u, kappa, rhs, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt, F);
                     }
                 }
@@ -903,6 +934,92 @@ cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, co
         case 2: return kgrad2_p<2>(dims, u, mu, g, dt, s);
         case 3: return kgrad2_p<3>(dims, u, mu, g, dt, s);
         case 4: return kgrad2_p<4>(dims, u, mu, g, dt, s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+// kappa at every Gauss point of every element, one thread per point, stored
+// by element colour in the element kernel's launch order (colour blocks,
+// elements in their launch index within a block, then the point
+// qx + Q (qy + Q qz)): a warp of the element kernel reads its elements'
+// values as one contiguous run.
+// The contractions are elem3_kernel's (x, then y, then z, each an FMA chain
+// from zero over the element's coefficients in the same order), so the values
+// equal the ones that kernel interpolates alongside u, bit for bit.
+template <int P>
+__global__ void __launch_bounds__(256) kappa_points_kernel(const double* __restrict__ kappa, double* __restrict__ kq,
+                                                           dim_dev X, dim_dev Y, dim_dev Z) {
+    constexpr int N = P + 1, Q = P + 1, Q3 = Q * Q * Q;
+    const long long ne = static_cast<long long>(X.elements) * Y.elements * Z.elements;
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= ne * Q3) return;
+    const long long el = i / Q3;
+    const int t = static_cast<int>(i - el * Q3);
+    const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
+    const int e0 = static_cast<int>(el % X.elements), e1 = static_cast<int>((el / X.elements) % Y.elements),
+              e2 = static_cast<int>(el / (static_cast<long long>(X.elements) * Y.elements));
+    const long long nx = X.n, nxy = static_cast<long long>(X.n) * Y.n;
+    const int f0 = X.first[e0], f1 = Y.first[e1], f2 = Z.first[e2];
+    if (!(ADSG_IN(f0 + N - 1, X.n) && ADSG_IN(f1 + N - 1, Y.n) && ADSG_IN(f2 + N - 1, Z.n) && f0 >= 0 && f1 >= 0 &&
+          f2 >= 0))
+        return;
+    const double* bx = X.btab + ((static_cast<long long>(e0) * Q + qx) * 2) * N;  // value row of qx
+    const double* by = Y.btab + ((static_cast<long long>(e1) * Q + qy) * 2) * N;
+    const double* bz = Z.btab + ((static_cast<long long>(e2) * Q + qz) * 2) * N;
+    double kv = 0.0;
+#pragma unroll
+    for (int cz = 0; cz < N; ++cz) {
+        double k1 = 0.0;
+#pragma unroll
+        for (int cy = 0; cy < N; ++cy) {
+            const double* row = kappa + (f0 + nx * (f1 + cy) + nxy * (f2 + cz));
+            double k0 = 0.0;
+#pragma unroll
+            for (int cx = 0; cx < N; ++cx) k0 = fma(bx[cx], row[cx], k0);
+            k1 = fma(by[cy], k0, k1);
+        }
+        kv = fma(bz[cz], k1, kv);
+    }
+    const int cx = e0 % N, cy = e1 % N, cz = e2 % N;
+    const long long my = colour_count(Y.elements, cy, N), mz = colour_count(Z.elements, cz, N);
+    const long long id = (static_cast<long long>(e0 / N) * my + e1 / N) * mz + e2 / N;
+    kq[(colour_base(X.elements, Y.elements, Z.elements, N, cx, cy, cz) + id) * Q3 + t] = kv;
+}
+
+cudaError_t launch_kappa_points(const dim_dev* dims, const double* kappa, double* kq, cudaStream_t s) {
+    const int p = dims[0].p;
+    for (int d = 0; d < 3; ++d)
+        if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    const long long total = kappa_points_count(3, dims);
+    if (total <= 0) return cudaSuccess;
+    const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
+    switch (p) {
+        case 1: kappa_points_kernel<1><<<blocks, 256, 0, s>>>(kappa, kq, dims[0], dims[1], dims[2]); break;
+        case 2: kappa_points_kernel<2><<<blocks, 256, 0, s>>>(kappa, kq, dims[0], dims[1], dims[2]); break;
+        case 3: kappa_points_kernel<3><<<blocks, 256, 0, s>>>(kappa, kq, dims[0], dims[1], dims[2]); break;
+        case 4: kappa_points_kernel<4><<<blocks, 256, 0, s>>>(kappa, kq, dims[0], dims[1], dims[2]); break;
+        default: return cudaErrorNotSupported;
+    }
+    return cudaGetLastError();
+}
+
+long long kappa_points_count(int ndim, const dim_dev* dims) {
+    if (ndim != 3) return 0;
+    const long long q = dims[0].q;
+    return static_cast<long long>(dims[0].elements) * dims[1].elements * dims[2].elements * q * q * q;
+}
+
+cudaError_t launch_rhs_elem_points(const dim_dev* dims, const double* u_prev, const double* kq, double* rhs,
+                                   double dt, cudaStream_t s) {
+    const int p = dims[0].p;
+    for (int d = 0; d < 3; ++d)
+        if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
+    const point_form none;
+    switch (p) {
+        case 1: return elem_p<1, false>(3, dims, u_prev, kq, rhs, dt, none, s, true);
+        case 2: return elem_p<2, false>(3, dims, u_prev, kq, rhs, dt, none, s, true);
+        case 3: return elem_p<3, false>(3, dims, u_prev, kq, rhs, dt, none, s, true);
+        case 4: return elem_p<4, false>(3, dims, u_prev, kq, rhs, dt, none, s, true);
         default: return cudaErrorNotSupported;
     }
 }

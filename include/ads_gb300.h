@@ -112,6 +112,19 @@ int adsg_heat_rhs(adsg_ctx* ctx, const double* u_prev_dev, double* rhs_dev, doub
 int adsg_heat_rhs_elem(adsg_ctx* ctx, const double* u_prev_dev, const double* kappa_dev,
                        double* rhs_dev, double dt);
 
+/* For many right-hand sides with one kappa field (a time loop, the adjoint),
+ * 3D contexts: adsg_kappa_points evaluates the field at every element's Gauss
+ * points once, into kq_dev (adsg_kappa_points_count doubles, element-major:
+ * kq[(ex + Ex (ey + Ey ez)) Q^3 + qx + Q (qy + Q qz)]), and
+ * adsg_heat_rhs_elem_points takes those values instead of interpolating the
+ * coefficients on every call.  The values are the ones adsg_heat_rhs_elem
+ * interpolates, bit for bit, so both give the same rhs.  count: 0 for a 2D
+ * context (ADSG_ERR_UNSUPPORTED from the other two). */
+long long adsg_kappa_points_count(const adsg_ctx* ctx);
+int adsg_kappa_points(adsg_ctx* ctx, const double* kappa_dev, double* kq_dev);
+int adsg_heat_rhs_elem_points(adsg_ctx* ctx, const double* u_prev_dev, const double* kq_dev, double* rhs_dev,
+                              double dt);
+
 /* ads_solve(rhs, buf, dims...) (reference include/ads/solver.hpp:222-226,
  * standard ADS, 1D case :199-203): solves (M_x (x) M_y (x) M_z) x = rhs with the
  * factorised bands, one pivoted band substitution (dgbtrs) per grid line and

@@ -78,6 +78,41 @@ def test_element_quadrature_with_kappa_against_oracle(cuda):
     assert oracle.rel_l2(r.cpu().numpy(), ref) <= 1e-13
 
 
+@pytest.mark.parametrize("p,elements", [((2, 2, 2), (7, 5, 6)), ((1, 1, 1), (9, 4, 5)), ((3, 3, 3), (4, 6, 5)),
+                                        ((4, 4, 4), (5, 4, 6))])
+def test_kappa_at_gauss_points_gives_the_same_rhs(p, elements, cuda):
+    """adsg_kappa_points + adsg_heat_rhs_elem_points (kappa evaluated once at
+    every element's Gauss points) against adsg_heat_rhs_elem with the
+    coefficients: the same bits, and the oracle's kappa RHS."""
+    import torch
+
+    dims = [ads.Dimension(pp, e) for pp, e in zip(p, elements)]
+    ctx = ads.Context(dims)
+    q = p[0] + 1
+    assert ctx.kappa_points_count() == int(np.prod(elements)) * q ** 3
+    rng = np.random.default_rng(sum(elements))
+    u = rng.uniform(-1, 1, ctx.size)
+    kappa = 1.0 + 0.5 * rng.uniform(-1, 1, ctx.size)
+    ud, kd = torch.from_numpy(u).to(cuda), torch.from_numpy(kappa).to(cuda)
+    r1, r2 = torch.empty_like(ud), torch.empty_like(ud)
+    kq = torch.empty(ctx.kappa_points_count(), dtype=torch.float64, device=cuda)
+    ctx.heat_rhs_elem(ud, r1, 1e-3, kappa=kd)
+    ctx.kappa_points(kd, kq)
+    ctx.heat_rhs_elem_points(ud, r2, 1e-3, kq)
+    ctx.synchronize()
+    assert torch.equal(r1, r2)
+    ref = oracle.Problem(list(p), list(elements)).heat_rhs_kappa(u, kappa, 1e-3)
+    check(f"kappa points p={p} E={elements}", oracle.rel_l2(r2.cpu().numpy(), ref), 1e-13)
+
+
+def test_kappa_points_need_a_3d_context(cuda):
+    ctx = ads.Context([ads.Dimension(2, 8), ads.Dimension(2, 9)])
+    assert ctx.kappa_points_count() == 0
+    with pytest.raises(ads.AdsError) as err:  # refused before any device access
+        ctx.kappa_points(16, 32)
+    assert err.value.code == 1005
+
+
 def _raw_dim(n, lu, ipiv, kl=1, ku=1):
     """A descriptor for a bare factorised band (basis tables of a p = 1 space
     with n-1 elements; only the solve uses the band)."""
