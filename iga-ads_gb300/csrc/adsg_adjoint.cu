@@ -181,8 +181,8 @@ int adsg_adjoint_backward(adsg_adjoint* a, const double* dL_duT_dev, double* gra
             {
                 // grad kappa += mu^T (dR/dkappa) u_k and other = R^T mu (R is symmetric)
                 stage_scope sc(c, ADSG_STAGE_RHS_ELEM);
-                ADSG_CUDA_TRY(launch_adjoint_pair(c->ndim, c->dims, state(k), lam, a->kappa, other, grad_kappa_dev,
-                                                  a->dt, s),
+                ADSG_CUDA_TRY(launch_adjoint_pair(c->ndim, c->dims, state(k), lam, a->kq ? a->kq : a->kappa, other,
+                                                  grad_kappa_dev, a->dt, s, a->kq != nullptr),
                               "kappa gradient and R^T mu");
             }
             std::swap(lam, other);  // lam <- lambda_k = R mu_{k+1}

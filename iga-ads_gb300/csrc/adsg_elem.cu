@@ -495,11 +495,14 @@ struct adj3_smem {
         };
     };
     double J;
+    long long id;  // index in the colour launch
     int e[3], f0[3];
     int valid;
 };
 
-template <int P, int Q, int EPW = elems_per_warp<(P + 1) * (P + 1) * (P + 1)>(),
+// KP: kappa holds the field's values at the Gauss points (this colour's block
+// of kappa_points_kernel's output) instead of its coefficients.
+template <int P, int Q, bool KP = false, int EPW = elems_per_warp<(P + 1) * (P + 1) * (P + 1)>(),
           int kWarpsPerBlock = warps_for<elem_group<adj3_smem<P + 1, Q>, EPW>>()>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     adj3_kernel(const double* __restrict__ u, const double* __restrict__ mu, const double* __restrict__ kappa,
@@ -517,6 +520,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     if (lane < EPW) {
         S_t& S = el[lane];
         const long long id = wid * EPW + lane;
+        S.id = id;
         S.valid = id < count;
         if (S.valid) {
             const int iz = static_cast<int>(id % mz);
@@ -541,7 +545,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         const long long gi = (S.f0[0] + ax) + nx * (S.f0[1] + ay) + nxy * (S.f0[2] + az);
         S.cm[t] = mu[gi];
         S.cu[t] = u[gi];
-        S.kc[t] = kappa[gi];
+        if constexpr (!KP) S.kc[t] = kappa[gi];
     });
     each_item<Q * N, EPW>(el, lane, [&](S_t& S, int t) {
         const int q = t / N, a = t % N;
@@ -566,13 +570,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             const double cv = S.cm[byz * N + b], uv = S.cu[byz * N + b];
             a0 = fma(bv, cv, a0);
             a1 = fma(dv, cv, a1);
-            k0 = fma(bv, S.kc[byz * N + b], k0);
+            if constexpr (!KP) k0 = fma(bv, S.kc[byz * N + b], k0);
             b0 = fma(bv, uv, b0);
             b1 = fma(dv, uv, b1);
         }
         S.Tm0[t] = a0;
         S.Tm1[t] = a1;
-        S.K0[t] = k0;
+        if constexpr (!KP) S.K0[t] = k0;
         S.Tu0[t] = b0;
         S.Tu1[t] = b1;
     });
@@ -588,7 +592,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             v00 = fma(by, S.Tm0[src], v00);
             v01 = fma(dby, S.Tm0[src], v01);
             v10 = fma(by, S.Tm1[src], v10);
-            k1 = fma(by, S.K0[src], k1);
+            if constexpr (!KP) k1 = fma(by, S.K0[src], k1);
             u00 = fma(by, S.Tu0[src], u00);
             u01 = fma(dby, S.Tu0[src], u01);
             u10 = fma(by, S.Tu1[src], u10);
@@ -596,7 +600,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
         S.Vm00[t] = v00;
         S.Vm01[t] = v01;
         S.Vm10[t] = v10;
-        S.K1[t] = k1;
+        if constexpr (!KP) S.K1[t] = k1;
         S.Vu00[t] = u00;
         S.Vu01[t] = u01;
         S.Vu10[t] = u10;
@@ -614,11 +618,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             mz_ = fma(dbz, S.Vm00[src], mz_);
             my_ = fma(bz, S.Vm01[src], my_);
             mx_ = fma(bz, S.Vm10[src], mx_);
-            kv = fma(bz, S.K1[src], kv);
+            if constexpr (!KP) kv = fma(bz, S.K1[src], kv);
             uz = fma(dbz, S.Vu00[src], uz);
             uy = fma(bz, S.Vu01[src], uy);
             ux = fma(bz, S.Vu10[src], ux);
         }
+        if constexpr (KP) kv = kappa[S.id * (Q * Q * Q) + t];
         const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
         const double gk = (-dt * kv) * W;
         S.f[t] = mv * W;
@@ -886,7 +891,7 @@ cudaError_t kgrad2_p(const dim_dev* d, const double* u, const double* mu, double
 
 template <int P>
 cudaError_t adj3_p(const dim_dev* d, const double* u, const double* mu, const double* kappa, double* rmu, double* g,
-                   double dt, cudaStream_t s) {
+                   double dt, cudaStream_t s, bool kappa_points) {
     constexpr int N = P + 1, Q = P + 1;
     constexpr int E3 = elems_per_warp<N * N * N>();
     constexpr int W3 = warps_for<elem_group<adj3_smem<N, Q>, E3>>();
@@ -897,8 +902,15 @@ cudaError_t adj3_p(const dim_dev* d, const double* u, const double* mu, const do
                           mz = colour_count(d[2].elements, cz, N);
                 const long long work = static_cast<long long>(mx) * my * mz;
                 if (!work) continue;
-                adj3_kernel<P, Q><<<((work + E3 - 1) / E3 + W3 - 1) / W3, 32 * W3, 0, s>>>(
-                    u, mu, kappa, rmu, g, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt);
+                const long long blocks = ((work + E3 - 1) / E3 + W3 - 1) / W3;
+                if (kappa_points)
+                    adj3_kernel<P, Q, true><<<blocks, 32 * W3, 0, s>>>(
+                        u, mu,
+                        kappa + colour_base(d[0].elements, d[1].elements, d[2].elements, N, cx, cy, cz) * (Q * Q * Q),
+                        rmu, g, d[0], d[1], d[2], cx, cy, cz, mx, my, mz, dt);
+                else
+                    adj3_kernel<P, Q><<<blocks, 32 * W3, 0, s>>>(u, mu, kappa, rmu, g, d[0], d[1], d[2], cx, cy, cz,
+                                                                 mx, my, mz, dt);
             }
     return cudaGetLastError();
 }
@@ -906,8 +918,10 @@ cudaError_t adj3_p(const dim_dev* d, const double* u, const double* mu, const do
 }  // namespace
 
 cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, const double* mu,
-                                const double* kappa, double* rmu, double* g, double dt, cudaStream_t s) {
+                                const double* kappa, double* rmu, double* g, double dt, cudaStream_t s,
+                                bool kappa_points) {
     if (ndim != 3) {
+        if (kappa_points) return cudaErrorNotSupported;
         cudaError_t e = launch_kappa_grad(ndim, dims, u, mu, g, dt, s);
         return e != cudaSuccess ? e : launch_rhs_elem(ndim, dims, mu, kappa, rmu, dt, s);
     }
@@ -915,10 +929,10 @@ cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, 
     for (int d = 0; d < ndim; ++d)
         if (dims[d].p != p || dims[d].q != p + 1) return cudaErrorNotSupported;
     switch (p) {
-        case 1: return adj3_p<1>(dims, u, mu, kappa, rmu, g, dt, s);
-        case 2: return adj3_p<2>(dims, u, mu, kappa, rmu, g, dt, s);
-        case 3: return adj3_p<3>(dims, u, mu, kappa, rmu, g, dt, s);
-        case 4: return adj3_p<4>(dims, u, mu, kappa, rmu, g, dt, s);
+        case 1: return adj3_p<1>(dims, u, mu, kappa, rmu, g, dt, s, kappa_points);
+        case 2: return adj3_p<2>(dims, u, mu, kappa, rmu, g, dt, s, kappa_points);
+        case 3: return adj3_p<3>(dims, u, mu, kappa, rmu, g, dt, s, kappa_points);
+        case 4: return adj3_p<4>(dims, u, mu, kappa, rmu, g, dt, s, kappa_points);
         default: return cudaErrorNotSupported;
     }
 }

@@ -215,7 +215,8 @@ cudaError_t launch_kappa_grad(int ndim, const dim_dev* dims, const double* u, co
 // rmu += R(kappa) mu and g += mu^T (dR/dkappa) u, in one pass in 3D (the
 // R(kappa) mu part bitwise launch_rhs_elem's), in two kernels in 2D
 cudaError_t launch_adjoint_pair(int ndim, const dim_dev* dims, const double* u, const double* mu,
-                                const double* kappa, double* rmu, double* g, double dt, cudaStream_t s);
+                                const double* kappa, double* rmu, double* g, double dt, cudaStream_t s,
+                                bool kappa_points = false);  // kappa_points: kappa at the Gauss points (3D)
 
 // small vector kernels of the adjoint driver
 cudaError_t launch_axpby(double* y, double a, const double* x, double b, long long n, cudaStream_t s);  // y = a*x + b*y
