@@ -225,6 +225,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     each_item<Q * Q * Q, EPW>(el, lane, [&](S_t& S, int t) {
         const int qx = t % Q, qy = (t / Q) % Q, qz = t / (Q * Q);
         double uv = 0.0, ux = 0.0, uy = 0.0, uz = 0.0, kv = 0.0;
+        // this colour's block: the warp's elements are consecutive; issued
+        // before the contraction so that it arrives during it
+        if constexpr (KAPPA == kKappaPoints) kv = kappa[S.id * (Q * Q * Q) + t];
 #pragma unroll
         for (int b = 0; b < N; ++b) {
             const int src = (b * Q + qy) * Q + qx;
@@ -235,8 +238,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             ux = fma(bz, S.V10[src], ux);
             if constexpr (KAPPA == kKappaCoef) kv = fma(bz, S.K1[src], kv);
         }
-        if constexpr (KAPPA == kKappaPoints)  // this colour's block: the warp's elements are consecutive
-            kv = kappa[S.id * (Q * Q * Q) + t];
         const double W = X.wq[qx] * Y.wq[qy] * Z.wq[qz] * S.J;
         if (FORM) {
             const long long Qx = static_cast<long long>(X.elements) * Q, Qy = static_cast<long long>(Y.elements) * Q;
