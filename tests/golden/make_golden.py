@@ -4,6 +4,8 @@ Run in a container where the reference sources are present:
     make -C oracle ref           # builds oracle/_ref/libadsref.so from them
     python tests/golden/make_golden.py          # the small cases
     python tests/golden/make_golden.py --runs   # the full-size runs (hours)
+    python tests/golden/make_golden.py --runs-self run_3d_p4_e256 4
+                                                # their first step on another thread count
 
 Every output array below is produced by the reference implementation
 (oracle/_ref: the reference's src/ads/*.cpp and headers compiled as they lie,
@@ -391,6 +393,32 @@ def heat2d_dirichlet_case(L, p, E, dt, nsteps):
     return dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps), u1=u1, uN=u, row=row)
 
 
+def run_self_case(L, name, p, E, dt, seed, nthreads):
+    """The first step of a full-size run once more, on another thread count
+    of the executor (the scatter order, and so the rounding, differs): the
+    reference's disagreement with itself at that size, recorded like the run
+    (<name>_self.npz)."""
+    import time
+
+    sys.path.insert(0, os.path.join(ROOT, "iga-ads_gb300"))
+    import ads_gb300 as ads
+    from ads_gb300 import inputs
+
+    L.ref_heat_steps_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp,
+                                    ctypes.c_int]
+    u = inputs.initial_field([ads.Dimension(p, E) for _ in range(3)], seed=seed)
+    n = E + p
+    mass = tables(L, p, E)["mass"]
+    out = dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), seed=np.int64(seed), threads=np.int32(nthreads),
+               u0_norm=np.float64(np.linalg.norm(u)))
+    t0 = time.time()
+    assert L.ref_heat_steps_mt(3, p, E, dt, 1, dp(u), nthreads) == 0
+    out.update(snapshot(u, n, mass, p, "u1_", "z"))
+    out["seconds"] = np.float64(time.time() - t0)
+    np.savez_compressed(os.path.join(HERE, name + "_self.npz"), **out)
+    print(f"wrote {name}_self after {time.time() - t0:.0f} s", flush=True)
+
+
 def main_runs(names, nthreads):
     L = load_ref()
     for name, p, E, dt, nsteps, seed in RUNS:
@@ -401,6 +429,11 @@ def main_runs(names, nthreads):
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "--runs":
         return main_runs(sys.argv[2:], os.cpu_count() or 1)
+    if len(sys.argv) > 2 and sys.argv[1] == "--runs-self":
+        # python make_golden.py --runs-self NAME THREADS
+        L = load_ref()
+        name, p, E, dt, nsteps, seed = next(r for r in RUNS if r[0] == sys.argv[2])
+        return run_self_case(L, name, p, E, dt, seed, int(sys.argv[3]) if len(sys.argv) > 3 else 4)
     L = load_ref()
     for name, which, p, E, dt, seed in FORM_CASES:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **form_case(L, which, p, E, dt, seed))

@@ -33,6 +33,8 @@ def main():
     ap.add_argument("name", choices=[r[0] for r in RUNS])
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--out", default=HERE)
+    ap.add_argument("--sequential-first-step", action="store_true",
+                    help="only the first step, by the sequential element loop (<name>_oracle_seq.npz)")
     a = ap.parse_args()
     import oracle
 
@@ -47,6 +49,14 @@ def main():
     out = dict(p=np.int32(p), elements=np.int32(E), dt=np.float64(dt), nsteps=np.int32(nsteps), seed=np.int64(seed),
                threads=np.int32(a.threads), u0_norm=np.float64(np.linalg.norm(u)))
     t0 = time.time()
+    if a.sequential_first_step:
+        u = pr.heat_steps(u, dt, 1)
+        out.update(snapshot(u, n, mass, p, "u1_", "z"))
+        out["threads"] = np.int32(1)
+        path = os.path.join(a.out, name + "_oracle_seq.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} after {time.time() - t0:.0f} s", flush=True)
+        return
     u = pr.heat_steps(u, dt, 1, nthreads=a.threads)
     out.update(snapshot(u, n, mass, p, "u1_", "z"))
     print(f"{name} (oracle): step 1 done in {time.time() - t0:.0f} s", flush=True)

@@ -61,9 +61,11 @@ def _vs_run(u, g, prefix, n, ctx):
     """Largest relative difference of u from the reference run's record:
     whole planes (rel L2) and the global L2 and mass norms."""
     t = u.reshape(n, n, n)
-    errs = [oracle.rel_l2(t[int(g["plane_z_index"])], g[prefix + "plane_z"])]
+    kz = int(g["plane_z_index"]) if "plane_z_index" in g.files else n // 2  # the snapshot's planes
+    ky = int(g["plane_y_index"]) if "plane_y_index" in g.files else n // 3
+    errs = [oracle.rel_l2(t[kz], g[prefix + "plane_z"])]
     if prefix + "plane_y" in g.files:
-        errs.append(oracle.rel_l2(t[:, int(g["plane_y_index"]), :], g[prefix + "plane_y"]))
+        errs.append(oracle.rel_l2(t[:, ky, :], g[prefix + "plane_y"]))
     s = float(np.abs(u).max())
     errs.append(abs(np.linalg.norm(u / s) * s - float(g[prefix + "norm"])) / float(g[prefix + "norm"]))
     if ctx is not None:
@@ -123,8 +125,22 @@ def test_heat_260cubed_p4_run(cuda):
     uN = u0.copy()
     ctx.heat_steps_host(uN, dt, N)
     pr = oracle.Problem([p] * 3, [E] * 3)
+    # CPU forms of the first step: the reference's executor on 8 and on 4
+    # threads (the run's record and run_3d_p4_e256_self.npz), the oracle's
+    # sequential element loop (run_3d_p4_e256_oracle_seq.npz) and its executor
+    # on two thread counts here; the scatter order, and so the rounding,
+    # differs between them, and at p = 4 the Kronecker mass matrix (condition
+    # ~3e5) makes their disagreement comparable to the contract.  The bound
+    # takes twice the largest pairwise disagreement.
     ref1 = pr.heat_steps(u0, dt, 1, nthreads=THREADS)
-    d_cpu1 = _vs_run(ref1, g, "u1_", n, None)  # oracle against the reference after one step
+    ref1b = pr.heat_steps(u0, dt, 1, nthreads=max(2, THREADS // 2))
+    recs = [g, _fixture("run_3d_p4_e256_self"), _fixture("run_3d_p4_e256_oracle_seq")]
+    d_cpu1 = oracle.rel_l2(ref1, ref1b)
+    for k, a in enumerate(recs):
+        d_cpu1 = max(d_cpu1, _vs_run(ref1, a, "u1_", n, None), _vs_run(ref1b, a, "u1_", n, None))
+        for b in recs[k + 1:]:
+            d_cpu1 = max(d_cpu1, _records_apart(a, b, "u1_"))
+    print(f"[parity] 260^3 p=4 first step, CPU forms' largest disagreement {d_cpu1:.3e}")
     check("260^3 p=4 1 step vs oracle (whole field)", oracle.rel_l2(u1, ref1), STEP, d_cpu1)
     check("260^3 p=4 1 step vs reference run", _vs_run(u1, g, "u1_", n, ctx), STEP, d_cpu1)
     # the run's other CPU form: the oracle's executor over the same 20 steps
