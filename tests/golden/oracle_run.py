@@ -6,10 +6,13 @@ How far the two CPU forms of the reference's algorithm drift apart over the
 run bounds the GPU's drift from the reference (tests/test_gpu_fullsize.py).
 
     python tests/golden/oracle_run.py run_3d_p4_e256 [--threads N]
+    python tests/golden/oracle_run.py run_3d_p4_e256 --sequential-first-step
 
-writes tests/golden/<name>_oracle.npz.  Needs the oracle (make -C oracle) and
-the engine's Python package (for the seeded initial field); not the
-reference sources."""
+writes tests/golden/<name>_oracle.npz (the whole run on the executor), or
+<name>_oracle_seq.npz (the first step by the sequential element loop, the
+order a reference build without Galois runs).  Needs the oracle (make -C
+oracle) and the engine's Python package (for the seeded initial field); not
+the reference sources."""
 from __future__ import annotations
 
 import argparse
