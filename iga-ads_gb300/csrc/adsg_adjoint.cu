@@ -93,8 +93,15 @@ int adsg_adjoint_create(adsg_ctx* ctx, int nsteps, double dt, int checkpoint_eve
     if (e == cudaSuccess) e = a->arena.alloc(&a->work[0], n);
     if (e == cudaSuccess) e = a->arena.alloc(&a->work[1], n);
     if (e == cudaSuccess) e = a->arena.alloc(&a->kappa, n);
-    if (e == cudaSuccess && ctx->ndim == 3)
-        e = a->arena.alloc(&a->kq, static_cast<size_t>(kappa_points_count(3, ctx->dims)));
+    if (e == cudaSuccess && ctx->ndim == 3) {
+        // kappa at the Gauss points: (p+1)^3 doubles per element, 1.2 to 15
+        // times a state tensor; without the room the passes interpolate the
+        // coefficients instead (the same bits, ~10% more time)
+        if (a->arena.alloc(&a->kq, static_cast<size_t>(kappa_points_count(3, ctx->dims))) != cudaSuccess) {
+            cudaGetLastError();
+            a->kq = nullptr;
+        }
+    }
     if (e == cudaSuccess) e = a->arena.alloc(&a->partial, 1024);
     if (e == cudaSuccess) e = a->arena.alloc(&a->scalar, 1);
     if (e != cudaSuccess) {

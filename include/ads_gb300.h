@@ -370,7 +370,11 @@ int adsg_ads_solve_general_host(adsg_ctx* ctx, int special_dim, const adsg_line_
  *     mu = M^{-T} lambda (transposed line solves),  dL/dkappa += mu^T dR/dkappa u_k,
  *     lambda <- R(kappa) mu (R is symmetric).
  * Needs a 2D or 3D context with one degree p <= 4 and p+1 Gauss points.
- * kappa is copied at forward time; buffers are device pointers of ctx's size. */
+ * kappa is copied at forward time; buffers are device pointers of ctx's size.
+ * In 3D the forward call also evaluates kappa at every element's Gauss points
+ * ((p+1)^3 doubles per element, as adsg_kappa_points) and every element pass
+ * reads those values; where that memory cannot be had at creation, the passes
+ * interpolate the coefficients instead, with the same results bit for bit. */
 typedef struct adsg_adjoint adsg_adjoint;
 int adsg_adjoint_create(adsg_ctx* ctx, int nsteps, double dt, int checkpoint_every, adsg_adjoint** out);
 int adsg_adjoint_destroy(adsg_adjoint* a);

@@ -94,8 +94,21 @@ def test_adjoint_and_gauss_point_space_under_each_allocation_failure(cuda):
     dims = [ads.Dimension(2, 10), ads.Dimension(2, 12), ads.Dimension(2, 9)]
     ctx = ads.Context(dims)
     failed, absorbed, adj = _under_each_failure(lambda: ads.Adjoint(ctx, 6, 1e-6))
-    assert failed >= 5 and not absorbed
-    adj.close()
+    # one failure is absorbed: kappa at the Gauss points, without which the
+    # passes interpolate the coefficients (the same gradients, bit for bit)
+    assert failed >= 5 and len(absorbed) == 1
+    u0 = torch.from_numpy(np.random.default_rng(8).uniform(-1, 1, ctx.size)).cuda()
+    kap = torch.from_numpy(1.0 + 0.3 * np.random.default_rng(9).uniform(-1, 1, ctx.size)).cuda()
+    res = []
+    for a in (adj, absorbed[0]):
+        uT, gu, gk = torch.empty_like(u0), torch.empty_like(u0), torch.empty_like(u0)
+        a.forward(u0, kap, uT)
+        a.backward(uT, gu, gk)
+        ctx.synchronize()
+        res.append((uT.clone(), gu.clone(), gk.clone()))
+        a.close()
+    for x, y in zip(*res):
+        assert torch.equal(x, y)
     # the Gauss-point work space, taken on first use
     E, q = (10, 12, 9), 3
     u = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, ctx.size)).cuda()
