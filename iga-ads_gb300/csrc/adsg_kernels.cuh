@@ -240,9 +240,10 @@ struct field_set {
 cudaError_t launch_quad_wdiff(const field_set& F, const dim_dev* dims, int ndim, long long total, double* partial,
                               double* out, cudaStream_t s);
 
-// kappa at every Gauss point of every element of a 3D grid (element-major,
-// kappa_points_count doubles), and the kappa RHS from those values: bitwise
-// launch_rhs_elem with the coefficients
+// kappa at every Gauss point of every element of a 3D grid
+// (kappa_points_count doubles, by element colour in the element kernel's
+// launch order), and the kappa RHS from those values: bitwise launch_rhs_elem
+// with the coefficients
 long long kappa_points_count(int ndim, const dim_dev* dims);
 cudaError_t launch_kappa_points(const dim_dev* dims, const double* kappa, double* kq, cudaStream_t s);
 cudaError_t launch_rhs_elem_points(const dim_dev* dims, const double* u_prev, const double* kq, double* rhs,

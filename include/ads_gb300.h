@@ -114,10 +114,10 @@ int adsg_heat_rhs_elem(adsg_ctx* ctx, const double* u_prev_dev, const double* ka
 
 /* For many right-hand sides with one kappa field (a time loop, the adjoint),
  * 3D contexts: adsg_kappa_points evaluates the field at every element's Gauss
- * points once, into kq_dev (adsg_kappa_points_count doubles, element-major:
- * kq[(ex + Ex (ey + Ey ez)) Q^3 + qx + Q (qy + Q qz)]), and
- * adsg_heat_rhs_elem_points takes those values instead of interpolating the
- * coefficients on every call.  The values are the ones adsg_heat_rhs_elem
+ * points once, into kq_dev (adsg_kappa_points_count doubles, (p+1)^3 per
+ * element, in the element kernel's own order: by element colour, so that a
+ * warp's elements are contiguous), and adsg_heat_rhs_elem_points takes those
+ * values instead of interpolating the coefficients on every call.  The values are the ones adsg_heat_rhs_elem
  * interpolates, bit for bit, so both give the same rhs.  count: 0 for a 2D
  * context (ADSG_ERR_UNSUPPORTED from the other two). */
 long long adsg_kappa_points_count(const adsg_ctx* ctx);
