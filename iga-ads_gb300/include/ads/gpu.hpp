@@ -23,6 +23,7 @@
 
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../../include/ads_gb300.h"
@@ -130,6 +131,23 @@ public:
         check(adsg_heat_step(ctx_, u_prev, u_next, dt));
     }
     void heat_steps_dev(double* u, double dt, int nsteps) { check(adsg_heat_steps(ctx_, u, dt, nsteps)); }
+    // the element-wise RHS with a diffusion field kappa (spline coefficients;
+    // nullptr: kappa = 1), and with kappa evaluated once at the Gauss points
+    // (3D; kappa_points_count() doubles) for many right-hand sides
+    void compute_rhs_kappa_dev(const double* u_prev, const double* kappa, double* rhs, double dt) {
+        check(adsg_heat_rhs_elem(ctx_, u_prev, kappa, rhs, dt));
+    }
+    long long kappa_points_count() const { return adsg_kappa_points_count(ctx_); }
+    void kappa_points_dev(const double* kappa, double* kq) { check(adsg_kappa_points(ctx_, kappa, kq)); }
+    void compute_rhs_kappa_points_dev(const double* u_prev, const double* kq, double* rhs, double dt) {
+        check(adsg_heat_rhs_elem_points(ctx_, u_prev, kq, rhs, dt));
+    }
+    // L = (u - target)^T M (u - target) and dL/du = 2 M (u - target)
+    double mass_loss_dev(const double* u, const double* target, double* scratch, double* grad) {
+        double loss = 0.0;
+        check(adsg_mass_loss(ctx_, u, target, scratch, &loss, grad));
+        return loss;
+    }
     void synchronize() { check(adsg_ctx_synchronize(ctx_)); }
 
 private:
@@ -137,6 +155,36 @@ private:
         if (n != adsg_ctx_size(ctx_)) throw std::invalid_argument("ads::gpu: tensor size does not match the context");
     }
     adsg_ctx* ctx_ = nullptr;
+};
+
+// Reverse mode of the kappa-weighted explicit run u_{k+1} = M^-1 R(kappa) u_k
+// (adsg_adjoint_*): the C++ counterpart of a torch.autograd.Function.
+// forward() runs nsteps from u0 keeping checkpoints (every ceil(sqrt(nsteps))
+// steps unless checkpoint_every says otherwise; 1 keeps every state) and
+// returns u(T); backward() takes dL/du(T) and returns dL/du0 and dL/dkappa.
+// Device buffers of the context's size.
+class adjoint {
+public:
+    adjoint(context& ctx, int nsteps, double dt, int checkpoint_every = 0) {
+        check(adsg_adjoint_create(ctx.handle(), nsteps, dt, checkpoint_every, &a_));
+    }
+    adjoint(const adjoint&) = delete;
+    adjoint& operator=(const adjoint&) = delete;
+    ~adjoint() { adsg_adjoint_destroy(a_); }
+
+    void forward(const double* u0, const double* kappa, double* uT) { check(adsg_adjoint_forward(a_, u0, kappa, uT)); }
+    void backward(const double* dL_duT, double* grad_u0, double* grad_kappa) {
+        check(adsg_adjoint_backward(a_, dL_duT, grad_u0, grad_kappa));
+    }
+    // (steps between checkpoints, checkpoints kept)
+    std::pair<int, int> checkpoints() const {
+        int every = 0, count = 0;
+        check(adsg_adjoint_checkpoints(a_, &every, &count));
+        return {every, count};
+    }
+
+private:
+    adsg_adjoint* a_ = nullptr;
 };
 
 // ads_solve(rhs, buf, dims...) of the reference with a GPU context in place

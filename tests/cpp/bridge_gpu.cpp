@@ -14,10 +14,13 @@
 // fixtures), and the bridge's compute_rhs_heat, solve and heat_steps are
 // checked against the oracle's step.  Test code: prints "ok" when every
 // check holds, the errors either way.
+#include <cuda_runtime.h>
+
 #include <cmath>
 #include <cstdio>
 #include <memory>
 #include <random>
+#include <string>
 #include <vector>
 
 #include "ads/gpu.hpp"
@@ -154,6 +157,71 @@ static bool run_case(const char* name, const orc_problem* pr, double dt, int nst
     return ok;
 }
 
+// The reverse-mode class on device buffers: the dot-product identity of the
+// linear map u0 -> u(T) and central differences of the mass-norm loss along a
+// seeded direction in u0 (the loss is quadratic in u0, so the difference is
+// exact up to rounding).
+template <typename... Dims>
+static bool run_adjoint(const char* name, const Dims&... dims) {
+    ads::gpu::context gpu{dims...};
+    const long long n = gpu.size();
+    const size_t bytes = sizeof(double) * static_cast<size_t>(n);
+    std::mt19937_64 gen(7);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    auto host = [&](double lo, double scale) {
+        std::vector<double> v(n);
+        for (auto& x : v) x = lo + scale * U(gen);
+        return v;
+    };
+    const std::vector<double> u0 = host(0.0, 1.0), kap = host(1.0, 0.3), tgt = host(0.0, 1.0), x = host(0.0, 1.0),
+                              y = host(0.0, 1.0), d = host(0.0, 1.0);
+    double* buf[10];
+    for (auto& b : buf)
+        if (cudaMalloc(&b, bytes) != cudaSuccess) return false;
+    double *du0 = buf[0], *dk = buf[1], *dt_ = buf[2], *uT = buf[3], *gu = buf[4], *gk = buf[5], *sc = buf[6],
+           *dL = buf[7], *dx = buf[8], *dy = buf[9];
+    cudaMemcpy(du0, u0.data(), bytes, cudaMemcpyHostToDevice);
+    cudaMemcpy(dk, kap.data(), bytes, cudaMemcpyHostToDevice);
+    cudaMemcpy(dt_, tgt.data(), bytes, cudaMemcpyHostToDevice);
+    cudaMemcpy(dx, x.data(), bytes, cudaMemcpyHostToDevice);
+    cudaMemcpy(dy, y.data(), bytes, cudaMemcpyHostToDevice);
+    ads::gpu::adjoint adj(gpu, 4, 1e-5);
+    auto dot = [&](const double* a, const std::vector<double>& b) {
+        std::vector<double> h(n);
+        cudaMemcpy(h.data(), a, bytes, cudaMemcpyDeviceToHost);
+        double s = 0;
+        for (long long i = 0; i < n; ++i) s += h[i] * b[i];
+        return s;
+    };
+    // <A x, y> against <x, A^T y>
+    adj.forward(dx, dk, uT);
+    const double lhs = dot(uT, y);
+    adj.backward(dy, gu, gk);
+    const double rhs = dot(gu, x);
+    bool ok = report((std::string(name) + " adjoint dot-product identity").c_str(),
+                     std::fabs(lhs - rhs) / std::fmax(std::fabs(lhs), std::fabs(rhs)), 1e-12);
+    // dL/du0 . d against central differences of the loss
+    adj.forward(du0, dk, uT);
+    gpu.mass_loss_dev(uT, dt_, sc, dL);
+    adj.backward(dL, gu, gk);
+    const double an = dot(gu, d);
+    const double h = 1e-4;
+    auto loss_at = [&](double s) {
+        std::vector<double> v(u0);
+        for (long long i = 0; i < n; ++i) v[i] += s * d[i];
+        cudaMemcpy(dx, v.data(), bytes, cudaMemcpyHostToDevice);
+        adj.forward(dx, dk, uT);
+        return gpu.mass_loss_dev(uT, dt_, sc, dL);
+    };
+    const double num = (loss_at(h) - loss_at(-h)) / (2 * h);
+    ok &= report((std::string(name) + " adjoint dL/du0 against central differences").c_str(),
+                 std::fabs(num - an) / std::fmax(std::fabs(num), std::fabs(an)), 1e-7);
+    const auto ck = adj.checkpoints();
+    ok &= ck.first == 2 && ck.second == 2;  // ceil(sqrt(4)) steps apart, 2 kept
+    for (auto b : buf) cudaFree(b);
+    return ok;
+}
+
 int main() {
     bool ok = true;
     {
@@ -163,6 +231,7 @@ int main() {
         auto y = standin::from_oracle(pr, 1, p[1], E[1]);
         auto z = standin::from_oracle(pr, 2, p[2], E[2]);
         ok &= run_case("3D p=2 20x16x12", pr, 1e-5, 4, *x, *y, *z);
+        ok &= run_adjoint("3D p=2 20x16x12", *x, *y, *z);
         orc_problem_destroy(pr);
     }
     {

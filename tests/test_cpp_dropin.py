@@ -8,6 +8,7 @@ the reference test's 3D known-answer ADS system on the GPU."""
 from __future__ import annotations
 
 import os
+import shutil
 import subprocess
 
 import pytest
@@ -59,10 +60,17 @@ def _build_bridge(tmp_path):
     exe = str(tmp_path / "bridge_gpu")
     lib_dir = os.path.join(ROOT, "iga-ads_gb300", "ads_gb300")
     orc_dir = os.path.join(ROOT, "oracle", "_build")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    cuda_lib = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"),
+                                 os.path.join(cuda, "targets", "sbsa-linux", "lib"),
+                                 os.path.join(cuda, "targets", "x86_64-linux", "lib"))
+                     if os.path.exists(os.path.join(d, "libcudart.so"))), os.path.join(cuda, "lib64"))
     cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "iga-ads_gb300", "include"), "-I",
-           os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "oracle"), "-o", exe,
-           os.path.join(ROOT, "tests", "cpp", "bridge_gpu.cpp"), os.path.join(lib_dir, "libads_gb300.so"),
-           os.path.join(orc_dir, "libads_oracle.so"), f"-Wl,-rpath,{lib_dir}", f"-Wl,-rpath,{orc_dir}"]
+           os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "oracle"), "-I", os.path.join(cuda, "include"),
+           "-o", exe, os.path.join(ROOT, "tests", "cpp", "bridge_gpu.cpp"), os.path.join(lib_dir, "libads_gb300.so"),
+           os.path.join(orc_dir, "libads_oracle.so"), "-L", cuda_lib, "-lcudart", f"-Wl,-rpath,{lib_dir}",
+           f"-Wl,-rpath,{orc_dir}", f"-Wl,-rpath,{cuda_lib}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
     return exe
@@ -76,7 +84,9 @@ def test_bridge_program_compiles(tmp_path):
 def test_bridge_on_gpu_against_oracle(tmp_path, cuda):
     """ads::gpu::context built from reference-shaped dimensions runs
     compute_rhs_heat, solve and heat_steps on the GPU; each matches the
-    oracle (the program prints every error and its bound)."""
+    oracle.  ads::gpu::adjoint (the C++ reverse-mode class) passes the
+    dot-product identity and central differences of the mass-norm loss (the
+    program prints every error and its bound)."""
     exe = _build_bridge(tmp_path)
     out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     print(out.stdout)
